@@ -1,0 +1,291 @@
+"""Python face of the CPU oracle (test infrastructure only).
+
+The oracle restates the reference's algorithm on the CPU in FP64:
+
+* :func:`kantorovich` -- ``MA::kantorovich`` (include/MA/kantorovich.hpp:35-141)
+  plus the moments of ``first_moment`` / ``second_moment`` (include/MA/lloyd.hpp:30-123),
+  computed by ``ma_oracle.c``;
+* :func:`ot_solve` -- ``MA::ot_solve`` (include/MA/optimal_transport.hpp:89-193) with
+  ``solve_laplacian_matrix`` (optimal_transport.hpp:41-87) done by a direct sparse
+  factorisation of the Hessian with its last row and column removed;
+* :func:`lloyd` -- ``MA::lloyd`` (lloyd.hpp:126-144).
+
+Only the test-suite, the smoke check and the CPU-baseline leg of the benchmark
+import this module.  Its results are pinned by the exact-arithmetic fixtures in
+``tests/golden`` and by the invariants the reference's own drivers print
+(total area, mass conservation, finite-difference consistency).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+import build as _build  # noqa: E402
+
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_long)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        L.ora_kantorovich.restype = ctypes.c_void_p
+        L.ora_kantorovich.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, ctypes.c_int,
+                                      _dp, _dp, _dp, ctypes.c_int, ctypes.c_int]
+        for name in ("ora_value", "ora_total_mass", "ora_total_area"):
+            getattr(L, name).restype = ctypes.c_double
+            getattr(L, name).argtypes = [ctypes.c_void_p]
+        for name in ("ora_nnz", "ora_npieces", "ora_neighbor_count"):
+            getattr(L, name).restype = ctypes.c_long
+            getattr(L, name).argtypes = [ctypes.c_void_p]
+        L.ora_masses.argtypes = [ctypes.c_void_p, _dp]
+        L.ora_moments.argtypes = [ctypes.c_void_p, _dp]
+        L.ora_hessian.argtypes = [ctypes.c_void_p, _ip, _ip, _dp]
+        L.ora_pieces.argtypes = [ctypes.c_void_p, _ip, _ip, _ip]
+        L.ora_piece_vertices.restype = ctypes.c_long
+        L.ora_piece_vertices.argtypes = [ctypes.c_void_p, _dp, _ip]
+        L.ora_neighbors.argtypes = [ctypes.c_void_p, _ip, _ip]
+        L.ora_pred_stats.argtypes = [ctypes.c_void_p, _lp]
+        L.ora_free.argtypes = [ctypes.c_void_p]
+        L.ora_set_threads.argtypes = [ctypes.c_int]
+        L.ora_max_threads.restype = ctypes.c_int
+        L.ora_side1.restype = ctypes.c_int
+        L.ora_side1.argtypes = [_dp, _dp, ctypes.c_double, ctypes.c_double]
+        L.ora_side2.restype = ctypes.c_int
+        L.ora_side2.argtypes = [_dp, _dp, _dp, _dp]
+        L.ora_side3.restype = ctypes.c_int
+        L.ora_side3.argtypes = [_dp, _dp, _dp, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(_ip)
+
+
+@dataclass
+class Pieces:
+    face: np.ndarray
+    site: np.ndarray
+    nvert: np.ndarray
+    offsets: np.ndarray
+    xy: np.ndarray       # (sum nvert, 2) polygon vertices, kantorovich.hpp:95-102 order
+    label: np.ndarray    # edge label: site index of an EDGE_DT edge, -1 for a mesh edge
+
+
+@dataclass
+class KResult:
+    value: float
+    g: np.ndarray          # cell masses (the gradient of kantorovich.hpp)
+    moments: np.ndarray    # (N, 6): rho, rho x, rho y, rho x^2, rho y^2, rho xy
+    rows: np.ndarray
+    cols: np.ndarray
+    vals: np.ndarray
+    total_mass: float
+    total_area: float
+    neighbors: list
+    filter_calls: int
+    exact_calls: int
+    pieces: Pieces | None = None
+
+    @property
+    def n(self):
+        return self.g.shape[0]
+
+    def hessian(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.vals, (self.rows, self.cols)), shape=(self.n, self.n))
+
+
+def set_threads(n: int) -> None:
+    lib().ora_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().ora_max_threads())
+
+
+def kantorovich(mesh, x, y, w, mode: int = 1, keep_pieces: bool = False) -> KResult:
+    """One evaluation of ``MA::kantorovich`` (+ moments) on the CPU.
+
+    ``mode=0`` runs the reference's global flood fill on one thread
+    (voronoi_triangulation_intersection.hpp:219-313); ``mode=1`` finds the same
+    pieces triangle by triangle on all OpenMP threads.  Both give identical bits.
+    """
+    L = lib()
+    m = mesh.explicit()
+    vx, pvx = _d(m.vx)
+    vy, pvy = _d(m.vy)
+    vv, pvv = _d(m.values)
+    tri, ptri = _i(m.tri)
+    x, px = _d(x)
+    y, py = _d(y)
+    w, pw = _d(w)
+    n = x.shape[0]
+    h = L.ora_kantorovich(m.nv, pvx, pvy, pvv, m.nt, ptri, n, px, py, pw, int(mode), int(keep_pieces))
+    if not h:
+        raise RuntimeError("oracle failed")
+    try:
+        g = np.zeros(n)
+        L.ora_masses(h, g.ctypes.data_as(_dp))
+        mom = np.zeros((n, 6))
+        L.ora_moments(h, mom.ctypes.data_as(_dp))
+        nnz = L.ora_nnz(h)
+        rows = np.zeros(nnz, np.int32)
+        cols = np.zeros(nnz, np.int32)
+        vals = np.zeros(nnz)
+        L.ora_hessian(h, rows.ctypes.data_as(_ip), cols.ctypes.data_as(_ip), vals.ctypes.data_as(_dp))
+        nc = L.ora_neighbor_count(h)
+        start = np.zeros(n + 1, np.int32)
+        lst = np.zeros(max(nc, 1), np.int32)
+        L.ora_neighbors(h, start.ctypes.data_as(_ip), lst.ctypes.data_as(_ip))
+        nbrs = [lst[start[i]:start[i + 1]].copy() for i in range(n)]
+        st = np.zeros(2, np.int64)
+        L.ora_pred_stats(h, st.ctypes.data_as(_lp))
+        pieces = None
+        np_ = L.ora_npieces(h)
+        if keep_pieces:
+            face = np.zeros(np_, np.int32)
+            site = np.zeros(np_, np.int32)
+            nvert = np.zeros(np_, np.int32)
+            L.ora_pieces(h, face.ctypes.data_as(_ip), site.ctypes.data_as(_ip), nvert.ctypes.data_as(_ip))
+            tot = int(nvert.sum())
+            xy = np.zeros((max(tot, 1), 2))
+            lab = np.zeros(max(tot, 1), np.int32)
+            L.ora_piece_vertices(h, xy.ctypes.data_as(_dp), lab.ctypes.data_as(_ip))
+            off = np.zeros(np_ + 1, np.int64)
+            off[1:] = np.cumsum(nvert)
+            pieces = Pieces(face, site, nvert, off, xy[:tot], lab[:tot])
+        return KResult(L.ora_value(h), g, mom, rows, cols, vals, L.ora_total_mass(h),
+                       L.ora_total_area(h), nbrs, int(st[0]), int(st[1]), pieces)
+    finally:
+        L.ora_free(h)
+
+
+def side1(v, w, e):
+    L = lib()
+    return bool(L.ora_side1(_d(v)[1], _d(w)[1], float(e[0]), float(e[1])))
+
+
+def side2(v, a, b, w):
+    L = lib()
+    arrs = [np.ascontiguousarray(t, dtype=np.float64) for t in (v, a, b, w)]
+    return bool(L.ora_side2(*[t.ctypes.data_as(_dp) for t in arrs]))
+
+
+def side3(v, u, p, q, w):
+    L = lib()
+    arrs = [np.ascontiguousarray(t, dtype=np.float64) for t in (v, u, p, q, w)]
+    return bool(L.ora_side3(*[t.ctypes.data_as(_dp) for t in arrs]))
+
+
+# --------------------------------------------------------------------------- #
+# the damped Newton solve (optimal_transport.hpp:41-193)                      #
+# --------------------------------------------------------------------------- #
+
+class EmptyCellError(RuntimeError):
+    pass
+
+
+@dataclass
+class SolveResult:
+    w: np.ndarray
+    m: np.ndarray
+    niter: int
+    neval: int
+    value: float
+    grad_norm: float
+    max_rel_err: float
+    history: list
+
+
+def solve_laplacian_matrix(h, g):
+    """optimal_transport.hpp:41-87: drop the last row and column, factorise, set
+    d[N-1] = 0.  The reference factorises with Eigen's SimplicialLLT; a sparse LU
+    of the same symmetric positive-definite block gives the same direction."""
+    import scipy.sparse.linalg as spla
+    n = g.shape[0]
+    d = np.zeros(n)
+    if n == 1:
+        return d
+    hs = h[: n - 1, : n - 1].tocsc()
+    d[: n - 1] = spla.splu(hs).solve(g[: n - 1])
+    return d
+
+
+def ot_solve(mesh, x, y, nu, w=None, eps_g: float = 1e-7, maxiter: int = 100,
+             tol_rel: float | None = None, mode: int = 1, verbose: bool = False) -> SolveResult:
+    """``MA::ot_solve`` restated.  The stop rule is the reference's
+    ``|m - nu|_2 < eps_g`` unless ``tol_rel`` is given, in which case it is
+    ``max_i |m_i - nu_i| / nu_i <= tol_rel``."""
+    nu = np.asarray(nu, dtype=np.float64)
+    n = nu.shape[0]
+    w = np.zeros(n) if w is None or len(w) != n else np.array(w, dtype=np.float64)
+    stats = {"neval": 0}
+    history = []
+
+    def f(wv):
+        stats["neval"] += 1
+        r = kantorovich(mesh, x, y, wv, mode=mode)
+        m = r.g
+        g = m - nu
+        return r.value - nu @ wv, m, g, r.hessian()
+
+    def converged(g):
+        if tol_rel is not None:
+            return np.max(np.abs(g) / nu) <= tol_rel
+        return np.linalg.norm(g) < eps_g
+
+    fx, m, g, h = f(w)
+    eps0 = min(m.min(), nu.min()) / 2.0
+    if eps0 <= 0:
+        raise EmptyCellError(f"cell {int(np.argmin(m))} is empty")
+    niter = 0
+    while not converged(g):
+        if niter > maxiter:
+            break
+        niter += 1
+        d = -solve_laplacian_matrix(h, g)
+        alpha = 1.0
+        w0 = w.copy()
+        n0 = np.linalg.norm(g)
+        while True:
+            w = w0 + alpha * d
+            fx, m, g, h = f(w)
+            if m.min() >= eps0 and np.linalg.norm(g) <= (1.0 - alpha / 2.0) * n0:
+                break
+            alpha *= 0.5
+            if alpha < 2.0 ** -40:
+                raise RuntimeError("line search failed")
+        history.append((niter, fx, float(np.linalg.norm(g)), alpha, stats["neval"]))
+        if verbose:
+            print(f"it {niter}: f={fx} |df|={np.linalg.norm(g)} tau={alpha} eval={stats['neval']}")
+    return SolveResult(w, m, niter, stats["neval"], fx, float(np.linalg.norm(g)),
+                       float(np.max(np.abs(m - nu) / nu)), history)
+
+
+def lloyd(mesh, x, y, w, mode: int = 1):
+    """lloyd.hpp:126-144: masses and centroids (first moments / mass)."""
+    r = kantorovich(mesh, x, y, w, mode=mode)
+    m = r.moments[:, 0]
+    c = r.moments[:, 1:3] / m[:, None]
+    return m, c

@@ -1,0 +1,207 @@
+"""The CPU oracle, pinned before anything is compared with it.
+
+Pins, in order of strength:
+* exact-rational golden fixtures (tests/golden/make_golden.py): pieces, adjacency,
+  value, masses, moments and Hessian;
+* the invariants the reference's drivers print: total area of the pieces
+  (tests/test_voronoi_tri.cpp:67, tests/test_voronoi.cpp:50, tests/test_power.cpp:51),
+  conservation of mass (tests/test_quantization.cpp:78-79), and finite-difference
+  consistency of the gradient and Hessian (tests/test_opttransport_eval.cpp:20-55);
+* the regular-triangulation adjacency recomputed independently from scipy's qhull
+  (power diagram = lower convex hull of the lifted sites);
+* the exact predicates against rational arithmetic on near-degenerate inputs.
+"""
+from fractions import Fraction as Fr
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, hessian_dict, load_golden
+from mongeampere_gb300 import workloads as W
+from mongeampere_gb300.mesh import GridMesh, unit_grid
+
+
+@pytest.mark.parametrize("name", golden_cases())
+@pytest.mark.parametrize("mode", [0, 1])
+def test_oracle_matches_exact_golden(oracle, name, mode):
+    d = load_golden(name)
+    r = oracle.kantorovich(d["mesh_obj"], d["x"], d["y"], d["w"], mode=mode, keep_pieces=True)
+    gs = max(1.0, np.abs(d["g"]).max())
+    assert abs(r.value - d["value"]) <= 1e-14 * gs
+    np.testing.assert_allclose(r.g, d["g"], rtol=0, atol=1e-14 * gs)
+    np.testing.assert_allclose(r.moments, d["moments"], rtol=0, atol=1e-14 * gs)
+    H = {(i, j): v for i, j, v in d["hessian"]}
+    Ho = hessian_dict(r.rows, r.cols, r.vals)
+    assert set(H) == set(Ho), "adjacency differs from the exact pieces"
+    hs = max([abs(v) for v in H.values()] + [1.0])
+    for k, v in H.items():
+        assert abs(Ho[k] - v) <= 1e-13 * hs
+    got = sorted(zip(r.pieces.face.tolist(), r.pieces.site.tolist(), r.pieces.nvert.tolist()))
+    assert got == sorted(tuple(p) for p in d["pieces"])
+
+
+def test_flood_fill_modes_identical(oracle):
+    p = W.make_problem(16, 200, seed=3)
+    w = np.random.default_rng(1).uniform(-1e-3, 1e-3, p.n)
+    a = oracle.kantorovich(p.mesh, p.x, p.y, w, mode=0)
+    b = oracle.kantorovich(p.mesh, p.x, p.y, w, mode=1)
+    assert a.value == b.value
+    assert np.array_equal(a.g, b.g)
+    assert np.array_equal(a.vals, b.vals) and np.array_equal(a.cols, b.cols)
+
+
+def test_total_area_and_mass(oracle):
+    # tests/test_voronoi_tri.cpp:67 (sum of piece areas), test_quantization.cpp:78 (mass)
+    p = W.make_problem(32, 500, seed=5)
+    r = oracle.kantorovich(p.mesh, p.x, p.y, p.w0)
+    assert abs(r.total_area - 1.0) < 1e-12
+    assert abs(r.g.sum() - p.mesh.total_mass()) < 1e-12
+    # the Hessian is a graph Laplacian: rows sum to zero, symmetric
+    H = r.hessian()
+    assert np.abs(np.asarray(H.sum(axis=1))).max() < 1e-12
+    assert abs(H - H.T).max() < 1e-13
+
+
+def test_voronoi_of_square_has_area_four(oracle):
+    # tests/test_voronoi.cpp:25-51: 10k Voronoi cells of [-1, 1]^2 have total area 4
+    g = np.array([-1.0, 0.0, 1.0])
+    mesh = GridMesh(g, g, np.ones(9))
+    rng = np.random.default_rng(0)
+    pts = rng.uniform(-1, 1, (5000, 2))
+    r = oracle.kantorovich(mesh, pts[:, 0], pts[:, 1], np.zeros(5000))
+    assert abs(r.total_area - 4.0) < 1e-11
+    assert abs(r.g.sum() - 4.0) < 1e-11
+
+
+def test_fd_gradient_and_hessian(oracle):
+    # the method of tests/test_opttransport_eval.cpp:20-55 (central differences,
+    # eps = 1e-5) on 50 sites
+    p = W.make_problem(24, 50, seed=11)
+    rng = np.random.default_rng(2)
+    w = rng.uniform(-2e-3, 2e-3, p.n)
+    r = oracle.kantorovich(p.mesh, p.x, p.y, w)
+    H = r.hessian().toarray()
+    eps = 1e-5
+    gfd = np.zeros(p.n)
+    hfd = np.zeros((p.n, p.n))
+    for i in range(p.n):
+        wp, wm = w.copy(), w.copy()
+        wp[i] += eps
+        wm[i] -= eps
+        rp = oracle.kantorovich(p.mesh, p.x, p.y, wp)
+        rm = oracle.kantorovich(p.mesh, p.x, p.y, wm)
+        gfd[i] = (rp.value - rm.value) / (2 * eps)
+        hfd[i] = (rp.g - rm.g) / (2 * eps)
+    assert np.linalg.norm(gfd - r.g) < 1e-5 * np.linalg.norm(r.g)
+    assert np.linalg.norm(hfd - H) < 1e-3 * np.linalg.norm(H)
+
+
+def _lower_hull_edges(x, y, w):
+    from scipy.spatial import ConvexHull
+    pts = np.c_[x, y, x * x + y * y - w]
+    hull = ConvexHull(pts)
+    edges = set()
+    for simplex, eq in zip(hull.simplices, hull.equations):
+        if eq[2] < -1e-12:
+            a, b, c = sorted(int(v) for v in simplex)
+            edges |= {(a, b), (a, c), (b, c)}
+    return edges
+
+
+def test_adjacency_vs_qhull(oracle):
+    # independent cross-check of the (domain-restricted) regular-triangulation
+    # adjacency: every Hessian off-diagonal pair is an edge of the lower hull of the
+    # lifted sites, and every lower-hull edge whose Laguerre edge crosses the square
+    # appears in the Hessian
+    p = W.make_problem(16, 400, seed=7)
+    rng = np.random.default_rng(3)
+    w = rng.uniform(-5e-4, 5e-4, p.n)
+    r = oracle.kantorovich(p.mesh, p.x, p.y, w)
+    pairs = {(min(i, j), max(i, j)) for i, j in zip(r.rows, r.cols) if i != j}
+    rt = _lower_hull_edges(p.x, p.y, w)
+    assert pairs <= rt
+    # an RT edge whose radical axis meets the cell pair inside the square must appear:
+    # sample the midpoint of the Laguerre edge via the two cells' common points
+    missing = rt - pairs
+    for (i, j) in missing:
+        # points on the radical axis of (i, j) that are closer to i, j than to all
+        # others and inside the square would contradict the Hessian: check a fine
+        # sample of the axis
+        d = np.array([p.x[j] - p.x[i], p.y[j] - p.y[i]])
+        c = 0.5 * (np.dot(d, d) - (w[j] - w[i]))
+        base = np.array([p.x[i], p.y[i]]) + d * (c / np.dot(d, d))
+        t = np.array([-d[1], d[0]]) / np.linalg.norm(d)
+        s = np.linspace(-1.5, 1.5, 3001)
+        q = base[None, :] + s[:, None] * t[None, :]
+        inside = (q > 1e-9).all(1) & (q < 1 - 1e-9).all(1)
+        q = q[inside]
+        if q.size == 0:
+            continue
+        pw = (q[:, 0, None] - p.x[None]) ** 2 + (q[:, 1, None] - p.y[None]) ** 2 - w[None]
+        own = pw[:, i]
+        others = np.delete(pw, [i, j], axis=1).min(axis=1)
+        assert not np.any(own < others - 1e-9), f"pair {(i, j)} has a Laguerre edge inside the domain"
+
+
+def _exact_pi(v, w, e):
+    v = [Fr(t) for t in v]
+    w = [Fr(t) for t in w]
+    e = [Fr(t) for t in e]
+    return ((e[0] - v[0]) ** 2 + (e[1] - v[1]) ** 2 - v[2]) - ((e[0] - w[0]) ** 2 + (e[1] - w[1]) ** 2 - w[2])
+
+
+def test_predicates_exact_on_near_degenerate_inputs(oracle):
+    rng = np.random.default_rng(4)
+    for _ in range(300):
+        v = rng.uniform(0, 1, 3)
+        w = rng.uniform(0, 1, 3)
+        # a point on (or within a few ulps of) the radical axis of v and w
+        d = w[:2] - v[:2]
+        c = 0.5 * (d @ d - (w[2] - v[2]))
+        base = v[:2] + d * (c / (d @ d))
+        e = base + rng.uniform(-1, 1) * np.array([-d[1], d[0]])
+        e = e + rng.integers(-3, 4, 2) * np.spacing(e)
+        assert oracle.side1(v, w, e) == (_exact_pi(v, w, e) < 0)
+        # Side3: segment through e
+        pq = rng.uniform(-1, 1, 2)
+        p_, q_ = e - pq, e + pq * rng.uniform(0.5, 2)
+        u = rng.uniform(0, 1, 3)
+        A = lambda x: _exact_pi(v, u, x)
+        B = lambda x: _exact_pi(v, w, x)
+        den = A(p_) - A(q_)
+        if den != 0:
+            want = (A(p_) * B(q_) - A(q_) * B(p_)) / den < 0
+            assert oracle.side3(v, u, p_, q_, w) == want
+    # Side2 on co-circular configurations (exact ties must be "outside") and
+    # perturbations of them
+    for _ in range(200):
+        cx, cy, R = rng.uniform(0.3, 0.7), rng.uniform(0.3, 0.7), rng.uniform(0.05, 0.2)
+        ang = np.sort(rng.uniform(0, 2 * np.pi, 4))
+        P = [np.array([cx + R * np.cos(a), cy + R * np.sin(a), 0.0]) for a in ang]
+        P[3][:2] += rng.integers(-2, 3, 2) * np.spacing(P[3][:2])
+        v, a, b, w = P
+        Fv, Fa, Fb, Fw = ([Fr(t) for t in q] for q in (v, a, b, w))
+        d = lambda q: (q[0] - Fv[0], q[1] - Fv[1], (q[0] - Fv[0]) ** 2 + (q[1] - Fv[1]) ** 2 - (q[2] - Fv[2]))
+        da, db, dw = d(Fa), d(Fb), d(Fw)
+        D = da[0] * db[1] - da[1] * db[0]
+        M = dw[0] * (da[2] * db[1] - db[2] * da[1]) + dw[1] * (da[0] * db[2] - db[0] * da[2]) - dw[2] * D
+        want = D != 0 and (M / D) < 0
+        assert oracle.side2(v, a, b, w) == want
+
+
+def test_ot_solve_reference_semantics(oracle):
+    p = W.make_problem(24, 150, seed=2)
+    s = oracle.ot_solve(p.mesh, p.x, p.y, p.nu, tol_rel=1e-10)
+    assert s.max_rel_err <= 1e-10
+    assert s.w[-1] == 0.0           # gauge of solve_laplacian_matrix: d[N-1] = 0
+    assert s.niter <= 10
+
+
+def test_empty_cell_is_reported(oracle):
+    # optimal_transport.hpp:137-148: a non-positive minimum mass stops the solve
+    mesh = unit_grid(4, np.ones((4, 4)))
+    x = np.array([0.2, 0.8, 0.5])
+    y = np.array([0.5, 0.5, 0.5])
+    w = np.array([0.0, 0.0, -1.0])
+    with pytest.raises(oracle.EmptyCellError):
+        oracle.ot_solve(mesh, x, y, np.full(3, 1 / 3), w=w)
