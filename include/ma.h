@@ -1,0 +1,154 @@
+/*
+ * ma.h -- C ABI of the GB300 semi-discrete optimal-transport engine.
+ *
+ * Drop-in boundary for the hot path of MongeAmpere++ (mrgt/MongeAmpere).  Each
+ * entry point below replaces one header-only C++ template of the reference and
+ * keeps its argument meaning:
+ *
+ *   ma_kantorovich     MA::kantorovich               include/MA/kantorovich.hpp:35-141
+ *   ma_hessian_copy    the SparseMatrix h it fills    include/MA/kantorovich.hpp:137-139
+ *   ma_ot_solve        MA::ot_solve + Statistics      include/MA/optimal_transport.hpp:35-39, 89-193
+ *   ma_laplacian_solve MA::solve_laplacian_matrix     include/MA/optimal_transport.hpp:41-87
+ *   ma_moments         MA::first_moment / second_moment  include/MA/lloyd.hpp:30-123
+ *   ma_lloyd           MA::lloyd                      include/MA/lloyd.hpp:126-144
+ *   ma_pieces          MA::voronoi_triangulation_intersection
+ *                                                     include/MA/voronoi_triangulation_intersection.hpp:315-343
+ *   ma_mesh_create_*   the density: a triangulation plus one linear function per
+ *                      face (include/MA/functions.hpp:55-120,
+ *                      include/CGAL/Triangulation_incremental_builder_2.h:27-80)
+ *
+ * Conventions
+ *   - Sites are passed as two arrays x[n], y[n]: for the reference's N x 2
+ *     column-major Eigen matrix X, x = X.data() and y = X.data() + N.
+ *   - Every pointer argument is caller-owned; `mem` says whether the arrays live in
+ *     host memory (MA_MEM_HOST, copied through the context's pinned staging) or in
+ *     device memory of the context's GPU (MA_MEM_DEVICE, used in place).
+ *   - Every call returns an ma_status; the reference reports errors only through
+ *     assert() and stderr (optimal_transport.hpp:49-58, 137-148).
+ *   - A context owns one CUDA stream and all scratch memory.  Calls on one context
+ *     must not overlap; separate contexts may be used from separate threads.
+ */
+#ifndef MA_H
+#define MA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ma_status {
+    MA_OK = 0,
+    MA_ERR_INVALID_ARGUMENT = 1,
+    MA_ERR_NO_DEVICE = 2,       /* no CUDA device, or the device is not sm_103 */
+    MA_ERR_CUDA = 3,            /* a CUDA runtime call failed (see ma_ctx_last_error) */
+    MA_ERR_OUT_OF_MEMORY = 4,
+    MA_ERR_CAPACITY = 5,        /* a cell needed more polygon vertices than any kernel holds */
+    MA_ERR_EXACT_OVERFLOW = 6,  /* an exact predicate ran out of expansion capacity */
+    MA_EMPTY_CELL = 7,          /* ot_solve: a Laguerre cell is empty at the start
+                                   (optimal_transport.hpp:137-148) */
+    MA_LINESEARCH_FAIL = 8,     /* ot_solve: the step fell below 2^-40 */
+    MA_MAXITER = 9,             /* ot_solve: maxiter reached before the stop rule held */
+    MA_ERR_BUFFER_TOO_SMALL = 10
+} ma_status;
+
+typedef enum ma_mem { MA_MEM_HOST = 0, MA_MEM_DEVICE = 1 } ma_mem;
+
+typedef enum ma_precision {
+    MA_FP64 = 0,   /* the reference's arithmetic: FP64 integrals, exact combinatorics */
+    MA_MIXED = 1   /* FP32 geometry and integrals with compensated sums, exact combinatorics,
+                      FP64 Newton residual and refined linear solves */
+} ma_precision;
+
+typedef enum ma_stop_rule {
+    MA_STOP_GRAD_NORM = 0,   /* the reference's rule: |m - nu|_2 < eps_g (optimal_transport.hpp:150) */
+    MA_STOP_MAX_REL = 1      /* max_i |m_i - nu_i| / nu_i <= eps_g */
+} ma_stop_rule;
+
+typedef struct ma_ctx ma_ctx;
+typedef struct ma_mesh ma_mesh;
+
+/* ------------------------------------------------------------------ context */
+const char* ma_status_string(ma_status s);
+ma_status ma_ctx_create(int device, ma_ctx** out);
+void ma_ctx_destroy(ma_ctx* ctx);
+/* Use `stream` (a cudaStream_t) instead of the context's own stream. */
+ma_status ma_ctx_set_stream(ma_ctx* ctx, void* stream);
+const char* ma_ctx_last_error(const ma_ctx* ctx);
+/* Number of kernel launches the context has issued since it was created. */
+int64_t ma_ctx_launch_count(const ma_ctx* ctx);
+
+/* --------------------------------------------------------------------- mesh */
+/* Tensor-product grid: vertex (i, j) at (gx[i], gy[j]) with value values[j*nx + i];
+ * square (i, j) is split along its (i,j)-(i+1,j+1) diagonal.  Host arrays. */
+ma_status ma_mesh_create_grid(ma_ctx* ctx, int nx, int ny, const double* gx, const double* gy,
+                              const double* values, ma_mesh** out);
+/* Explicit triangulation (nv vertices, nt counter-clockwise triangles).  Host arrays. */
+ma_status ma_mesh_create_triangles(ma_ctx* ctx, int nv, const double* vx, const double* vy,
+                                   const double* values, int nt, const int32_t* tri, ma_mesh** out);
+void ma_mesh_destroy(ma_mesh* mesh);
+/* Integral of the density (the value image_to_pl_function returns, functions.hpp:116-119). */
+ma_status ma_mesh_total_mass(const ma_mesh* mesh, double* out);
+
+/* -------------------------------------------------------------- kantorovich */
+/* One evaluation of MA::kantorovich: value = sum_i (w_i m_i - int_{Lag_i} rho |x - x_i|^2),
+ * g[i] = m_i = int_{Lag_i} rho, and the Hessian H (kept in the context; read it with
+ * ma_hessian_copy).  *nnz receives the number of stored Hessian entries. */
+ma_status ma_kantorovich(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
+                         const double* w, ma_mem mem, ma_precision prec, double* value, double* g,
+                         int64_t* nnz);
+/* The Hessian of the last ma_kantorovich call in CSR form: rowptr[n+1], col[nnz] (sorted,
+ * diagonal included), val[nnz].  Since H is symmetric this is also the reference's
+ * column-major SparseMatrix storage (outer = rowptr, inner = col). */
+ma_status ma_hessian_copy(ma_ctx* ctx, int32_t* rowptr, int32_t* col, double* val, ma_mem mem);
+
+/* ------------------------------------------------------------------ solver */
+typedef struct ma_solve_opts {
+    double eps_g;          /* stop threshold (reference default 1e-7) */
+    int64_t maxiter;       /* Newton iterations (reference default 100) */
+    int stop_rule;         /* ma_stop_rule */
+    int precision;         /* ma_precision */
+    int verbose;           /* print the reference's per-iteration line to stderr */
+    double cg_rtol;        /* relative residual of the preconditioned CG (0: default 1e-10) */
+    int64_t cg_maxiter;    /* CG iteration cap (0: default 20000) */
+} ma_solve_opts;
+
+typedef struct ma_stats {
+    size_t niter;                /* Statistics::niter (optimal_transport.hpp:35-39) */
+    size_t neval;                /* Statistics::neval */
+    size_t cg_iters;             /* total CG iterations */
+    size_t linesearch_halvings;
+    double grad_norm;            /* |m - nu|_2 at exit */
+    double max_rel_err;          /* max_i |m_i - nu_i| / nu_i at exit */
+    double value;                /* Kantorovich value minus <nu, w> at exit */
+    double t_eval_ms;            /* device time spent in Laguerre evaluations */
+    double t_linsolve_ms;        /* device time spent in linear solves */
+} ma_stats;
+
+void ma_solve_opts_default(ma_solve_opts* o);
+/* Damped Newton (Kitagawa-Merigot-Thibert) on m(w) = nu.  w_inout holds the initial
+ * guess on entry (pass all zeros for the reference's empty-vector start) and the
+ * solution on exit; the gauge is w[n-1] fixed, as solve_laplacian_matrix does. */
+ma_status ma_ot_solve(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
+                      const double* nu, double* w_inout, ma_mem mem, const ma_solve_opts* opts,
+                      ma_stats* stats);
+/* Newton direction of solve_laplacian_matrix: solve H[:n-1,:n-1] d = g[:n-1], d[n-1] = 0,
+ * for the Hessian of the last ma_kantorovich call.  Returns the CG iteration count in *iters. */
+ma_status ma_laplacian_solve(ma_ctx* ctx, const double* g, double* d, ma_mem mem, double rtol,
+                             int64_t maxiter, int64_t* iters);
+
+/* --------------------------------------------------------- moments / Lloyd */
+/* mass[n]; first[2n] = (int rho x, int rho y) per site; second[3n] (nullable) =
+ * (int rho x^2, int rho y^2, int rho x y) per site. */
+ma_status ma_moments(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
+                     const double* w, ma_mem mem, double* mass, double* first, double* second);
+/* mass[n] and centroids[2n] (first moments divided by mass). */
+ma_status ma_lloyd(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
+                   const double* w, ma_mem mem, double* mass, double* centroids);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MA_H */

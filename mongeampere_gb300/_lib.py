@@ -1,0 +1,106 @@
+"""ctypes binding of ``libma_gb300.so`` (the C ABI declared in ``include/ma.h``).
+
+The library is built in-tree by :func:`mongeampere_gb300.build.build`.  There is
+no fallback: if the library is missing or cannot be loaded, every entry point
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_vp = ctypes.c_void_p
+
+
+class MaSolveOpts(ctypes.Structure):
+    _fields_ = [("eps_g", ctypes.c_double), ("maxiter", ctypes.c_int64), ("stop_rule", ctypes.c_int),
+                ("precision", ctypes.c_int), ("verbose", ctypes.c_int), ("cg_rtol", ctypes.c_double),
+                ("cg_maxiter", ctypes.c_int64)]
+
+
+class MaStats(ctypes.Structure):
+    _fields_ = [("niter", ctypes.c_size_t), ("neval", ctypes.c_size_t), ("cg_iters", ctypes.c_size_t),
+                ("linesearch_halvings", ctypes.c_size_t), ("grad_norm", ctypes.c_double),
+                ("max_rel_err", ctypes.c_double), ("value", ctypes.c_double), ("t_eval_ms", ctypes.c_double),
+                ("t_linsolve_ms", ctypes.c_double)]
+
+
+# every symbol include/ma.h declares, with its ctypes signature
+SIGNATURES = {
+    "ma_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "ma_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
+    "ma_ctx_destroy": (None, [_vp]),
+    "ma_ctx_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "ma_ctx_last_error": (ctypes.c_char_p, [_vp]),
+    "ma_ctx_launch_count": (ctypes.c_int64, [_vp]),
+    "ma_mesh_create_grid": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.POINTER(_vp)]),
+    "ma_mesh_create_triangles": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip,
+                                                ctypes.POINTER(_vp)]),
+    "ma_mesh_destroy": (None, [_vp]),
+    "ma_mesh_total_mass": (ctypes.c_int, [_vp, _dp]),
+    "ma_kantorovich": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _dp,
+                                      _vp, _i64p]),
+    "ma_hessian_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
+    "ma_solve_opts_default": (None, [ctypes.POINTER(MaSolveOpts)]),
+    "ma_ot_solve": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int,
+                                   ctypes.POINTER(MaSolveOpts), ctypes.POINTER(MaStats)]),
+    "ma_laplacian_solve": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_int64, _i64p]),
+    "ma_moments": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp]),
+    "ma_lloyd": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) and return the ctypes library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ImportError(f"{path} is not built; run mongeampere_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class MaError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+MA_OK = 0
+MA_ERR_INVALID_ARGUMENT = 1
+MA_ERR_NO_DEVICE = 2
+MA_ERR_CUDA = 3
+MA_ERR_OUT_OF_MEMORY = 4
+MA_ERR_CAPACITY = 5
+MA_ERR_EXACT_OVERFLOW = 6
+MA_EMPTY_CELL = 7
+MA_LINESEARCH_FAIL = 8
+MA_MAXITER = 9
+MA_ERR_BUFFER_TOO_SMALL = 10
+
+MA_MEM_HOST = 0
+MA_MEM_DEVICE = 1
+MA_FP64 = 0
+MA_MIXED = 1
+MA_STOP_GRAD_NORM = 0
+MA_STOP_MAX_REL = 1

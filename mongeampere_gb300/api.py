@@ -1,0 +1,344 @@
+"""Python mirror of the reference's C++ API over the C ABI.
+
+Names and argument meaning follow MongeAmpere++:
+
+* :func:`kantorovich` -- ``MA::kantorovich(densityT, densityF, X, weights, g, h)``
+  (include/MA/kantorovich.hpp:35-141): returns the value, fills ``g`` (cell masses)
+  and returns the Hessian ``h`` as a CSR matrix;
+* :func:`ot_solve` -- ``MA::ot_solve(t, functions, X, masses, x, eps_g, maxiter,
+  verbose, stats)`` (include/MA/optimal_transport.hpp:89-193);
+* :func:`first_moment`, :func:`second_moment`, :func:`lloyd` --
+  include/MA/lloyd.hpp:30-144;
+* :func:`solve_laplacian_matrix` -- include/MA/optimal_transport.hpp:41-87, for the
+  Hessian of the last evaluation on the context.
+
+``X`` is an ``(N, 2)`` array (or a pair ``(x, y)``).  Arrays may be numpy arrays
+(host memory) or CUDA torch tensors (device memory, used in place).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .mesh import GridMesh, TriMesh
+
+
+def _is_device(a) -> bool:
+    return hasattr(a, "is_cuda") and bool(a.is_cuda)
+
+
+def _check(lib, ctx, st: int, what: str):
+    if st != L.MA_OK:
+        msg = lib.ma_status_string(st).decode()
+        if ctx:
+            extra = lib.ma_ctx_last_error(ctx).decode()
+            if extra:
+                msg += ": " + extra
+        raise L.MaError(st, f"{what}: {msg}")
+
+
+def _host(a, dtype=np.float64):
+    return np.ascontiguousarray(np.asarray(a, dtype=dtype))
+
+
+class Context:
+    """One CUDA stream plus the scratch memory of the engine (``ma_ctx``)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        st = self.lib.ma_ctx_create(int(device), ctypes.byref(h))
+        _check(self.lib, None, st, "ma_ctx_create")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ma_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def use_stream(self, stream_handle: int):
+        _check(self.lib, self.h, self.lib.ma_ctx_set_stream(self.h, ctypes.c_void_p(int(stream_handle))),
+               "ma_ctx_set_stream")
+
+    def use_torch_stream(self):
+        import torch
+        self.use_stream(torch.cuda.current_stream(self.device).cuda_stream)
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.ma_ctx_launch_count(self.h))
+
+    def mesh(self, mesh) -> "DeviceMesh":
+        return DeviceMesh(self, mesh)
+
+
+class DeviceMesh:
+    """A density uploaded to the device (``ma_mesh``)."""
+
+    def __init__(self, ctx: Context, mesh):
+        self.ctx = ctx
+        self.src = mesh
+        lib = ctx.lib
+        h = ctypes.c_void_p()
+        if isinstance(mesh, GridMesh):
+            gx, gy, v = _host(mesh.gx), _host(mesh.gy), _host(mesh.values.ravel())
+            st = lib.ma_mesh_create_grid(ctx.h, mesh.nx, mesh.ny, gx.ctypes.data_as(L._dp),
+                                         gy.ctypes.data_as(L._dp), v.ctypes.data_as(L._dp), ctypes.byref(h))
+        elif isinstance(mesh, TriMesh):
+            vx, vy, v = _host(mesh.vx), _host(mesh.vy), _host(mesh.values)
+            tri = _host(mesh.tri.ravel(), np.int32)
+            st = lib.ma_mesh_create_triangles(ctx.h, mesh.nv, vx.ctypes.data_as(L._dp), vy.ctypes.data_as(L._dp),
+                                              v.ctypes.data_as(L._dp), mesh.nt, tri.ctypes.data_as(L._ip),
+                                              ctypes.byref(h))
+        else:
+            raise TypeError("mesh must be a GridMesh or a TriMesh")
+        _check(lib, ctx.h, st, "ma_mesh_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.ma_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def total_mass(self) -> float:
+        out = ctypes.c_double()
+        _check(self.ctx.lib, self.ctx.h, self.ctx.lib.ma_mesh_total_mass(self.h, ctypes.byref(out)), "total_mass")
+        return out.value
+
+
+_default_ctx = None
+_mesh_cache = {}
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _dmesh(ctx: Context, mesh):
+    if isinstance(mesh, DeviceMesh):
+        return mesh
+    key = (id(ctx), id(mesh))
+    dm = _mesh_cache.get(key)
+    if dm is None or dm.src is not mesh:
+        dm = DeviceMesh(ctx, mesh)
+        _mesh_cache[key] = dm
+    return dm
+
+
+def _split_xy(X, y=None):
+    if y is not None:
+        return X, y
+    if _is_device(X):
+        return X[:, 0].contiguous(), X[:, 1].contiguous()
+    X = np.asarray(X, dtype=np.float64)
+    return np.ascontiguousarray(X[:, 0]), np.ascontiguousarray(X[:, 1])
+
+
+class _Args:
+    """Hold pointers of a call's array arguments (all host or all device)."""
+
+    def __init__(self, *arrays):
+        self.device = any(_is_device(a) for a in arrays if a is not None)
+        self.keep = []
+        self.ptrs = []
+        for a in arrays:
+            if a is None:
+                self.ptrs.append(None)
+                continue
+            if self.device:
+                import torch
+                t = a if _is_device(a) else torch.as_tensor(np.asarray(a, dtype=np.float64), device="cuda")
+                t = t.to(torch.float64).contiguous()
+                self.keep.append(t)
+                self.ptrs.append(ctypes.c_void_p(t.data_ptr()))
+            else:
+                h = _host(a)
+                self.keep.append(h)
+                self.ptrs.append(ctypes.c_void_p(h.ctypes.data))
+        self.mem = L.MA_MEM_DEVICE if self.device else L.MA_MEM_HOST
+
+    def out(self, n, like=None):
+        if self.device:
+            import torch
+            t = torch.empty(n, dtype=torch.float64, device=self.keep[0].device)
+            return t, ctypes.c_void_p(t.data_ptr())
+        h = np.empty(n, dtype=np.float64)
+        return h, ctypes.c_void_p(h.ctypes.data)
+
+
+@dataclass
+class Hessian:
+    rowptr: np.ndarray
+    col: np.ndarray
+    val: np.ndarray
+    n: int
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.val, self.col, self.rowptr), shape=(self.n, self.n))
+
+
+def kantorovich(mesh, X, weights, y=None, *, precision: str = "fp64", hessian: bool = True,
+                ctx: Context | None = None):
+    """``MA::kantorovich``: returns ``(value, g, h)`` with ``g`` the cell masses and
+    ``h`` a :class:`Hessian` (``None`` when ``hessian=False``)."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    x, yy = _split_xy(X, y)
+    a = _Args(x, yy, weights)
+    n = int(a.keep[0].shape[0])
+    g, gp = a.out(n)
+    val = ctypes.c_double()
+    nnz = ctypes.c_int64()
+    prec = L.MA_MIXED if precision == "mixed" else L.MA_FP64
+    st = ctx.lib.ma_kantorovich(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.mem, prec, ctypes.byref(val),
+                                gp, ctypes.byref(nnz))
+    _check(ctx.lib, ctx.h, st, "ma_kantorovich")
+    h = None
+    if hessian:
+        h = hessian_copy(ctx, n, int(nnz.value))
+    return val.value, g, h
+
+
+def hessian_copy(ctx: Context, n: int, nnz: int) -> Hessian:
+    rowptr = np.empty(n + 1, np.int32)
+    col = np.empty(nnz, np.int32)
+    val = np.empty(nnz, np.float64)
+    st = ctx.lib.ma_hessian_copy(ctx.h, ctypes.c_void_p(rowptr.ctypes.data), ctypes.c_void_p(col.ctypes.data),
+                                 ctypes.c_void_p(val.ctypes.data), L.MA_MEM_HOST)
+    _check(ctx.lib, ctx.h, st, "ma_hessian_copy")
+    return Hessian(rowptr, col, val, n)
+
+
+@dataclass
+class Statistics:
+    """``MA::Statistics`` (optimal_transport.hpp:35-39) plus the engine's counters."""
+
+    niter: int = 0
+    neval: int = 0
+    cg_iters: int = 0
+    linesearch_halvings: int = 0
+    grad_norm: float = 0.0
+    max_rel_err: float = 0.0
+    value: float = 0.0
+    t_eval_ms: float = 0.0
+    t_linsolve_ms: float = 0.0
+    status: int = 0
+
+
+def ot_solve(mesh, X, masses, x=None, eps_g: float = 1e-7, maxiter: int = 100, verbose: bool = False,
+             stats: Statistics | None = None, *, y=None, stop: str = "grad", precision: str = "fp64",
+             cg_rtol: float = 0.0, cg_maxiter: int = 0, ctx: Context | None = None, raise_on_error: bool = True):
+    """``MA::ot_solve``.  Returns the weights (``x`` is the initial guess; ``None``
+    or a wrong-sized array starts from zero like the reference).  ``stop="rel"``
+    uses ``max_i |m_i - nu_i| / nu_i <= eps_g`` instead of ``|m - nu|_2 < eps_g``."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    xs, ys = _split_xy(X, y)
+    n = int(xs.shape[0])
+    if x is None or len(x) != n:
+        if _is_device(xs):
+            import torch
+            x = torch.zeros(n, dtype=torch.float64, device=xs.device)
+        else:
+            x = np.zeros(n)
+    a = _Args(xs, ys, masses, x)
+    w = a.keep[3] if a.device else a.keep[3].copy()
+    wp = ctypes.c_void_p(w.data_ptr()) if a.device else ctypes.c_void_p(w.ctypes.data)
+    o = L.MaSolveOpts()
+    ctx.lib.ma_solve_opts_default(ctypes.byref(o))
+    o.eps_g = eps_g
+    o.maxiter = maxiter
+    o.stop_rule = L.MA_STOP_MAX_REL if stop == "rel" else L.MA_STOP_GRAD_NORM
+    o.precision = L.MA_MIXED if precision == "mixed" else L.MA_FP64
+    o.verbose = 1 if verbose else 0
+    if cg_rtol:
+        o.cg_rtol = cg_rtol
+    if cg_maxiter:
+        o.cg_maxiter = cg_maxiter
+    s = L.MaStats()
+    st = ctx.lib.ma_ot_solve(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], wp, a.mem, ctypes.byref(o),
+                             ctypes.byref(s))
+    if stats is not None:
+        for f, _ in L.MaStats._fields_:
+            setattr(stats, f, getattr(s, f))
+        stats.status = st
+    if raise_on_error and st not in (L.MA_OK,):
+        _check(ctx.lib, ctx.h, st, "ma_ot_solve")
+    return w
+
+
+def solve_laplacian_matrix(g, rtol: float = 1e-10, maxiter: int = 0, ctx: Context | None = None):
+    """Newton direction for the Hessian of the context's last evaluation
+    (optimal_transport.hpp:41-87): ``H[:n-1,:n-1] d = g[:n-1]``, ``d[n-1] = 0``."""
+    ctx = ctx or default_context()
+    a = _Args(g)
+    n = int(a.keep[0].shape[0])
+    d, dp = a.out(n)
+    it = ctypes.c_int64()
+    st = ctx.lib.ma_laplacian_solve(ctx.h, a.ptrs[0], dp, a.mem, float(rtol), int(maxiter), ctypes.byref(it))
+    _check(ctx.lib, ctx.h, st, "ma_laplacian_solve")
+    return d, int(it.value)
+
+
+def first_moment(mesh, X, weights, y=None, ctx: Context | None = None):
+    """``MA::first_moment``: ``(masses, first)`` with ``first[i] = (int rho x, int rho y)``."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    x, yy = _split_xy(X, y)
+    a = _Args(x, yy, weights)
+    n = int(a.keep[0].shape[0])
+    m, mp = a.out(n)
+    f, fp = a.out(2 * n)
+    st = ctx.lib.ma_moments(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.mem, mp, fp, None)
+    _check(ctx.lib, ctx.h, st, "ma_moments")
+    return m, f.reshape(n, 2)
+
+
+def second_moment(mesh, X, weights, y=None, ctx: Context | None = None):
+    """``MA::second_moment``: ``(masses, first, inertia)``, inertia = (xx, yy, xy)."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    x, yy = _split_xy(X, y)
+    a = _Args(x, yy, weights)
+    n = int(a.keep[0].shape[0])
+    m, mp = a.out(n)
+    f, fp = a.out(2 * n)
+    s, sp = a.out(3 * n)
+    st = ctx.lib.ma_moments(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.mem, mp, fp, sp)
+    _check(ctx.lib, ctx.h, st, "ma_moments")
+    return m, f.reshape(n, 2), s.reshape(n, 3)
+
+
+def lloyd(mesh, X, weights, y=None, ctx: Context | None = None):
+    """``MA::lloyd``: ``(masses, centroids)``."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    x, yy = _split_xy(X, y)
+    a = _Args(x, yy, weights)
+    n = int(a.keep[0].shape[0])
+    m, mp = a.out(n)
+    c, cp = a.out(2 * n)
+    st = ctx.lib.ma_lloyd(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.mem, mp, cp)
+    _check(ctx.lib, ctx.h, st, "ma_lloyd")
+    return m, c.reshape(n, 2)

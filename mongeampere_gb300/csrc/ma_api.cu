@@ -1,0 +1,636 @@
+// ma_api.cu -- the C ABI: contexts, meshes, and one Laguerre evaluation
+// (MA::kantorovich, include/MA/kantorovich.hpp:35-141; MA::first_moment /
+// second_moment / lloyd, include/MA/lloyd.hpp:30-144).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "ma_runtime.h"
+
+using namespace ma;
+
+namespace ma {
+
+ma_status fail(Ctx* c, ma_status s, const std::string& msg)
+{
+    if (c) c->last_error = msg;
+    return s;
+}
+
+ma_status cuda_fail(Ctx* c, cudaError_t e, const char* what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (c) c->last_error = m;
+    if (e == cudaErrorMemoryAllocation) return MA_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return MA_ERR_NO_DEVICE;
+    return MA_ERR_CUDA;
+}
+
+MeshGridDev Mesh::grid_dev() const
+{
+    MeshGridDev d;
+    d.nx = nx;
+    d.ny = ny;
+    d.gx = gx.as<double>();
+    d.gy = gy.as<double>();
+    d.val = val.as<double>();
+    d.ihx = ihx.as<double>();
+    d.ihy = ihy.as<double>();
+    return d;
+}
+
+MeshTriDev Mesh::tri_dev() const
+{
+    MeshTriDev d;
+    d.nv = nv;
+    d.nt = nt;
+    d.vx = vx.as<double>();
+    d.vy = vy.as<double>();
+    d.tri = tri.as<int>();
+    d.lin = lin.as<double>();
+    d.tbin = tbin.as<int4>();
+    d.bnx = bnx;
+    d.bny = bny;
+    d.bx0 = bx0;
+    d.by0 = by0;
+    d.bcw = bcw;
+    d.bch = bch;
+    d.bin_start = bin_start.as<int>();
+    d.bin_tri = bin_tri.as<int>();
+    return d;
+}
+
+static constexpr int kScap = 65;  // staging slots per Hessian row (largest cell capacity + diagonal)
+
+// Build the uniform site grid (counting sort by cell).  Positions only: call once
+// per set of sites.
+ma_status build_site_grid(Ctx* c, const Mesh* m, int n, const double* x, const double* y, const double* w)
+{
+    cudaStream_t s = c->stream;
+    MA_CUDA(c, c->keys.ensure(8 * sizeof(unsigned long long)));
+    MA_CUDA(c, c->bboxd.ensure(8 * sizeof(double)));
+    unsigned long long init[5] = {~0ull, 0ull, ~0ull, 0ull, 0ull};
+    MA_CUDA(c, cudaMemcpyAsync(c->keys.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    launch_bbox(x, y, nullptr, n, c->keys.as<unsigned long long>(), s);
+    launch_key_to_double(c->keys.as<unsigned long long>(), c->bboxd.as<double>(), 4, s);
+    c->launches += 2;
+    MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->bboxd.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaStreamSynchronize(s));
+    double xmin = c->hstat[0], xmax = c->hstat[1], ymin = c->hstat[2], ymax = c->hstat[3];
+    if (!(std::isfinite(xmin) && std::isfinite(xmax) && std::isfinite(ymin) && std::isfinite(ymax)))
+        return fail(c, MA_ERR_INVALID_ARGUMENT, "non-finite site coordinates");
+    xmin = std::min(xmin, m->X0);
+    xmax = std::max(xmax, m->X1);
+    ymin = std::min(ymin, m->Y0);
+    ymax = std::max(ymax, m->Y1);
+    double W = xmax - xmin, H = ymax - ymin;
+    double sc = std::max(std::max(W, H), 1e-300);
+    W = std::max(W, 1e-9 * sc);
+    H = std::max(H, 1e-9 * sc);
+    double target = std::max(1.0, n / 2.0);
+    int gnx = (int)std::max(1.0, std::floor(std::sqrt(target * W / H)));
+    int gny = (int)std::max(1.0, std::floor(target / gnx));
+    gnx = std::min(gnx, 16384);
+    gny = std::min(gny, 16384);
+    SiteGrid g;
+    g.gnx = gnx;
+    g.gny = gny;
+    g.gx0 = xmin;
+    g.gy0 = ymin;
+    g.gcw = W * (1.0 + 1e-9) / gnx;
+    g.gch = H * (1.0 + 1e-9) / gny;
+    int ncell = gnx * gny;
+    MA_CUDA(c, c->cell.ensure(sizeof(int) * (size_t)n));
+    MA_CUDA(c, c->count.ensure(sizeof(int) * (size_t)ncell));
+    MA_CUDA(c, c->fill.ensure(sizeof(int) * (size_t)ncell));
+    MA_CUDA(c, c->start.ensure(sizeof(int) * ((size_t)ncell + 1)));
+    MA_CUDA(c, c->perm.ensure(sizeof(int) * (size_t)n));
+    MA_CUDA(c, c->sites.ensure(sizeof(SiteD) * (size_t)n));
+    size_t scr = std::max(scan_scratch_ints(ncell), scan_scratch_ints(n));
+    MA_CUDA(c, c->scan_scratch.ensure(sizeof(int) * scr));
+    MA_CUDA(c, cudaMemsetAsync(c->count.p, 0, sizeof(int) * ncell, s));
+    MA_CUDA(c, cudaMemsetAsync(c->fill.p, 0, sizeof(int) * ncell, s));
+    g.cell_start = c->start.as<int>();
+    launch_grid_cells(x, y, n, g, c->cell.as<int>(), c->count.as<int>(), s);
+    launch_scan(c->count.as<int>(), c->start.as<int>(), ncell, c->scan_scratch.as<int>(), s);
+    launch_scatter(c->cell.as<int>(), n, c->start.as<int>(), c->fill.as<int>(), c->perm.as<int>(), s);
+    launch_sort_cells(ncell, c->start.as<int>(), c->perm.as<int>(), s);
+    c->launches += 6;
+    c->grid = g;
+    c->n = n;
+    if (w) {
+        launch_gather(x, y, w, c->perm.as<int>(), n, c->sites.as<SiteD>(), s);
+        c->launches += 1;
+    }
+    return MA_OK;
+}
+
+static ma_status ensure_eval_buffers(Ctx* c, int n, bool mom)
+{
+    MA_CUDA(c, c->mass.ensure(sizeof(double) * (size_t)n));
+    MA_CUDA(c, c->vpart.ensure(sizeof(double) * (size_t)n));
+    if (mom) MA_CUDA(c, c->mom.ensure(sizeof(double) * 6 * (size_t)n));
+    MA_CUDA(c, c->rowcnt.ensure(sizeof(int) * (size_t)n));
+    MA_CUDA(c, c->st_col.ensure(sizeof(int) * kScap * (size_t)n));
+    MA_CUDA(c, c->st_val.ensure(sizeof(double) * kScap * (size_t)n));
+    MA_CUDA(c, c->rowptr.ensure(sizeof(int) * ((size_t)n + 1)));
+    MA_CUDA(c, c->status.ensure(sizeof(uint32_t) * 4));
+    MA_CUDA(c, c->redo.ensure(sizeof(int) * (size_t)n));
+    MA_CUDA(c, c->nredo.ensure(sizeof(int) * 4));
+    int nb = stats_blocks(n);
+    MA_CUDA(c, c->stat_partial.ensure(sizeof(double) * 5 * (size_t)nb));
+    MA_CUDA(c, c->stat_out.ensure(sizeof(double) * 16));
+    MA_CUDA(c, c->keys.ensure(8 * sizeof(unsigned long long)));
+    MA_CUDA(c, c->bboxd.ensure(8 * sizeof(double)));
+    size_t guess = (size_t)n * 8 + 64;
+    MA_CUDA(c, c->col.ensure(sizeof(int) * guess));
+    MA_CUDA(c, c->val.ensure(sizeof(double) * guess));
+    return MA_OK;
+}
+
+static void launch_cells(Ctx* c, const Mesh* m, const CellArgs& a, int cap_kind, bool mom)
+{
+    if (m->kind == 0)
+        launch_cells_grid(a, m->grid_dev(), cap_kind, mom, c->stream);
+    else
+        launch_cells_tri(a, m->tri_dev(), cap_kind, mom, c->stream);
+    c->launches += 1;
+}
+
+// One Laguerre evaluation for the sites of the current grid with weights w (device,
+// original order).  Leaves mass, vpart (and mom), the CSR Hessian and the statistics
+// in the context.
+ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlags& f)
+{
+    cudaStream_t s = c->stream;
+    ma_status st = ensure_eval_buffers(c, n, f.moments > 0);
+    if (st != MA_OK) return st;
+    launch_update_weights(w, c->perm.as<int>(), n, c->sites.as<SiteD>(), s);
+    unsigned long long zero = 0;
+    MA_CUDA(c, cudaMemcpyAsync(c->keys.as<unsigned long long>() + 4, &zero, sizeof(zero), cudaMemcpyHostToDevice, s));
+    launch_wmax(w, n, c->keys.as<unsigned long long>() + 4, s);
+    launch_key_to_double(c->keys.as<unsigned long long>() + 4, c->bboxd.as<double>() + 4, 1, s);
+    c->launches += 3;
+    MA_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * 4, s));
+    MA_CUDA(c, cudaMemsetAsync(c->nredo.p, 0, sizeof(int) * 4, s));
+
+    CellArgs a;
+    a.n = n;
+    a.sites = c->sites.as<SiteD>();
+    a.perm = c->perm.as<int>();
+    a.grid = c->grid;
+    a.X0 = m->X0;
+    a.Y0 = m->Y0;
+    a.X1 = m->X1;
+    a.Y1 = m->Y1;
+    a.wmax = c->bboxd.as<double>() + 4;
+    a.mass = c->mass.as<double>();
+    a.vpart = c->vpart.as<double>();
+    a.mom = f.moments > 0 ? c->mom.as<double>() : nullptr;
+    a.rowcnt = c->rowcnt.as<int>();
+    a.st_col = c->st_col.as<int>();
+    a.st_val = c->st_val.as<double>();
+    a.scap = kScap;
+    a.status = c->status.as<uint32_t>();
+    a.redo = c->redo.as<int>();
+    a.nredo = c->nredo.as<int>();
+    a.work = nullptr;
+    a.nwork = 0;
+    launch_cells(c, m, a, 0, f.moments > 0);
+    MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaStreamSynchronize(s));
+    int nredo = c->hinfo[0];
+    if (nredo > 0) {
+        // sites whose cell outgrew the small capacity: redo them with the large one
+        CellArgs b = a;
+        b.work = c->redo.as<int>();
+        b.nwork = nredo;
+        MA_CUDA(c, c->fill.ensure(sizeof(int) * ((size_t)n + 4)));
+        b.redo = c->fill.as<int>();
+        b.nredo = c->nredo.as<int>() + 1;
+        launch_cells(c, m, b, 1, f.moments > 0);
+        MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        MA_CUDA(c, cudaStreamSynchronize(s));
+        if (c->hinfo[0] > 0)
+            return fail(c, MA_ERR_CAPACITY, "a Laguerre cell has more vertices than the largest kernel capacity");
+    }
+    uint32_t stbits = (uint32_t)c->hinfo[1];
+    if (stbits & ST_EXACT_OVERFLOW)
+        return fail(c, MA_ERR_EXACT_OVERFLOW, "an exact predicate exceeded its expansion capacity");
+    if (stbits & ST_BAD_INPUT) return fail(c, MA_ERR_INVALID_ARGUMENT, "non-finite site or weight");
+
+    c->have_h = false;
+    if (f.hessian) {
+        launch_scan(c->rowcnt.as<int>(), c->rowptr.as<int>(), n, c->scan_scratch.as<int>(), s);
+        c->launches += 2;
+        MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 2, c->rowptr.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MA_CUDA(c, cudaStreamSynchronize(s));
+        int64_t nnz = c->hinfo[2];
+        MA_CUDA(c, c->col.ensure(sizeof(int) * (size_t)(nnz + 1)));
+        MA_CUDA(c, c->val.ensure(sizeof(double) * (size_t)(nnz + 1)));
+        launch_csr_compact(n, c->rowptr.as<int>(), c->rowcnt.as<int>(), c->st_col.as<int>(), c->st_val.as<double>(),
+                           kScap, c->col.as<int>(), c->val.as<double>(), s);
+        c->launches += 1;
+        c->nnz = nnz;
+        c->have_h = true;
+    }
+    int nb = stats_blocks(n);
+    launch_stats(c->mass.as<double>(), c->vpart.as<double>(), f.nu, w, n, c->stat_partial.as<double>(), nb,
+                 c->stat_out.as<double>(), s);
+    c->launches += 2;
+    return MA_OK;
+}
+
+}  // namespace ma
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+const char* ma_status_string(ma_status s)
+{
+    switch (s) {
+    case MA_OK: return "ok";
+    case MA_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case MA_ERR_NO_DEVICE: return "no usable CUDA device";
+    case MA_ERR_CUDA: return "CUDA error";
+    case MA_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case MA_ERR_CAPACITY: return "cell capacity exceeded";
+    case MA_ERR_EXACT_OVERFLOW: return "exact predicate capacity exceeded";
+    case MA_EMPTY_CELL: return "a Laguerre cell is empty";
+    case MA_LINESEARCH_FAIL: return "line search failed";
+    case MA_MAXITER: return "maximum number of iterations reached";
+    case MA_ERR_BUFFER_TOO_SMALL: return "buffer too small";
+    }
+    return "unknown status";
+}
+
+ma_status ma_ctx_create(int device, ma_ctx** out)
+{
+    if (!out) return MA_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return MA_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return MA_ERR_INVALID_ARGUMENT;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return MA_ERR_NO_DEVICE;
+    if (prop.major != 10 || prop.minor != 3) return MA_ERR_NO_DEVICE;  // built for sm_103a only
+    if (cudaSetDevice(device) != cudaSuccess) return MA_ERR_NO_DEVICE;
+    ma_ctx* c = new ma_ctx();
+    c->device = device;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return MA_ERR_CUDA;
+    }
+    if (cudaMallocHost(&c->hstat, 16 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&c->hinfo, 8 * sizeof(int)) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return MA_ERR_OUT_OF_MEMORY;
+    }
+    *out = c;
+    return MA_OK;
+}
+
+void ma_ctx_destroy(ma_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    DevBuf* bufs[] = {&c->hx, &c->hy, &c->hw, &c->hnu, &c->cell, &c->count, &c->fill, &c->start, &c->perm,
+                      &c->sites, &c->scan_scratch, &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,
+                      &c->st_col, &c->st_val, &c->rowptr, &c->col, &c->val, &c->status, &c->redo, &c->nredo,
+                      &c->stat_partial, &c->stat_out, &c->info, &c->wcur, &c->w0, &c->dirn, &c->g, &c->cg_r,
+                      &c->cg_z, &c->cg_p, &c->cg_q, &c->cg_dinv, &c->cg_scal, &c->cg_part};
+    for (DevBuf* b : bufs) b->release();
+    if (c->hstat) cudaFreeHost(c->hstat);
+    if (c->hinfo) cudaFreeHost(c->hinfo);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+ma_status ma_ctx_set_stream(ma_ctx* c, void* stream)
+{
+    if (!c) return MA_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+    return MA_OK;
+}
+
+const char* ma_ctx_last_error(const ma_ctx* c) { return c ? c->last_error.c_str() : ""; }
+
+int64_t ma_ctx_launch_count(const ma_ctx* c) { return c ? c->launches : 0; }
+
+ma_status ma_mesh_create_grid(ma_ctx* c, int nx, int ny, const double* gx, const double* gy, const double* values,
+                              ma_mesh** out)
+{
+    if (!c || !out || !gx || !gy || !values || nx < 2 || ny < 2) return MA_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i + 1 < nx; i++)
+        if (!(gx[i + 1] > gx[i])) return fail(c, MA_ERR_INVALID_ARGUMENT, "gx must increase strictly");
+    for (int j = 0; j + 1 < ny; j++)
+        if (!(gy[j + 1] > gy[j])) return fail(c, MA_ERR_INVALID_ARGUMENT, "gy must increase strictly");
+    cudaSetDevice(c->device);
+    ma_mesh* m = new ma_mesh();
+    m->ctx = c;
+    m->kind = 0;
+    m->nx = nx;
+    m->ny = ny;
+    m->X0 = gx[0];
+    m->X1 = gx[nx - 1];
+    m->Y0 = gy[0];
+    m->Y1 = gy[ny - 1];
+    std::vector<double> ihx(nx), ihy(ny);
+    for (int i = 0; i + 1 < nx; i++) ihx[i] = 1.0 / (gx[i + 1] - gx[i]);
+    for (int j = 0; j + 1 < ny; j++) ihy[j] = 1.0 / (gy[j + 1] - gy[j]);
+    ihx[nx - 1] = 0;
+    ihy[ny - 1] = 0;
+    // total mass: every square holds two triangles of area A/2; the linear
+    // interpolant integrates to area * mean of the three vertex values
+    double tot = 0;
+    for (int j = 0; j + 1 < ny; j++) {
+        for (int i = 0; i + 1 < nx; i++) {
+            double a = (gx[i + 1] - gx[i]) * (gy[j + 1] - gy[j]) / 2.0;
+            double v00 = values[j * nx + i], v10 = values[j * nx + i + 1];
+            double v01 = values[(j + 1) * nx + i], v11 = values[(j + 1) * nx + i + 1];
+            tot += a * (v00 + v10 + v11) / 3.0 + a * (v00 + v11 + v01) / 3.0;
+        }
+    }
+    m->total_mass = tot;
+    cudaError_t e = cudaSuccess;
+    if ((e = m->gx.ensure(sizeof(double) * nx)) != cudaSuccess ||
+        (e = m->gy.ensure(sizeof(double) * ny)) != cudaSuccess ||
+        (e = m->val.ensure(sizeof(double) * (size_t)nx * ny)) != cudaSuccess ||
+        (e = m->ihx.ensure(sizeof(double) * nx)) != cudaSuccess ||
+        (e = m->ihy.ensure(sizeof(double) * ny)) != cudaSuccess) {
+        ma_mesh_destroy(m);
+        return cuda_fail(c, e, "mesh allocation");
+    }
+    cudaMemcpy(m->gx.p, gx, sizeof(double) * nx, cudaMemcpyHostToDevice);
+    cudaMemcpy(m->gy.p, gy, sizeof(double) * ny, cudaMemcpyHostToDevice);
+    cudaMemcpy(m->val.p, values, sizeof(double) * (size_t)nx * ny, cudaMemcpyHostToDevice);
+    cudaMemcpy(m->ihx.p, ihx.data(), sizeof(double) * nx, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(m->ihy.p, ihy.data(), sizeof(double) * ny, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        ma_mesh_destroy(m);
+        return cuda_fail(c, e, "mesh upload");
+    }
+    *out = m;
+    return MA_OK;
+}
+
+ma_status ma_mesh_create_triangles(ma_ctx* c, int nv, const double* vx, const double* vy, const double* values,
+                                   int nt, const int32_t* tri, ma_mesh** out)
+{
+    if (!c || !out || !vx || !vy || !values || !tri || nv < 3 || nt < 1) return MA_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    std::vector<int> t(tri, tri + 3 * (size_t)nt);
+    std::vector<double> lin(3 * (size_t)nt);
+    double X0 = vx[0], X1 = vx[0], Y0 = vy[0], Y1 = vy[0];
+    for (int i = 0; i < nv; i++) {
+        X0 = std::min(X0, vx[i]);
+        X1 = std::max(X1, vx[i]);
+        Y0 = std::min(Y0, vy[i]);
+        Y1 = std::max(Y1, vy[i]);
+    }
+    double tot = 0;
+    for (int f = 0; f < nt; f++) {
+        int a = t[3 * f], b = t[3 * f + 1], d = t[3 * f + 2];
+        if (a < 0 || b < 0 || d < 0 || a >= nv || b >= nv || d >= nv)
+            return fail(c, MA_ERR_INVALID_ARGUMENT, "triangle index out of range");
+        double e1x = vx[b] - vx[a], e1y = vy[b] - vy[a], e2x = vx[d] - vx[a], e2y = vy[d] - vy[a];
+        double det = e1x * e2y - e1y * e2x;
+        if (det == 0) return fail(c, MA_ERR_INVALID_ARGUMENT, "degenerate triangle");
+        if (det < 0) {
+            // counter-clockwise orientation, as the incremental builder's reorient_faces
+            std::swap(t[3 * f + 1], t[3 * f + 2]);
+            std::swap(b, d);
+            std::swap(e1x, e2x);
+            std::swap(e1y, e2y);
+            det = -det;
+        }
+        double f1 = values[b] - values[a], f2 = values[d] - values[a];
+        lin[3 * f] = values[a];
+        lin[3 * f + 1] = (f1 * e2y - f2 * e1y) / det;
+        lin[3 * f + 2] = (e1x * f2 - e2x * f1) / det;
+        tot += det / 2.0 * (values[a] + values[b] + values[d]) / 3.0;
+    }
+    ma_mesh* m = new ma_mesh();
+    m->ctx = c;
+    m->kind = 1;
+    m->nv = nv;
+    m->nt = nt;
+    m->X0 = X0;
+    m->X1 = X1;
+    m->Y0 = Y0;
+    m->Y1 = Y1;
+    m->total_mass = tot;
+    // bins: about two triangles per bin
+    double W = std::max(X1 - X0, 1e-300), H = std::max(Y1 - Y0, 1e-300);
+    double target = std::max(1.0, nt / 2.0);
+    int bnx = std::max(1, (int)std::floor(std::sqrt(target * W / H)));
+    int bny = std::max(1, (int)std::floor(target / bnx));
+    bnx = std::min(bnx, 8192);
+    bny = std::min(bny, 8192);
+    m->bnx = bnx;
+    m->bny = bny;
+    m->bx0 = X0;
+    m->by0 = Y0;
+    m->bcw = W * (1 + 1e-9) / bnx;
+    m->bch = H * (1 + 1e-9) / bny;
+    std::vector<int4> tb(nt);
+    std::vector<int> cnt((size_t)bnx * bny + 1, 0);
+    auto clampb = [](int v, int n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); };
+    for (int f = 0; f < nt; f++) {
+        double tx0 = std::min({vx[t[3 * f]], vx[t[3 * f + 1]], vx[t[3 * f + 2]]});
+        double tx1 = std::max({vx[t[3 * f]], vx[t[3 * f + 1]], vx[t[3 * f + 2]]});
+        double ty0 = std::min({vy[t[3 * f]], vy[t[3 * f + 1]], vy[t[3 * f + 2]]});
+        double ty1 = std::max({vy[t[3 * f]], vy[t[3 * f + 1]], vy[t[3 * f + 2]]});
+        int4 r;
+        r.x = clampb((int)std::floor((tx0 - m->bx0) / m->bcw) - 1, bnx);
+        r.y = clampb((int)std::floor((ty0 - m->by0) / m->bch) - 1, bny);
+        r.z = clampb((int)std::floor((tx1 - m->bx0) / m->bcw) + 1, bnx);
+        r.w = clampb((int)std::floor((ty1 - m->by0) / m->bch) + 1, bny);
+        tb[f] = r;
+        for (int by = r.y; by <= r.w; by++)
+            for (int bx = r.x; bx <= r.z; bx++) cnt[(size_t)by * bnx + bx + 1]++;
+    }
+    for (size_t b = 0; b < (size_t)bnx * bny; b++) cnt[b + 1] += cnt[b];
+    std::vector<int> fillp(cnt.begin(), cnt.end() - 1), bt(cnt.back());
+    for (int f = 0; f < nt; f++) {
+        int4 r = tb[f];
+        for (int by = r.y; by <= r.w; by++)
+            for (int bx = r.x; bx <= r.z; bx++) bt[fillp[(size_t)by * bnx + bx]++] = f;
+    }
+    cudaError_t e = cudaSuccess;
+    if ((e = m->vx.ensure(sizeof(double) * nv)) != cudaSuccess ||
+        (e = m->vy.ensure(sizeof(double) * nv)) != cudaSuccess ||
+        (e = m->tri.ensure(sizeof(int) * 3 * (size_t)nt)) != cudaSuccess ||
+        (e = m->lin.ensure(sizeof(double) * 3 * (size_t)nt)) != cudaSuccess ||
+        (e = m->tbin.ensure(sizeof(int4) * (size_t)nt)) != cudaSuccess ||
+        (e = m->bin_start.ensure(sizeof(int) * cnt.size())) != cudaSuccess ||
+        (e = m->bin_tri.ensure(sizeof(int) * (bt.size() + 1))) != cudaSuccess) {
+        ma_mesh_destroy(m);
+        return cuda_fail(c, e, "mesh allocation");
+    }
+    cudaMemcpy(m->vx.p, vx, sizeof(double) * nv, cudaMemcpyHostToDevice);
+    cudaMemcpy(m->vy.p, vy, sizeof(double) * nv, cudaMemcpyHostToDevice);
+    cudaMemcpy(m->tri.p, t.data(), sizeof(int) * 3 * (size_t)nt, cudaMemcpyHostToDevice);
+    cudaMemcpy(m->lin.p, lin.data(), sizeof(double) * 3 * (size_t)nt, cudaMemcpyHostToDevice);
+    cudaMemcpy(m->tbin.p, tb.data(), sizeof(int4) * (size_t)nt, cudaMemcpyHostToDevice);
+    cudaMemcpy(m->bin_start.p, cnt.data(), sizeof(int) * cnt.size(), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(m->bin_tri.p, bt.data(), sizeof(int) * bt.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        ma_mesh_destroy(m);
+        return cuda_fail(c, e, "mesh upload");
+    }
+    *out = m;
+    return MA_OK;
+}
+
+void ma_mesh_destroy(ma_mesh* m)
+{
+    if (!m) return;
+    if (m->ctx) cudaSetDevice(m->ctx->device);
+    DevBuf* bufs[] = {&m->gx, &m->gy, &m->val, &m->ihx, &m->ihy, &m->vx, &m->vy, &m->tri, &m->lin,
+                      &m->tbin, &m->bin_start, &m->bin_tri};
+    for (DevBuf* b : bufs) b->release();
+    delete m;
+}
+
+ma_status ma_mesh_total_mass(const ma_mesh* m, double* out)
+{
+    if (!m || !out) return MA_ERR_INVALID_ARGUMENT;
+    *out = m->total_mass;
+    return MA_OK;
+}
+
+// stage caller arrays on the device: host arrays are copied into context buffers
+static ma_status stage_in(ma_ctx* c, DevBuf& buf, const double* src, int64_t n, ma_mem mem, const double** dst)
+{
+    if (mem == MA_MEM_DEVICE) {
+        *dst = src;
+        return MA_OK;
+    }
+    MA_CUDA(c, buf.ensure(sizeof(double) * (size_t)n));
+    MA_CUDA(c, cudaMemcpyAsync(buf.p, src, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    *dst = buf.as<double>();
+    return MA_OK;
+}
+
+static ma_status copy_out(ma_ctx* c, double* dst, const double* src, size_t count, ma_mem mem)
+{
+    if (!dst) return MA_OK;
+    MA_CUDA(c, cudaMemcpyAsync(dst, src, sizeof(double) * count,
+                               mem == MA_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+    return MA_OK;
+}
+
+ma_status ma_kantorovich(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x, const double* y, const double* w,
+                         ma_mem mem, ma_precision prec, double* value, double* g, int64_t* nnz)
+{
+    if (!c || !m || !x || !y || !w || n < 1 || n > (int64_t)1 << 30) return MA_ERR_INVALID_ARGUMENT;
+    if (prec != MA_FP64 && prec != MA_MIXED) return MA_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    const double *dx, *dy, *dw;
+    ma_status st;
+    if ((st = stage_in(c, c->hx, x, n, mem, &dx)) != MA_OK) return st;
+    if ((st = stage_in(c, c->hy, y, n, mem, &dy)) != MA_OK) return st;
+    if ((st = stage_in(c, c->hw, w, n, mem, &dw)) != MA_OK) return st;
+    if ((st = build_site_grid(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
+    EvalFlags f;
+    f.hessian = true;
+    if ((st = run_eval(c, m, (int)n, dw, f)) != MA_OK) return st;
+    if ((st = copy_out(c, g, c->mass.as<double>(), (size_t)n, mem)) != MA_OK) return st;
+    MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->stat_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MA_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (value) *value = c->hstat[0];
+    if (nnz) *nnz = c->nnz;
+    return MA_OK;
+}
+
+ma_status ma_hessian_copy(ma_ctx* c, int32_t* rowptr, int32_t* col, double* val, ma_mem mem)
+{
+    if (!c) return MA_ERR_INVALID_ARGUMENT;
+    if (!c->have_h) return fail(c, MA_ERR_INVALID_ARGUMENT, "no Hessian has been computed");
+    cudaSetDevice(c->device);
+    cudaMemcpyKind k = mem == MA_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (rowptr) MA_CUDA(c, cudaMemcpyAsync(rowptr, c->rowptr.p, sizeof(int) * ((size_t)c->n + 1), k, c->stream));
+    if (col) MA_CUDA(c, cudaMemcpyAsync(col, c->col.p, sizeof(int) * (size_t)c->nnz, k, c->stream));
+    if (val) MA_CUDA(c, cudaMemcpyAsync(val, c->val.p, sizeof(double) * (size_t)c->nnz, k, c->stream));
+    MA_CUDA(c, cudaStreamSynchronize(c->stream));
+    return MA_OK;
+}
+
+static ma_status moments_impl(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x, const double* y,
+                              const double* w, ma_mem mem, int order)
+{
+    if (!c || !m || !x || !y || !w || n < 1 || n > (int64_t)1 << 30) return MA_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    const double *dx, *dy, *dw;
+    ma_status st;
+    if ((st = stage_in(c, c->hx, x, n, mem, &dx)) != MA_OK) return st;
+    if ((st = stage_in(c, c->hy, y, n, mem, &dy)) != MA_OK) return st;
+    if ((st = stage_in(c, c->hw, w, n, mem, &dw)) != MA_OK) return st;
+    if ((st = build_site_grid(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
+    EvalFlags f;
+    f.hessian = false;
+    f.moments = order;
+    return run_eval(c, m, (int)n, dw, f);
+}
+
+ma_status ma_moments(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x, const double* y, const double* w,
+                     ma_mem mem, double* mass, double* first, double* second)
+{
+    ma_status st = moments_impl(c, m, n, x, y, w, mem, second ? 2 : 1);
+    if (st != MA_OK) return st;
+    std::vector<double> mo(6 * (size_t)n);
+    MA_CUDA(c, cudaMemcpyAsync(mo.data(), c->mom.p, sizeof(double) * 6 * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    MA_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<double> ms(n), f1(2 * (size_t)n), f2(3 * (size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        ms[i] = mo[6 * i];
+        f1[2 * i] = mo[6 * i + 1];
+        f1[2 * i + 1] = mo[6 * i + 2];
+        f2[3 * i] = mo[6 * i + 3];
+        f2[3 * i + 1] = mo[6 * i + 4];
+        f2[3 * i + 2] = mo[6 * i + 5];
+    }
+    cudaMemcpyKind k = mem == MA_MEM_DEVICE ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+    if (mass) MA_CUDA(c, cudaMemcpy(mass, ms.data(), sizeof(double) * n, k));
+    if (first) MA_CUDA(c, cudaMemcpy(first, f1.data(), sizeof(double) * 2 * n, k));
+    if (second) MA_CUDA(c, cudaMemcpy(second, f2.data(), sizeof(double) * 3 * n, k));
+    return MA_OK;
+}
+
+ma_status ma_lloyd(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x, const double* y, const double* w,
+                   ma_mem mem, double* mass, double* centroids)
+{
+    ma_status st = moments_impl(c, m, n, x, y, w, mem, 1);
+    if (st != MA_OK) return st;
+    std::vector<double> mo(6 * (size_t)n);
+    MA_CUDA(c, cudaMemcpyAsync(mo.data(), c->mom.p, sizeof(double) * 6 * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    MA_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<double> ms(n), ce(2 * (size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        ms[i] = mo[6 * i];
+        ce[2 * i] = mo[6 * i + 1] / mo[6 * i];
+        ce[2 * i + 1] = mo[6 * i + 2] / mo[6 * i];
+    }
+    cudaMemcpyKind k = mem == MA_MEM_DEVICE ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+    if (mass) MA_CUDA(c, cudaMemcpy(mass, ms.data(), sizeof(double) * n, k));
+    if (centroids) MA_CUDA(c, cudaMemcpy(centroids, ce.data(), sizeof(double) * 2 * n, k));
+    return MA_OK;
+}
+
+}  // extern "C"

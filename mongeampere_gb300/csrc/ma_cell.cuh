@@ -1,0 +1,549 @@
+// ma_cell.cuh -- one Laguerre cell, clipped and integrated by one thread.
+//
+// Reference behaviour restated (paths in the MongeAmpere++ tree):
+//   include/MA/voronoi_triangulation_intersection.hpp:42-199  symbolic polygon
+//       edges (EDGE_T between two mesh points, EDGE_DT on the radical axis of two
+//       sites), inside(), and the Sutherland-Hodgman clip by one radical axis;
+//   include/MA/predicates.hpp:73-135  Side1 (power distance at a mesh point),
+//       Side2 (at the weighted circumcentre of three sites), Side3 (at the
+//       crossing of a mesh edge with a radical axis), strict SMALLER = inside;
+//   include/MA/kantorovich.hpp:95-135  per-piece integrals and Hessian triplets.
+//
+// Design:
+//   * A polygon is a cyclic list of edge labels.  Vertex k is the start of edge
+//     k, i.e. the crossing of edges k-1 and k.  Labels >= 0 name a slot (a site
+//     whose radical axis bounds the polygon); labels < 0 name fixed edge -1-e,
+//     the segment from fixed point e to fixed point e+1 (box corners in the cell
+//     stage, triangle corners in the triangle stage).
+//   * Every vertex also carries an FP32 position relative to the owner site and a
+//     rigorous per-component error bound.  "Is vertex k strictly closer to the
+//     owner than to site c?" is first answered in FP32 with that bound; only
+//     when the bound straddles zero is the question re-asked symbolically from
+//     the input doubles (Side1/2/3), with an FP64 running-error filter and, when
+//     that cannot decide either, exact expansion arithmetic.  The combinatorial
+//     result (which edges survive) is therefore exact.
+//   * Positions used for integrals are recomputed in FP64 from the labels, so the
+//     integrals do not inherit the FP32 positions.
+#pragma once
+
+#include "ma_exact.cuh"
+
+namespace ma {
+
+// status bits (per launch, OR-ed into a device word)
+enum : uint32_t {
+    ST_POLY_OVERFLOW = 1u,   // polygon / slot capacity exceeded: site redone with a larger capacity
+    ST_EXACT_OVERFLOW = 2u,  // an exact predicate ran out of expansion capacity
+    ST_ROW_OVERFLOW = 4u,    // a Hessian row did not fit its staging slots
+    ST_BAD_INPUT = 8u,       // non-finite input
+};
+
+struct SiteD {
+    double x, y, w, pad;
+};
+
+// A site whose radical axis (with the owner) bounds, or may bound, the polygon.
+// d = x_site - x_owner, z = |d|^2 - (w_site - w_owner); the radical axis is
+// {u : 2 u.d = z} in owner-relative coordinates u, and u is strictly closer to
+// the owner iff 2 u.d - z < 0.
+struct Slot {
+    int site;          // sorted index
+    float dx, dy, z;   // FP32 values
+    float ed, ez;      // per-component error bound of (dx, dy); error bound of z
+    float d1;          // |dx| + |dy|
+};
+
+struct Owner {
+    double x, y, w;
+    int self;          // sorted index
+};
+
+// fixed points of the fixed edges: box corners or triangle corners
+struct Fixed {
+    int n;
+    float ux[4], uy[4], ur[4];  // owner-relative FP32 and per-component error
+    double rx[4], ry[4];        // owner-relative FP64
+    double ax[4], ay[4];        // absolute (exact input doubles)
+};
+
+template <int CAP>
+struct Poly {
+    int n;
+    int lab[CAP];
+    float ux[CAP], uy[CAP], ur[CAP];
+};
+
+MA_HD Slot make_slot(int site, const SiteD& c, const Owner& o)
+{
+    double dx = dsub(c.x, o.x), dy = dsub(c.y, o.y), dw = dsub(c.w, o.w);
+    float fx = (float)dx, fy = (float)dy, fw = (float)dw;
+    float ed = kU32 * fmaxf(fabsf(fx), fabsf(fy)) + 1e-37f;
+    F X{fx, ed}, Y{fy, ed}, W{fw, kU32 * fabsf(fw) + 1e-37f};
+    F Z = f_sub(f_add(f_mul(X, X), f_mul(Y, Y)), W);
+    Slot s;
+    s.site = site;
+    s.dx = fx;
+    s.dy = fy;
+    s.z = Z.v;
+    s.ed = ed;
+    s.ez = Z.e;
+    s.d1 = fabsf(fx) + fabsf(fy);
+    return s;
+}
+
+MA_HD void set_fixed(Fixed& f, int k, double ax, double ay, const Owner& o)
+{
+    f.ax[k] = ax;
+    f.ay[k] = ay;
+    f.rx[k] = dsub(ax, o.x);
+    f.ry[k] = dsub(ay, o.y);
+    f.ux[k] = (float)f.rx[k];
+    f.uy[k] = (float)f.ry[k];
+    f.ur[k] = kU32 * fmaxf(fabsf(f.ux[k]), fabsf(f.uy[k])) + 1e-37f;
+}
+
+// FP32 certified side test of vertex (ux, uy) +- ur against slot c:
+// +1: certainly not inside (2u.d - z > 0), -1: certainly inside, 0: undecided.
+MA_HD int test32(float ux, float uy, float ur, const Slot& c)
+{
+    float val = 2.0f * fmaf(ux, c.dx, uy * c.dy) - c.z;
+    float u1 = fabsf(ux) + fabsf(uy);
+    float b = 2.0f * ur * c.d1 + 2.0f * (u1 + 2.0f * ur) * c.ed + c.ez +
+              4.8e-7f * (2.0f * u1 * c.d1 + fabsf(c.z));
+    b = b * 1.0001f + 1e-36f;
+    if (val > b) return 1;
+    if (val < -b) return -1;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// symbolic predicates on the input doubles (FP64 filter, then exact)
+// ---------------------------------------------------------------------------
+
+// pow(E, v) - pow(E, w) with pow(E, p) = |E - p|^2 - p.w  (Side1's quantity)
+MA_HD R r_pi(double vx, double vy, double vw, double wx, double wy, double ww, double ex, double ey)
+{
+    R ax = r_sub(rv(ex), rv(vx)), ay = r_sub(rv(ey), rv(vy));
+    R bx = r_sub(rv(ex), rv(wx)), by = r_sub(rv(ey), rv(wy));
+    R s = r_sub(r_add(r_mul(ax, ax), r_mul(ay, ay)), r_add(r_mul(bx, bx), r_mul(by, by)));
+    return r_add(s, r_sub(rv(ww), rv(vw)));
+}
+
+constexpr int kExS = 24;  // capacity of a power-difference expansion
+constexpr int kExL = 48;  // capacity of a product expansion
+
+template <int C>
+MA_HD void ex_pi(Exp<C>& h, double vx, double vy, double vw, double wx, double wy, double ww, double ex,
+                 double ey, bool& ok)
+{
+    double t[20];
+    two_prod(2.0 * ex, wx, t[1], t[0]);
+    two_prod(-2.0 * ex, vx, t[3], t[2]);
+    two_prod(2.0 * ey, wy, t[5], t[4]);
+    two_prod(-2.0 * ey, vy, t[7], t[6]);
+    two_prod(vx, vx, t[9], t[8]);
+    two_prod(vy, vy, t[11], t[10]);
+    two_prod(-wx, wx, t[13], t[12]);
+    two_prod(-wy, wy, t[15], t[14]);
+    t[16] = -vw;
+    t[17] = ww;
+    ex_set(h, 0.0);
+    for (int k = 0; k < 18 && ok; k++) ex_grow(h, t[k], ok);
+    ex_compress(h);
+}
+
+template <int CH, int CA, int CB>
+MA_HD void ex_mul2(Exp<CH>& h, const Exp<CA>& a, const Exp<CB>& b, bool& ok)
+{
+    ex_set(h, 0.0);
+    for (int j = 0; j < b.n && ok; j++) {
+        for (int i = 0; i < a.n && ok; i++) {
+            double p, e;
+            two_prod(a.c[i], b.c[j], p, e);
+            ex_grow(h, e, ok);
+            if (ok) ex_grow(h, p, ok);
+        }
+        ex_compress(h);
+    }
+}
+
+template <int CH, int CF>
+MA_HD void ex_acc(Exp<CH>& h, const Exp<CF>& f, double sgn, bool& ok)
+{
+    for (int j = 0; j < f.n && ok; j++) ex_grow(h, sgn * f.c[j], ok);
+    ex_compress(h);
+}
+
+// Side1: is fixed point E strictly closer (power distance) to the owner than to c?
+MA_HDNI int sym_side1(const Owner& o, const SiteD& c, double ex, double ey, uint32_t& st)
+{
+    int s = r_sign(r_pi(o.x, o.y, o.w, c.x, c.y, c.w, ex, ey));
+    if (s == 0) {
+        bool ok = true;
+        Exp<kExS> h;
+        ex_pi(h, o.x, o.y, o.w, c.x, c.y, c.w, ex, ey, ok);
+        if (!ok) st |= ST_EXACT_OVERFLOW;
+        s = ex_sign(h);
+    }
+    return s < 0;
+}
+
+// Side3: E = segment line (p, q) crossing the radical axis of (owner, u).
+// With A = pi(., owner, u), B = pi(., owner, c):
+//   pi(E, owner, c) = (A(p) B(q) - A(q) B(p)) / (A(p) - A(q)).
+MA_HDNI int sym_side3(const Owner& o, const SiteD& u, double px, double py, double qx, double qy,
+                      const SiteD& c, uint32_t& st)
+{
+    R Ap = r_pi(o.x, o.y, o.w, u.x, u.y, u.w, px, py), Aq = r_pi(o.x, o.y, o.w, u.x, u.y, u.w, qx, qy);
+    R Bp = r_pi(o.x, o.y, o.w, c.x, c.y, c.w, px, py), Bq = r_pi(o.x, o.y, o.w, c.x, c.y, c.w, qx, qy);
+    int sd = r_sign(r_sub(r_mul(Ap, Bq), r_mul(Aq, Bp)));
+    int sn = r_sign(r_sub(Ap, Aq));
+    if (sd == 0 || sn == 0) {
+        bool ok = true;
+        Exp<kExS> eAp, eAq, eBp, eBq;
+        ex_pi(eAp, o.x, o.y, o.w, u.x, u.y, u.w, px, py, ok);
+        ex_pi(eAq, o.x, o.y, o.w, u.x, u.y, u.w, qx, qy, ok);
+        ex_pi(eBp, o.x, o.y, o.w, c.x, c.y, c.w, px, py, ok);
+        ex_pi(eBq, o.x, o.y, o.w, c.x, c.y, c.w, qx, qy, ok);
+        Exp<kExL> t1, t2;
+        ex_mul2(t1, eAp, eBq, ok);
+        ex_mul2(t2, eAq, eBp, ok);
+        ex_acc(t1, t2, -1.0, ok);
+        sd = ex_sign(t1);
+        Exp<kExL> dn;
+        ex_set(dn, 0.0);
+        ex_acc(dn, eAp, 1.0, ok);
+        ex_acc(dn, eAq, -1.0, ok);
+        sn = ex_sign(dn);
+        if (!ok) st |= ST_EXACT_OVERFLOW;
+    }
+    if (sn == 0) return 0;
+    return sd * sn < 0;
+}
+
+// Side2: E = weighted circumcentre of (owner, a, b).  Relative to the owner, with
+// d_k = x_k - x_o and z_k = |d_k|^2 - (w_k - w_o):
+//   pi(E, owner, c) = M / D,  D = d_a x d_b,
+//   M = d_c.x (z_a d_b.y - z_b d_a.y) + d_c.y (d_a.x z_b - d_b.x z_a) - z_c D.
+MA_HDNI int sym_side2(const Owner& o, const SiteD& a, const SiteD& b, const SiteD& c, uint32_t& st)
+{
+    R dax = r_sub(rv(a.x), rv(o.x)), day = r_sub(rv(a.y), rv(o.y));
+    R dbx = r_sub(rv(b.x), rv(o.x)), dby = r_sub(rv(b.y), rv(o.y));
+    R dcx = r_sub(rv(c.x), rv(o.x)), dcy = r_sub(rv(c.y), rv(o.y));
+    R za = r_sub(r_add(r_mul(dax, dax), r_mul(day, day)), r_sub(rv(a.w), rv(o.w)));
+    R zb = r_sub(r_add(r_mul(dbx, dbx), r_mul(dby, dby)), r_sub(rv(b.w), rv(o.w)));
+    R zc = r_sub(r_add(r_mul(dcx, dcx), r_mul(dcy, dcy)), r_sub(rv(c.w), rv(o.w)));
+    R D = r_sub(r_mul(dax, dby), r_mul(day, dbx));
+    R M = r_mul(dcx, r_sub(r_mul(za, dby), r_mul(zb, day)));
+    M = r_add(M, r_mul(dcy, r_sub(r_mul(dax, zb), r_mul(dbx, za))));
+    M = r_sub(M, r_mul(zc, D));
+    int sm = r_sign(M), sd = r_sign(D);
+    if (sm == 0 || sd == 0) {
+        bool ok = true;
+        Exp<4> ax, ay, bx, by, cx, cy;
+        ex_diff(ax, a.x, o.x);
+        ex_diff(ay, a.y, o.y);
+        ex_diff(bx, b.x, o.x);
+        ex_diff(by, b.y, o.y);
+        ex_diff(cx, c.x, o.x);
+        ex_diff(cy, c.y, o.y);
+        Exp<kExS> Z[3];
+        const Exp<4>* px[3] = {&ax, &bx, &cx};
+        const Exp<4>* py[3] = {&ay, &by, &cy};
+        const SiteD* ps[3] = {&a, &b, &c};
+        for (int k = 0; k < 3; k++) {
+            Exp<kExS> sq;
+            ex_mul2(Z[k], *px[k], *px[k], ok);
+            ex_mul2(sq, *py[k], *py[k], ok);
+            ex_acc(Z[k], sq, 1.0, ok);
+            Exp<4> dw;
+            ex_diff(dw, ps[k]->w, o.w);
+            ex_acc(Z[k], dw, -1.0, ok);
+        }
+        Exp<kExS> Dx, t;
+        ex_mul2(Dx, ax, by, ok);
+        ex_mul2(t, ay, bx, ok);
+        ex_acc(Dx, t, -1.0, ok);
+        sd = ex_sign(Dx);
+        Exp<kExL> Mx, u1, u2, v;
+        // za*dby - zb*day
+        ex_mul2(u1, Z[0], by, ok);
+        ex_mul2(u2, Z[1], ay, ok);
+        ex_acc(u1, u2, -1.0, ok);
+        ex_mul2(Mx, u1, cx, ok);
+        // dax*zb - dbx*za
+        ex_mul2(u1, ax, Z[1], ok);
+        ex_mul2(u2, bx, Z[0], ok);
+        ex_acc(u1, u2, -1.0, ok);
+        ex_mul2(v, u1, cy, ok);
+        ex_acc(Mx, v, 1.0, ok);
+        ex_mul2(v, Z[2], Dx, ok);
+        ex_acc(Mx, v, -1.0, ok);
+        sm = ex_sign(Mx);
+        if (!ok) st |= ST_EXACT_OVERFLOW;
+    }
+    if (sd == 0) return 0;
+    return sm * sd < 0;
+}
+
+// Is the vertex between edges `prev` and `cur` strictly closer to the owner than
+// to slot c's site?  (Tri_intersector::inside, vti.hpp:129-166.)
+template <int CAP>
+MA_HDNI int sym_inside(int prev, int cur, const Slot* slots, const Fixed& fx, const Owner& o,
+                       const SiteD* sites, int csite, uint32_t& st)
+{
+    const SiteD c = sites[csite];
+    if (prev < 0 && cur < 0) {
+        int e = -1 - cur;
+        return sym_side1(o, c, fx.ax[e], fx.ay[e], st);
+    }
+    if (prev >= 0 && cur >= 0) {
+        const SiteD a = sites[slots[prev].site];
+        const SiteD b = sites[slots[cur].site];
+        return sym_side2(o, a, b, c, st);
+    }
+    int e = (prev < 0) ? -1 - prev : -1 - cur;
+    int u = (prev < 0) ? cur : prev;
+    int e1 = (e + 1 == fx.n) ? 0 : e + 1;
+    const SiteD us = sites[slots[u].site];
+    return sym_side3(o, us, fx.ax[e], fx.ay[e], fx.ax[e1], fx.ay[e1], c, st);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 vertex construction with error radius
+// ---------------------------------------------------------------------------
+
+MA_HD void sanitize(float& ux, float& uy, float& ur)
+{
+    if (!(ur < INFINITY) || !(fabsf(ux) < INFINITY) || !(fabsf(uy) < INFINITY)) {
+        ux = 0.0f;
+        uy = 0.0f;
+        ur = INFINITY;
+    }
+}
+
+// crossing of fixed edge e (fixed point e -> e+1) with the radical axis of slot a
+MA_HD void vtx_fixed_bis(const Fixed& fx, int e, const Slot& a, float& ux, float& uy, float& ur)
+{
+    int e1 = (e + 1 == fx.n) ? 0 : e + 1;
+    F px{fx.ux[e], fx.ur[e]}, py{fx.uy[e], fx.ur[e]};
+    F qx{fx.ux[e1], fx.ur[e1]}, qy{fx.uy[e1], fx.ur[e1]};
+    F dx{a.dx, a.ed}, dy{a.dy, a.ed}, z{a.z, a.ez};
+    F Ap = f_sub(f_scale2(f_add(f_mul(px, dx), f_mul(py, dy))), z);
+    F ex = f_sub(qx, px), ey = f_sub(qy, py);
+    F den = f_scale2(f_add(f_mul(ex, dx), f_mul(ey, dy)));  // A(q) - A(p)
+    F t = f_div(Ap, den);
+    t.v = -t.v;
+    F X = f_add(px, f_mul(t, ex)), Y = f_add(py, f_mul(t, ey));
+    ux = X.v;
+    uy = Y.v;
+    ur = fmaxf(X.e, Y.e);
+    sanitize(ux, uy, ur);
+}
+
+// crossing of the radical axes of slots a and b (weighted circumcentre)
+MA_HD void vtx_bis_bis(const Slot& a, const Slot& b, float& ux, float& uy, float& ur)
+{
+    F ax{a.dx, a.ed}, ay{a.dy, a.ed}, az{a.z, a.ez};
+    F bx{b.dx, b.ed}, by{b.dy, b.ed}, bz{b.z, b.ez};
+    F D = f_scale2(f_sub(f_mul(ax, by), f_mul(ay, bx)));
+    F Nx = f_sub(f_mul(az, by), f_mul(bz, ay));
+    F Ny = f_sub(f_mul(ax, bz), f_mul(bx, az));
+    F X = f_div(Nx, D), Y = f_div(Ny, D);
+    ux = X.v;
+    uy = Y.v;
+    ur = fmaxf(X.e, Y.e);
+    sanitize(ux, uy, ur);
+}
+
+template <int CAP>
+MA_HD void new_vertex(int edge, int cslot, const Slot* slots, const Fixed& fx, float& ux, float& uy, float& ur)
+{
+    if (edge < 0)
+        vtx_fixed_bis(fx, -1 - edge, slots[cslot], ux, uy, ur);
+    else
+        vtx_bis_bis(slots[edge], slots[cslot], ux, uy, ur);
+}
+
+// Sutherland-Hodgman clip of P by the half-plane of slot `cs` (vti.hpp:168-198).
+// Returns false (and leaves Q untouched) when no vertex lies outside.  Sets
+// `overflow` when the result would exceed CAP.
+template <int CAP>
+MA_HD bool clip_poly(const Poly<CAP>& P, Poly<CAP>& Q, int cs, const Slot* slots, const Fixed& fx,
+                     const Owner& o, const SiteD* sites, uint32_t& st, bool& overflow)
+{
+    const int n = P.n;
+    const Slot c = slots[cs];
+    uint64_t outm = 0;
+    for (int k = 0; k < n; k++) {
+        int t = test32(P.ux[k], P.uy[k], P.ur[k], c);
+        bool out;
+        if (t != 0) {
+            out = t > 0;
+        } else {
+            int prev = P.lab[k == 0 ? n - 1 : k - 1];
+            out = !sym_inside<CAP>(prev, P.lab[k], slots, fx, o, sites, c.site, st);
+        }
+        if (out) outm |= (1ull << k);
+    }
+    if (outm == 0) return false;
+    const uint64_t full = (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
+    if (outm == full) {
+        Q.n = 0;
+        return true;
+    }
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+        int i1 = (i + 1 == n) ? 0 : i + 1;
+        bool in0 = !((outm >> i) & 1ull), in1 = !((outm >> i1) & 1ull);
+        if (in0) {
+            if (m >= CAP) { overflow = true; return true; }
+            Q.lab[m] = P.lab[i];
+            Q.ux[m] = P.ux[i];
+            Q.uy[m] = P.uy[i];
+            Q.ur[m] = P.ur[i];
+            m++;
+            if (!in1) {
+                if (m >= CAP) { overflow = true; return true; }
+                Q.lab[m] = cs;
+                new_vertex<CAP>(P.lab[i], cs, slots, fx, Q.ux[m], Q.uy[m], Q.ur[m]);
+                m++;
+            }
+        } else if (in1) {
+            if (m >= CAP) { overflow = true; return true; }
+            Q.lab[m] = P.lab[i];
+            new_vertex<CAP>(P.lab[i], cs, slots, fx, Q.ux[m], Q.uy[m], Q.ur[m]);
+            m++;
+        }
+    }
+    Q.n = m;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 piece integration
+// ---------------------------------------------------------------------------
+
+// FP64 owner-relative data of a neighbour slot
+struct Nb64 {
+    double dx, dy, z;
+};
+
+MA_HD Nb64 make_nb64(const SiteD& c, const Owner& o)
+{
+    Nb64 r;
+    r.dx = dsub(c.x, o.x);
+    r.dy = dsub(c.y, o.y);
+    double dw = dsub(c.w, o.w);
+    r.z = dfma(r.dx, r.dx, dfma(r.dy, r.dy, -dw));
+    return r;
+}
+
+// FP64 vertex between edges prev and cur (owner-relative)
+MA_HD void vtx64(int prev, int cur, const Nb64* nb, const Fixed& fx, double& X, double& Y)
+{
+    if (prev < 0 && cur < 0) {
+        int e = -1 - cur;
+        X = fx.rx[e];
+        Y = fx.ry[e];
+        return;
+    }
+    if (prev >= 0 && cur >= 0) {
+        const Nb64 a = nb[prev], b = nb[cur];
+        double D = 2.0 * (a.dx * b.dy - a.dy * b.dx);
+        double inv = 1.0 / D;
+        X = (a.z * b.dy - b.z * a.dy) * inv;
+        Y = (a.dx * b.z - b.dx * a.z) * inv;
+        return;
+    }
+    int e = (prev < 0) ? -1 - prev : -1 - cur;
+    const Nb64 a = nb[(prev < 0) ? cur : prev];
+    int e1 = (e + 1 == fx.n) ? 0 : e + 1;
+    double px = fx.rx[e], py = fx.ry[e];
+    double ex = fx.rx[e1] - px, ey = fx.ry[e1] - py;
+    double Ap = 2.0 * (px * a.dx + py * a.dy) - a.z;
+    double den = 2.0 * (ex * a.dx + ey * a.dy);
+    double t = -Ap / den;
+    X = px + t * ex;
+    Y = py + t * ey;
+}
+
+// per-site FP64 accumulators
+struct Acc {
+    double mass, second;
+    double m1x, m1y;         // int rho u
+    double sxx, syy, sxy;    // int rho u u^T
+};
+
+// Integrate the linear density rho(u) = c0 + gx u.x + gy u.y over the polygon
+// (owner-relative coordinates) with the fan from the owner: for an edge a -> b
+// and cr = a x b, the triangle (0, a, b) contributes
+//   int 1          = cr/2
+//   int u          = cr (a + b) / 6
+//   int u u^T      = cr/12 (a a^T + b b^T) + cr/24 (a b^T + b a^T)
+//   int u |u|^2    = cr/60 [a (3|a|^2 + 2 a.b + |b|^2) + b (|a|^2 + 2 a.b + 3|b|^2)]
+// (monomial integrals over a simplex).  These are exact for the integrands of
+// kantorovich.hpp:125-131 and lloyd.hpp:57-62, as are the reference's
+// centroid and Albrecht-Collatz rules.  Each DT edge adds |e x d| rho(mid) to
+// hv[slot]; the Hessian entry is then -hv / (2 |d|^2) (kantorovich.hpp:110-121:
+// length * rho(mid) / (2 |x_i - x_j|), with length = |e x d| / |d|).
+template <int CAP, bool MOM>
+MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, double c0, double gx,
+                           double gy, Acc& acc, double* hv, uint64_t& touched)
+{
+    const int n = P.n;
+    double x0, y0;
+    vtx64(P.lab[n - 1], P.lab[0], nb, fx, x0, y0);
+    double ax = x0, ay = y0;
+    double m0 = 0, m1x = 0, m1y = 0, q2 = 0, c3x = 0, c3y = 0, sxx = 0, syy = 0, sxy = 0;
+    for (int k = 0; k < n; k++) {
+        double bx, by;
+        if (k + 1 < n)
+            vtx64(P.lab[k], P.lab[k + 1], nb, fx, bx, by);
+        else {
+            bx = x0;
+            by = y0;
+        }
+        double cr = ax * by - ay * bx;
+        double aa = ax * ax + ay * ay, ab = ax * bx + ay * by, bb = bx * bx + by * by;
+        m0 += cr;
+        m1x += cr * (ax + bx);
+        m1y += cr * (ay + by);
+        q2 += cr * (aa + ab + bb);
+        double ka = 3.0 * aa + 2.0 * ab + bb, kb = aa + 2.0 * ab + 3.0 * bb;
+        c3x += cr * (ax * ka + bx * kb);
+        c3y += cr * (ay * ka + by * kb);
+        if (MOM) {
+            sxx += cr * (2.0 * (ax * ax + bx * bx) + 2.0 * ax * bx);
+            syy += cr * (2.0 * (ay * ay + by * by) + 2.0 * ay * by);
+            sxy += cr * (2.0 * (ax * ay + bx * by) + ax * by + bx * ay);
+        }
+        int lab = P.lab[k];
+        if (lab >= 0) {
+            const Nb64 d = nb[lab];
+            double exv = bx - ax, eyv = by - ay;
+            double crs = fabs(exv * d.dy - eyv * d.dx);
+            double mx = 0.5 * (ax + bx), my = 0.5 * (ay + by);
+            hv[lab] += crs * (c0 + gx * mx + gy * my);
+            touched |= (1ull << lab);
+        }
+        ax = bx;
+        ay = by;
+    }
+    // int rho = c0 int 1 + g . int u ; int rho |u|^2 = c0 int |u|^2 + g . int u |u|^2
+    double I1 = m0 * 0.5;
+    double Iux = m1x * (1.0 / 6.0), Iuy = m1y * (1.0 / 6.0);
+    double Iq = q2 * (1.0 / 12.0);
+    double Icx = c3x * (1.0 / 60.0), Icy = c3y * (1.0 / 60.0);
+    acc.mass += c0 * I1 + gx * Iux + gy * Iuy;
+    acc.second += c0 * Iq + gx * Icx + gy * Icy;
+    if (MOM) {
+        double Sxx = sxx * (1.0 / 24.0), Syy = syy * (1.0 / 24.0), Sxy = sxy * (1.0 / 24.0);
+        acc.m1x += c0 * Iux + gx * Sxx + gy * Sxy;
+        acc.m1y += c0 * Iuy + gx * Sxy + gy * Syy;
+        // int rho u u^T needs third moments: int u_a u_b u_c
+        // (accumulated by the caller through integrate_piece_m2 when requested)
+    }
+}
+
+}  // namespace ma
