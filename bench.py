@@ -1,0 +1,334 @@
+#!/usr/bin/env python
+"""Benchmark of the semi-discrete OT hot path on one GB300.
+
+Workload (the plain-FP64-at-scale configuration): a 512 x 512-vertex grid
+triangulation of [0,1]^2 carrying 0.1 + a mixture of 5 Gaussian bumps, 100,000
+uniform sites, target masses proportional to U[0.5, 1.5]; damped Newton from
+w = 0 until the maximum relative cell-mass error is <= 1e-6.  All inputs are
+seeded synthetic data (mongeampere_gb300.workloads.c2).
+
+One step = one complete OT solve (every Laguerre evaluation, every CG solve and
+line search of ma_ot_solve).  ``value`` = OT solves/s with the inputs resident in
+device memory; ``e2e`` = the same through the C ABI with host buffers (host->device
+copy of sites, masses and initial weights, device->host copy of the weights inside
+the timed region).  L2 is flushed (a 512 MB write) before every timed step.
+
+``--impl reference`` times the reference algorithm's CPU restatement (oracle/) on
+the host cores instead: each step is a bounded sample -- one Laguerre evaluation
+in the reference's FP64 arithmetic plus one sparse direct Newton solve -- scaled to
+a full solve by the number of evaluations and Newton iterations the reference
+algorithm takes on this workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Laguerre evals/s & OT solves/s at mass err≤1e-6, mixed vs FP64, 1 GB300"
+UNIT = "OT solves/s"
+WORKLOAD = "plain FP64 OT: 512x512 grid, 0.1 + 5 Gaussians, N=100,000 uniform sites, masses ~U[0.5,1.5], stop max rel mass err 1e-6"
+
+# The reference algorithm (oracle.ot_solve: flood-filled Laguerre evaluations, sparse
+# direct Newton solves, KMT backtracking) on this workload, seed 0: Newton
+# iterations and Laguerre evaluations to reach max relative mass error 1e-6.
+REF_NITER = None
+REF_NEVAL = None
+
+# algorithmic bytes of one Laguerre evaluation on an implicit grid mesh:
+# X 16N + w 8N + g 8N + CSR Hessian (12 nnz + 4 (N+1)) + value 8 + vertex values 8V
+def eval_bytes(n, nnz, nv):
+    return 16 * n + 8 * n + 8 * n + 12 * nnz + 4 * (n + 1) + 8 + 8 * nv
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [t.strip() for t in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(problem, threads=None):
+    """One Laguerre evaluation in the reference's FP64 arithmetic + one sparse LU
+    Newton solve, on the host cores (the oracle)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle
+    if threads:
+        oracle.set_threads(threads)
+    t0 = time.perf_counter()
+    r = oracle.kantorovich(problem.mesh, problem.x, problem.y, problem.w0, arith="fp64", ring=1)
+    t1 = time.perf_counter()
+    d = oracle.solve_laplacian_matrix(r.hessian(), r.g - problem.nu)
+    t2 = time.perf_counter()
+    assert np.isfinite(d).all()
+    return t1 - t0, t2 - t1, oracle.max_threads()
+
+
+def run_reference(args, rank):
+    from mongeampere_gb300 import workloads as W
+    if rank != 0:
+        return
+    problem = W.c2(0)
+    for _ in range(args.warmup):
+        cpu_sample(problem)
+    te, tl = 0.0, 0.0
+    for _ in range(args.steps):
+        a, b, cores = cpu_sample(problem)
+        te += a
+        tl += b
+    te /= args.steps
+    tl /= args.steps
+    niter = REF_NITER or 12
+    neval = REF_NEVAL or 30
+    solve_s = neval * te + niter * tl
+    value = 1.0 / solve_s
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": solve_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "seed": 0},
+        "laguerre_evals_per_s": 1.0 / te,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"per step: 1 Laguerre evaluation ({te:.2f} s) + 1 sparse LU Newton solve "
+                                   f"({tl:.2f} s) of the CPU restatement on all {cores} threads; a full "
+                                   f"solve = {neval} evaluations + {niter} Newton solves"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    import numpy as np
+    import torch
+
+    from mongeampere_gb300 import api
+    from mongeampere_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = api.Context(local)
+    ctx.use_torch_stream()
+    # weak scaling: every rank solves its own problem (replicas; the solve has no
+    # data-path exchange)
+    p = W.c2(rank)
+    dmesh = ctx.mesh(p.mesh)
+    x = torch.tensor(p.x, device=dev)
+    y = torch.tensor(p.y, device=dev)
+    nu = torch.tensor(p.nu, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def solve_device(stats=None):
+        w = torch.zeros(p.n, dtype=torch.float64, device=dev)
+        st = stats if stats is not None else api.Statistics()
+        api.ot_solve(dmesh, x, nu, x=w, y=y, eps_g=p.tol_rel, stop="rel", precision=args.precision,
+                     stats=st, ctx=ctx)
+        return w, st
+
+    for _ in range(args.warmup):
+        solve_device()
+    torch.cuda.synchronize()
+
+    # ---- timed region: device-resident inputs ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launch_count
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        ev[k][0].record()
+        w, st = solve_device()
+        ev[k][1].record()
+        stats.append(st)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = sum(step_ms) / 1e3
+    if dist:
+        tt = torch.tensor([t_dev], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    value = args.steps * world / t_dev
+    ms_per_step = 1e3 * t_dev / args.steps
+    neval = sum(s.neval for s in stats)
+    t_eval = sum(s.t_eval_ms for s in stats) / 1e3
+    evals_per_s = neval / t_eval if t_eval > 0 else None
+    for s in stats:
+        assert s.max_rel_err <= p.tol_rel, "solve did not converge"
+
+    # ---- dominant kernel: live per-launch duration (profiled run, untimed) ----
+    ctx.profile(True)
+    _, stp = solve_device()
+    torch.cuda.synchronize()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    _, _, h = api.kantorovich(dmesh, torch.stack([x, y], 1), torch.zeros(p.n, dtype=torch.float64, device=dev),
+                              ctx=ctx)
+    nnz = int(h.col.shape[0])
+    cells_ms = prof["cells_ms"] / max(prof["cells_launches"], 1)
+    bytes_eval = eval_bytes(p.n, nnz, p.mesh.nv)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_eval / (cells_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as fh:
+            tj = json.load(fh)
+        if "cells_bytes_per_site" in tj:
+            traffic = tj["cells_bytes_per_site"] * p.n
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "k_cells_small (Laguerre cell + triangle clip + integrals)",
+                "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_eval,
+                "avg_launch_ms": cells_ms}
+
+    # ---- e2e through the C ABI with host buffers ----
+    xh = torch.tensor(p.x).pin_memory().numpy()
+    yh = torch.tensor(p.y).pin_memory().numpy()
+    nuh = torch.tensor(p.nu).pin_memory().numpy()
+    w0h = torch.zeros(p.n, dtype=torch.float64).pin_memory().numpy()
+    ctx2 = api.Context(local)
+    dmesh2 = ctx2.mesh(p.mesh)
+    api.ot_solve(dmesh2, xh, nuh, x=w0h, y=yh, eps_g=p.tol_rel, stop="rel", precision=args.precision, ctx=ctx2)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e2e_t = 0.0
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        wres = api.ot_solve(dmesh2, xh, nuh, x=w0h, y=yh, eps_g=p.tol_rel, stop="rel",
+                            precision=args.precision, ctx=ctx2)
+        e2e_t += time.perf_counter() - t1
+    assert np.isfinite(wres).all()
+    e2e = {"value": args.steps * world / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * p.n,
+           "d2h_bytes_per_step": 8 * p.n}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sites": p.n, "grid": 512, "precision": args.precision,
+                   "l2": "flushed (512 MB write) before every step", "seed_per_rank": "rank"},
+        "laguerre_evals_per_s": evals_per_s,
+        "solve_stats": {"newton_iters": stats[0].niter, "evals": stats[0].neval, "cg_iters": stats[0].cg_iters,
+                        "eval_ms": stats[0].t_eval_ms, "linsolve_ms": stats[0].t_linsolve_ms,
+                        "max_rel_err": stats[0].max_rel_err, "wall_s_per_step": t_wall / args.steps},
+        "e2e": e2e,
+        "roofline": roofline,
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        te, tl, cores = cpu_sample(W.c2(0))
+        niter = REF_NITER or stats[0].niter
+        neval = REF_NEVAL or stats[0].neval
+        cpu_solve = neval * te + niter * tl
+        line["cpu_baseline"] = {
+            "value": 1.0 / cpu_solve, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"1 Laguerre evaluation ({te:.2f} s) + 1 sparse LU Newton solve ({tl:.2f} s) of the CPU "
+                      f"restatement (reference FP64 arithmetic) on {cores} threads, scaled to {neval} "
+                      f"evaluations + {niter} Newton solves"}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

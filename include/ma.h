@@ -79,6 +79,23 @@ const char* ma_ctx_last_error(const ma_ctx* ctx);
 /* Number of kernel launches the context has issued since it was created. */
 int64_t ma_ctx_launch_count(const ma_ctx* ctx);
 
+/* Device-time profile of the main kernels (CUDA events around each launch). */
+typedef struct ma_profile {
+    double cells_ms;          /* Laguerre cell kernel (main pass) */
+    int64_t cells_launches;
+    double cells_large_ms;    /* large-capacity pass */
+    int64_t cells_large_launches;
+    double bounds_ms;         /* site-tree bounds, once per evaluation */
+    int64_t bounds_launches;
+    double pcg_ms;            /* cooperative CG kernel */
+    int64_t pcg_launches;
+    int64_t pcg_iters;
+    int64_t large_sites;      /* sites redone by the large-capacity pass */
+} ma_profile;
+/* enable != 0: reset the profile and start recording; 0: stop. */
+ma_status ma_ctx_profile(ma_ctx* ctx, int enable);
+ma_status ma_ctx_profile_read(const ma_ctx* ctx, ma_profile* out);
+
 /* --------------------------------------------------------------------- mesh */
 /* Tensor-product grid: vertex (i, j) at (gx[i], gy[j]) with value values[j*nx + i];
  * square (i, j) is split along its (i,j)-(i+1,j+1) diagonal.  Host arrays. */
@@ -110,7 +127,8 @@ typedef struct ma_solve_opts {
     int stop_rule;         /* ma_stop_rule */
     int precision;         /* ma_precision */
     int verbose;           /* print the reference's per-iteration line to stderr */
-    double cg_rtol;        /* relative residual of the preconditioned CG (0: default 1e-10) */
+    double cg_rtol;        /* relative residual of the preconditioned CG; 0 (default): inexact Newton,
+                              min(1e-3, max(1e-12, 0.1 |g| / |g0|)) at each step */
     int64_t cg_maxiter;    /* CG iteration cap (0: default 20000) */
 } ma_solve_opts;
 

@@ -30,6 +30,14 @@ class MaStats(ctypes.Structure):
                 ("t_linsolve_ms", ctypes.c_double)]
 
 
+class MaProfile(ctypes.Structure):
+    _fields_ = [("cells_ms", ctypes.c_double), ("cells_launches", ctypes.c_int64),
+                ("cells_large_ms", ctypes.c_double), ("cells_large_launches", ctypes.c_int64),
+                ("bounds_ms", ctypes.c_double), ("bounds_launches", ctypes.c_int64),
+                ("pcg_ms", ctypes.c_double), ("pcg_launches", ctypes.c_int64), ("pcg_iters", ctypes.c_int64),
+                ("large_sites", ctypes.c_int64)]
+
+
 # every symbol include/ma.h declares, with its ctypes signature
 SIGNATURES = {
     "ma_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -38,6 +46,8 @@ SIGNATURES = {
     "ma_ctx_set_stream": (ctypes.c_int, [_vp, _vp]),
     "ma_ctx_last_error": (ctypes.c_char_p, [_vp]),
     "ma_ctx_launch_count": (ctypes.c_int64, [_vp]),
+    "ma_ctx_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "ma_ctx_profile_read": (ctypes.c_int, [_vp, ctypes.POINTER(MaProfile)]),
     "ma_mesh_create_grid": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.POINTER(_vp)]),
     "ma_mesh_create_triangles": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip,
                                                 ctypes.POINTER(_vp)]),

@@ -78,6 +78,14 @@ class Context:
     def launch_count(self) -> int:
         return int(self.lib.ma_ctx_launch_count(self.h))
 
+    def profile(self, enable: bool = True):
+        _check(self.lib, self.h, self.lib.ma_ctx_profile(self.h, 1 if enable else 0), "ma_ctx_profile")
+
+    def profile_read(self) -> dict:
+        p = L.MaProfile()
+        _check(self.lib, self.h, self.lib.ma_ctx_profile_read(self.h, ctypes.byref(p)), "ma_ctx_profile_read")
+        return {f: getattr(p, f) for f, _ in L.MaProfile._fields_}
+
     def mesh(self, mesh) -> "DeviceMesh":
         return DeviceMesh(self, mesh)
 

@@ -62,13 +62,13 @@ MeshTriDev Mesh::tri_dev() const
     return d;
 }
 
-static constexpr int kScap = 65;  // staging slots per Hessian row (largest cell capacity + diagonal)
 
-// Build the uniform site grid (counting sort by cell).  Positions only: call once
-// per set of sites.
-ma_status build_site_grid(Ctx* c, const Mesh* m, int n, const double* x, const double* y, const double* w)
+// Build the site index: Morton keys over the bounding box of sites and mesh, a radix
+// sort, the radix tree and its node boxes.  Positions only: once per set of sites.
+ma_status build_site_index(Ctx* c, const Mesh* m, int n, const double* x, const double* y, const double* w)
 {
     cudaStream_t s = c->stream;
+    if (n >= (1 << 24)) return fail(c, MA_ERR_INVALID_ARGUMENT, "at most 2^24 - 1 sites per problem");
     MA_CUDA(c, c->keys.ensure(8 * sizeof(unsigned long long)));
     MA_CUDA(c, c->bboxd.ensure(8 * sizeof(double)));
     unsigned long long init[5] = {~0ull, 0ull, ~0ull, 0ull, 0ull};
@@ -85,45 +85,43 @@ ma_status build_site_grid(Ctx* c, const Mesh* m, int n, const double* x, const d
     xmax = std::max(xmax, m->X1);
     ymin = std::min(ymin, m->Y0);
     ymax = std::max(ymax, m->Y1);
-    double W = xmax - xmin, H = ymax - ymin;
-    double sc = std::max(std::max(W, H), 1e-300);
-    W = std::max(W, 1e-9 * sc);
-    H = std::max(H, 1e-9 * sc);
-    double target = std::max(1.0, n / 2.0);
-    int gnx = (int)std::max(1.0, std::floor(std::sqrt(target * W / H)));
-    int gny = (int)std::max(1.0, std::floor(target / gnx));
-    gnx = std::min(gnx, 16384);
-    gny = std::min(gny, 16384);
-    SiteGrid g;
-    g.gnx = gnx;
-    g.gny = gny;
-    g.gx0 = xmin;
-    g.gy0 = ymin;
-    g.gcw = W * (1.0 + 1e-9) / gnx;
-    g.gch = H * (1.0 + 1e-9) / gny;
-    int ncell = gnx * gny;
-    MA_CUDA(c, c->cell.ensure(sizeof(int) * (size_t)n));
-    MA_CUDA(c, c->count.ensure(sizeof(int) * (size_t)ncell));
-    MA_CUDA(c, c->fill.ensure(sizeof(int) * (size_t)ncell));
-    MA_CUDA(c, c->start.ensure(sizeof(int) * ((size_t)ncell + 1)));
-    MA_CUDA(c, c->perm.ensure(sizeof(int) * (size_t)n));
-    MA_CUDA(c, c->sites.ensure(sizeof(SiteD) * (size_t)n));
-    size_t scr = std::max(scan_scratch_ints(ncell), scan_scratch_ints(n));
+    int nb = radix_sort_blocks(n);
+    size_t nn = (size_t)n;
+    size_t ni = nn > 1 ? nn - 1 : 1;
+    MA_CUDA(c, c->mkeys.ensure(sizeof(uint64_t) * nn));
+    MA_CUDA(c, c->mkeys_tmp.ensure(sizeof(uint64_t) * nn));
+    MA_CUDA(c, c->hist.ensure(sizeof(int) * 256 * (size_t)nb));
+    MA_CUDA(c, c->hist_scan.ensure(sizeof(int) * (256 * (size_t)nb + 1)));
+    MA_CUDA(c, c->perm.ensure(sizeof(int) * nn));
+    MA_CUDA(c, c->sites.ensure(sizeof(SiteD) * nn));
+    MA_CUDA(c, c->posf.ensure(sizeof(float2) * nn));
+    size_t scr = std::max(scan_scratch_ints(256 * nb), scan_scratch_ints(n));
     MA_CUDA(c, c->scan_scratch.ensure(sizeof(int) * scr));
-    MA_CUDA(c, cudaMemsetAsync(c->count.p, 0, sizeof(int) * ncell, s));
-    MA_CUDA(c, cudaMemsetAsync(c->fill.p, 0, sizeof(int) * ncell, s));
-    g.cell_start = c->start.as<int>();
-    launch_grid_cells(x, y, n, g, c->cell.as<int>(), c->count.as<int>(), s);
-    launch_scan(c->count.as<int>(), c->start.as<int>(), ncell, c->scan_scratch.as<int>(), s);
-    launch_scatter(c->cell.as<int>(), n, c->start.as<int>(), c->fill.as<int>(), c->perm.as<int>(), s);
-    launch_sort_cells(ncell, c->start.as<int>(), c->perm.as<int>(), s);
-    c->launches += 6;
-    c->grid = g;
-    c->n = n;
-    if (w) {
-        launch_gather(x, y, w, c->perm.as<int>(), n, c->sites.as<SiteD>(), s);
-        c->launches += 1;
+    MA_CUDA(c, c->t_child.ensure(sizeof(int2) * ni));
+    MA_CUDA(c, c->t_range.ensure(sizeof(int2) * ni));
+    MA_CUDA(c, c->t_parent.ensure(sizeof(int) * ni));
+    MA_CUDA(c, c->t_leaf_parent.ensure(sizeof(int) * nn));
+    MA_CUDA(c, c->t_flag.ensure(sizeof(int) * ni));
+    MA_CUDA(c, c->t_box.ensure(sizeof(double4) * ni));
+    MA_CUDA(c, c->t_boxf.ensure(sizeof(float4) * ni));
+    MA_CUDA(c, c->t_mom.ensure(tree_mom_bytes(n)));
+    MA_CUDA(c, c->t_ab.ensure(sizeof(double4) * ni));
+    launch_morton(x, y, n, xmin, ymin, xmax, ymax, c->mkeys.as<uint64_t>(), s);
+    launch_radix_sort(c->mkeys.as<uint64_t>(), c->mkeys_tmp.as<uint64_t>(), n, c->hist.as<int>(),
+                      c->hist_scan.as<int>(), c->scan_scratch.as<int>(), s);
+    launch_perm_gather(c->mkeys.as<uint64_t>(), x, y, w, n, c->perm.as<int>(), c->sites.as<SiteD>(),
+                       c->posf.as<float2>(), s);
+    if (n == 1) {
+        int minus1 = -1;
+        MA_CUDA(c, cudaMemcpyAsync(c->t_leaf_parent.p, &minus1, sizeof(int), cudaMemcpyHostToDevice, s));
     }
+    launch_tree(c->mkeys.as<uint64_t>(), n, c->t_child.as<int2>(), c->t_range.as<int2>(), c->t_parent.as<int>(),
+                c->t_leaf_parent.as<int>(), s);
+    launch_tree_boxes(c->sites.as<SiteD>(), n, c->t_child.as<int2>(), c->t_parent.as<int>(),
+                      c->t_leaf_parent.as<int>(), c->t_flag.as<int>(), c->t_box.as<double4>(),
+                      c->t_boxf.as<float4>(), s);
+    c->launches += 1 + 8 * 5 + 1 + 2;
+    c->n = n;
     return MA_OK;
 }
 
@@ -133,8 +131,10 @@ static ma_status ensure_eval_buffers(Ctx* c, int n, bool mom)
     MA_CUDA(c, c->vpart.ensure(sizeof(double) * (size_t)n));
     if (mom) MA_CUDA(c, c->mom.ensure(sizeof(double) * 6 * (size_t)n));
     MA_CUDA(c, c->rowcnt.ensure(sizeof(int) * (size_t)n));
-    MA_CUDA(c, c->st_col.ensure(sizeof(int) * kScap * (size_t)n));
-    MA_CUDA(c, c->st_val.ensure(sizeof(double) * kScap * (size_t)n));
+    const size_t scap = (size_t)small_row_cap();
+    MA_CUDA(c, c->st_col.ensure(sizeof(int) * scap * (size_t)n));
+    MA_CUDA(c, c->st_val.ensure(sizeof(double) * scap * (size_t)n));
+    MA_CUDA(c, c->big_index.ensure(sizeof(int) * (size_t)n));
     MA_CUDA(c, c->rowptr.ensure(sizeof(int) * ((size_t)n + 1)));
     MA_CUDA(c, c->status.ensure(sizeof(uint32_t) * 4));
     MA_CUDA(c, c->redo.ensure(sizeof(int) * (size_t)n));
@@ -168,37 +168,53 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     ma_status st = ensure_eval_buffers(c, n, f.moments > 0);
     if (st != MA_OK) return st;
     launch_update_weights(w, c->perm.as<int>(), n, c->sites.as<SiteD>(), s);
-    unsigned long long zero = 0;
-    MA_CUDA(c, cudaMemcpyAsync(c->keys.as<unsigned long long>() + 4, &zero, sizeof(zero), cudaMemcpyHostToDevice, s));
-    launch_wmax(w, n, c->keys.as<unsigned long long>() + 4, s);
-    launch_key_to_double(c->keys.as<unsigned long long>() + 4, c->bboxd.as<double>() + 4, 1, s);
-    c->launches += 3;
+    {
+        ProfScope ps(c, &c->profile.bounds_ms, &c->profile.bounds_launches);
+        launch_tree_bounds(c->sites.as<SiteD>(), n, c->t_child.as<int2>(), c->t_parent.as<int>(),
+                           c->t_leaf_parent.as<int>(), c->t_flag.as<int>(), c->t_box.as<double4>(), c->t_mom.p,
+                           c->t_ab.as<double4>(), s);
+    }
+    c->launches += 2;
     MA_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * 4, s));
     MA_CUDA(c, cudaMemsetAsync(c->nredo.p, 0, sizeof(int) * 4, s));
+    MA_CUDA(c, cudaMemsetAsync(c->big_index.p, 0xFF, sizeof(int) * (size_t)n, s));
 
     CellArgs a;
     a.n = n;
     a.sites = c->sites.as<SiteD>();
     a.perm = c->perm.as<int>();
-    a.grid = c->grid;
+    a.tree.n = n;
+    a.tree.child = c->t_child.as<int2>();
+    a.tree.range = c->t_range.as<int2>();
+    a.tree.box = c->t_box.as<double4>();
+    a.tree.boxf = c->t_boxf.as<float4>();
+    a.tree.ab = c->t_ab.as<double4>();
+    a.tree.posf = c->posf.as<float2>();
     a.X0 = m->X0;
     a.Y0 = m->Y0;
     a.X1 = m->X1;
     a.Y1 = m->Y1;
-    a.wmax = c->bboxd.as<double>() + 4;
     a.mass = c->mass.as<double>();
     a.vpart = c->vpart.as<double>();
     a.mom = f.moments > 0 ? c->mom.as<double>() : nullptr;
     a.rowcnt = c->rowcnt.as<int>();
     a.st_col = c->st_col.as<int>();
     a.st_val = c->st_val.as<double>();
-    a.scap = kScap;
+    a.scap = small_row_cap();
     a.status = c->status.as<uint32_t>();
     a.redo = c->redo.as<int>();
     a.nredo = c->nredo.as<int>();
     a.work = nullptr;
     a.nwork = 0;
-    launch_cells(c, m, a, 0, f.moments > 0);
+    a.scratch = nullptr;
+    a.big_index = c->big_index.as<int>();
+    a.big_col = nullptr;
+    a.big_val = nullptr;
+    a.big_cap = large_row_cap();
+    {
+        ProfScope ps(c, &c->profile.cells_ms, &c->profile.cells_launches);
+        launch_cells(c, m, a, 0, f.moments > 0);
+    }
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaStreamSynchronize(s));
@@ -209,9 +225,19 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         b.work = c->redo.as<int>();
         b.nwork = nredo;
         MA_CUDA(c, c->fill.ensure(sizeof(int) * ((size_t)n + 4)));
+        MA_CUDA(c, c->big_work.ensure(large_work_bytes() * (size_t)nredo));
+        MA_CUDA(c, c->big_col.ensure(sizeof(int) * (size_t)large_row_cap() * nredo));
+        MA_CUDA(c, c->big_val.ensure(sizeof(double) * (size_t)large_row_cap() * nredo));
+        b.scratch = c->big_work.p;
+        b.big_col = c->big_col.as<int>();
+        b.big_val = c->big_val.as<double>();
         b.redo = c->fill.as<int>();
         b.nredo = c->nredo.as<int>() + 1;
-        launch_cells(c, m, b, 1, f.moments > 0);
+        {
+            ProfScope ps(c, &c->profile.cells_large_ms, &c->profile.cells_large_launches);
+            launch_cells(c, m, b, 1, f.moments > 0);
+        }
+        c->profile.large_sites += nredo;
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         MA_CUDA(c, cudaStreamSynchronize(s));
@@ -233,7 +259,8 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         MA_CUDA(c, c->col.ensure(sizeof(int) * (size_t)(nnz + 1)));
         MA_CUDA(c, c->val.ensure(sizeof(double) * (size_t)(nnz + 1)));
         launch_csr_compact(n, c->rowptr.as<int>(), c->rowcnt.as<int>(), c->st_col.as<int>(), c->st_val.as<double>(),
-                           kScap, c->col.as<int>(), c->val.as<double>(), s);
+                           small_row_cap(), c->big_index.as<int>(), c->big_col.as<int>(), c->big_val.as<double>(),
+                           large_row_cap(), c->col.as<int>(), c->val.as<double>(), s);
         c->launches += 1;
         c->nnz = nnz;
         c->have_h = true;
@@ -306,12 +333,16 @@ void ma_ctx_destroy(ma_ctx* c)
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->hx, &c->hy, &c->hw, &c->hnu, &c->cell, &c->count, &c->fill, &c->start, &c->perm,
-                      &c->sites, &c->scan_scratch, &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,
+    DevBuf* bufs[] = {&c->hx, &c->hy, &c->hw, &c->hnu, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
+                      &c->perm, &c->sites, &c->posf, &c->scan_scratch, &c->fill, &c->t_child, &c->t_range,
+                      &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab,
+                      &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,
                       &c->st_col, &c->st_val, &c->rowptr, &c->col, &c->val, &c->status, &c->redo, &c->nredo,
-                      &c->stat_partial, &c->stat_out, &c->info, &c->wcur, &c->w0, &c->dirn, &c->g, &c->cg_r,
+                      &c->stat_partial, &c->stat_out, &c->info, &c->big_index, &c->big_col, &c->big_val, &c->big_work, &c->wcur, &c->w0, &c->dirn, &c->g, &c->cg_r,
                       &c->cg_z, &c->cg_p, &c->cg_q, &c->cg_dinv, &c->cg_scal, &c->cg_part};
     for (DevBuf* b : bufs) b->release();
+    if (c->pev[0]) cudaEventDestroy(c->pev[0]);
+    if (c->pev[1]) cudaEventDestroy(c->pev[1]);
     if (c->hstat) cudaFreeHost(c->hstat);
     if (c->hinfo) cudaFreeHost(c->hinfo);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -331,6 +362,28 @@ ma_status ma_ctx_set_stream(ma_ctx* c, void* stream)
 const char* ma_ctx_last_error(const ma_ctx* c) { return c ? c->last_error.c_str() : ""; }
 
 int64_t ma_ctx_launch_count(const ma_ctx* c) { return c ? c->launches : 0; }
+
+ma_status ma_ctx_profile(ma_ctx* c, int enable)
+{
+    if (!c) return MA_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (enable) {
+        if (!c->pev[0]) {
+            if (cudaEventCreate(&c->pev[0]) != cudaSuccess || cudaEventCreate(&c->pev[1]) != cudaSuccess)
+                return MA_ERR_CUDA;
+        }
+        c->profile = ma_profile{};
+    }
+    c->prof = enable != 0;
+    return MA_OK;
+}
+
+ma_status ma_ctx_profile_read(const ma_ctx* c, ma_profile* out)
+{
+    if (!c || !out) return MA_ERR_INVALID_ARGUMENT;
+    *out = c->profile;
+    return MA_OK;
+}
 
 ma_status ma_mesh_create_grid(ma_ctx* c, int nx, int ny, const double* gx, const double* gy, const double* values,
                               ma_mesh** out)
@@ -547,7 +600,7 @@ ma_status ma_kantorovich(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x
     if ((st = stage_in(c, c->hx, x, n, mem, &dx)) != MA_OK) return st;
     if ((st = stage_in(c, c->hy, y, n, mem, &dy)) != MA_OK) return st;
     if ((st = stage_in(c, c->hw, w, n, mem, &dw)) != MA_OK) return st;
-    if ((st = build_site_grid(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
+    if ((st = build_site_index(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
     EvalFlags f;
     f.hessian = true;
     if ((st = run_eval(c, m, (int)n, dw, f)) != MA_OK) return st;
@@ -582,7 +635,7 @@ static ma_status moments_impl(ma_ctx* c, const ma_mesh* m, int64_t n, const doub
     if ((st = stage_in(c, c->hx, x, n, mem, &dx)) != MA_OK) return st;
     if ((st = stage_in(c, c->hy, y, n, mem, &dy)) != MA_OK) return st;
     if ((st = stage_in(c, c->hw, w, n, mem, &dw)) != MA_OK) return st;
-    if ((st = build_site_grid(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
+    if ((st = build_site_index(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
     EvalFlags f;
     f.hessian = false;
     f.moments = order;

@@ -73,6 +73,19 @@ struct Poly {
     float ux[CAP], uy[CAP], ur[CAP];
 };
 
+// fixed-size bit set (one word for the small capacities)
+template <int CAP>
+struct Bits {
+    static constexpr int W = (CAP + 63) / 64;
+    uint64_t w[W];
+    MA_HD void clear()
+    {
+        for (int i = 0; i < W; i++) w[i] = 0;
+    }
+    MA_HD void set(int i) { w[i >> 6] |= 1ull << (i & 63); }
+    MA_HD bool get(int i) const { return (w[i >> 6] >> (i & 63)) & 1ull; }
+};
+
 MA_HD Slot make_slot(int site, const SiteD& c, const Owner& o)
 {
     double dx = dsub(c.x, o.x), dy = dsub(c.y, o.y), dw = dsub(c.w, o.w);
@@ -374,7 +387,9 @@ MA_HD bool clip_poly(const Poly<CAP>& P, Poly<CAP>& Q, int cs, const Slot* slots
 {
     const int n = P.n;
     const Slot c = slots[cs];
-    uint64_t outm = 0;
+    Bits<CAP> outm;
+    outm.clear();
+    int nout = 0;
     for (int k = 0; k < n; k++) {
         int t = test32(P.ux[k], P.uy[k], P.ur[k], c);
         bool out;
@@ -384,18 +399,20 @@ MA_HD bool clip_poly(const Poly<CAP>& P, Poly<CAP>& Q, int cs, const Slot* slots
             int prev = P.lab[k == 0 ? n - 1 : k - 1];
             out = !sym_inside<CAP>(prev, P.lab[k], slots, fx, o, sites, c.site, st);
         }
-        if (out) outm |= (1ull << k);
+        if (out) {
+            outm.set(k);
+            nout++;
+        }
     }
-    if (outm == 0) return false;
-    const uint64_t full = (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
-    if (outm == full) {
+    if (nout == 0) return false;
+    if (nout == n) {
         Q.n = 0;
         return true;
     }
     int m = 0;
     for (int i = 0; i < n; i++) {
         int i1 = (i + 1 == n) ? 0 : i + 1;
-        bool in0 = !((outm >> i) & 1ull), in1 = !((outm >> i1) & 1ull);
+        bool in0 = !outm.get(i), in1 = !outm.get(i1);
         if (in0) {
             if (m >= CAP) { overflow = true; return true; }
             Q.lab[m] = P.lab[i];
@@ -489,7 +506,7 @@ struct Acc {
 // length * rho(mid) / (2 |x_i - x_j|), with length = |e x d| / |d|).
 template <int CAP, bool MOM>
 MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, double c0, double gx,
-                           double gy, Acc& acc, double* hv, uint64_t& touched)
+                           double gy, Acc& acc, double* hv, Bits<CAP>& touched)
 {
     const int n = P.n;
     double x0, y0;
@@ -525,7 +542,7 @@ MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, 
             double crs = fabs(exv * d.dy - eyv * d.dx);
             double mx = 0.5 * (ax + bx), my = 0.5 * (ay + by);
             hv[lab] += crs * (c0 + gx * mx + gy * my);
-            touched |= (1ull << lab);
+            touched.set(lab);
         }
         ax = bx;
         ay = by;

@@ -9,10 +9,16 @@
 
 namespace ma {
 
-struct SiteGrid {
-    int gnx, gny;
-    double gx0, gy0, gcw, gch;  // cell (cx, cy) = [gx0 + cx gcw, ...) x [gy0 + cy gch, ...)
-    const int* cell_start;      // gnx * gny + 1, positions in the sorted site array
+// binary radix tree over the Morton-sorted sites; internal node 0 is the root;
+// a child index with the top bit set is a leaf (sorted site position)
+struct SiteTree {
+    int n;
+    const int2* child;
+    const int2* range;    // first, last sorted position covered by the node
+    const double4* box;   // x0, y0, x1, y1 (exact)
+    const float4* boxf;   // the same rounded outwards
+    const double4* ab;    // alpha, beta_x, beta_y: phi_j >= alpha + beta . x_j over the node
+    const float2* posf;   // sorted site positions (FP32)
 };
 
 // implicit grid mesh: vertex (i, j) at (gx[i], gy[j]) with value val[j * nx + i];
@@ -44,9 +50,8 @@ struct CellArgs {
     int n;
     const SiteD* sites;  // sorted by grid cell
     const int* perm;     // sorted position -> original index
-    SiteGrid grid;
+    SiteTree tree;
     double X0, Y0, X1, Y1;   // box of the cell stage (contains the mesh)
-    const double* wmax;      // device scalar: max weight
     // outputs, original order
     double* mass;
     double* vpart;           // w_i m_i - int_{cell i} rho |x - x_i|^2
@@ -58,28 +63,45 @@ struct CellArgs {
     uint32_t* status;
     int* redo;
     int* nredo;
-    const int* work;         // when non-null, process only these sorted positions
+    const int* work;         // large-capacity pass: the sorted positions to redo
     int nwork;
+    void* scratch;           // large-capacity pass: one workspace per work item
+    int* big_index;          // per site: row slot in the side buffer, -1 otherwise
+    int* big_col;
+    double* big_val;
+    int big_cap;
 };
 
 // launches (all asynchronous on `s`)
 void launch_bbox(const double* x, const double* y, const double* w, int n, unsigned long long* keys,
                  cudaStream_t s);
-void launch_grid_cells(const double* x, const double* y, int n, SiteGrid g, int* cell, int* count,
-                       cudaStream_t s);
-void launch_scatter(const int* cell, int n, const int* start, int* fill, int* perm, cudaStream_t s);
-void launch_sort_cells(int ncell, const int* start, int* perm, cudaStream_t s);
-void launch_gather(const double* x, const double* y, const double* w, const int* perm, int n, SiteD* out,
-                   cudaStream_t s);
 void launch_update_weights(const double* w, const int* perm, int n, SiteD* sites, cudaStream_t s);
-void launch_wmax(const double* w, int n, unsigned long long* key, cudaStream_t s);
 void launch_key_to_double(const unsigned long long* key, double* out, int count, cudaStream_t s);
+// site index (ma_index.cu)
+void launch_morton(const double* x, const double* y, int n, double x0, double y0, double x1, double y1,
+                   uint64_t* keys, cudaStream_t s);
+int radix_sort_blocks(int n);
+void launch_radix_sort(uint64_t* keys, uint64_t* tmp, int n, int* hist, int* hist_scan, int* scan_scratch,
+                       cudaStream_t s);
+void launch_perm_gather(const uint64_t* keys, const double* x, const double* y, const double* w, int n, int* perm,
+                        SiteD* sites, float2* posf, cudaStream_t s);
+void launch_tree(const uint64_t* keys, int n, int2* child, int2* range, int* parent, int* leaf_parent,
+                 cudaStream_t s);
+void launch_tree_boxes(const SiteD* sites, int n, const int2* child, const int* parent, const int* leaf_parent,
+                       int* flag, double4* box, float4* boxf, cudaStream_t s);
+size_t tree_mom_bytes(int n);
+void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int* parent, const int* leaf_parent,
+                        int* flag, const double4* box, void* mom, double4* ab, cudaStream_t s);
 void launch_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);  // exclusive, out has n+1
 size_t scan_scratch_ints(int n);
 void launch_cells_grid(const CellArgs& a, const MeshGridDev& m, int cap_kind, bool mom, cudaStream_t s);
 void launch_cells_tri(const CellArgs& a, const MeshTriDev& m, int cap_kind, bool mom, cudaStream_t s);
 void launch_csr_compact(int n, const int* rowptr, const int* rowcnt, const int* st_col, const double* st_val,
-                        int scap, int* col, double* val, cudaStream_t s);
+                        int scap, const int* big_index, const int* big_col, const double* big_val, int big_cap,
+                        int* col, double* val, cudaStream_t s);
+size_t large_work_bytes();
+int large_row_cap();
+int small_row_cap();
 
 // deterministic reductions: out[0] = sum(vpart) - sum(nu * w) (if nu), [1] = sum(mass),
 // [2] = min(mass), [3] = |mass - nu|_2, [4] = max |mass - nu| / nu

@@ -88,22 +88,6 @@ void launch_bbox(const double* x, const double* y, const double* w, int n, unsig
     k_bbox<<<g, b, 0, s>>>(x, y, w, n, keys);
 }
 
-__global__ void k_wmax(const double* w, int n, unsigned long long* key)
-{
-    unsigned long long m = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = max(m, dkey(w[i]));
-    m = block_reduce_key(m, KMax());
-    if (threadIdx.x == 0) atomicMax(key, m);
-}
-
-void launch_wmax(const double* w, int n, unsigned long long* key, cudaStream_t s)
-{
-    int b = 256, g = (n + b - 1) / b;
-    if (g > 1216) g = 1216;
-    if (g < 1) g = 1;
-    k_wmax<<<g, b, 0, s>>>(w, n, key);
-}
-
 __global__ void k_key_to_double(const unsigned long long* key, double* out, int count)
 {
     int i = threadIdx.x;
@@ -113,87 +97,6 @@ __global__ void k_key_to_double(const unsigned long long* key, double* out, int 
 void launch_key_to_double(const unsigned long long* key, double* out, int count, cudaStream_t s)
 {
     k_key_to_double<<<1, 32, 0, s>>>(key, out, count);
-}
-
-__device__ __forceinline__ int grid_cx(const SiteGrid& g, double x)
-{
-    int c = (int)floor((x - g.gx0) / g.gcw);
-    return c < 0 ? 0 : (c >= g.gnx ? g.gnx - 1 : c);
-}
-__device__ __forceinline__ int grid_cy(const SiteGrid& g, double y)
-{
-    int c = (int)floor((y - g.gy0) / g.gch);
-    return c < 0 ? 0 : (c >= g.gny ? g.gny - 1 : c);
-}
-
-__global__ void k_grid_cells(const double* x, const double* y, int n, SiteGrid g, int* cell, int* count)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int c = grid_cy(g, y[i]) * g.gnx + grid_cx(g, x[i]);
-    cell[i] = c;
-    atomicAdd(&count[c], 1);
-}
-
-void launch_grid_cells(const double* x, const double* y, int n, SiteGrid g, int* cell, int* count, cudaStream_t s)
-{
-    k_grid_cells<<<(n + 255) / 256, 256, 0, s>>>(x, y, n, g, cell, count);
-}
-
-__global__ void k_scatter(const int* cell, int n, const int* start, int* fill, int* perm)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int c = cell[i];
-    int p = start[c] + atomicAdd(&fill[c], 1);
-    perm[p] = i;
-}
-
-void launch_scatter(const int* cell, int n, const int* start, int* fill, int* perm, cudaStream_t s)
-{
-    k_scatter<<<(n + 255) / 256, 256, 0, s>>>(cell, n, start, fill, perm);
-}
-
-// sort each cell's segment of perm by original index (the scatter's order is
-// arbitrary; sorting makes every later result independent of it)
-__global__ void k_sort_cells(int ncell, const int* start, int* perm)
-{
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int a = start[c], b = start[c + 1];
-    for (int i = a + 1; i < b; i++) {
-        int v = perm[i];
-        int j = i - 1;
-        while (j >= a && perm[j] > v) {
-            perm[j + 1] = perm[j];
-            j--;
-        }
-        perm[j + 1] = v;
-    }
-}
-
-void launch_sort_cells(int ncell, const int* start, int* perm, cudaStream_t s)
-{
-    k_sort_cells<<<(ncell + 255) / 256, 256, 0, s>>>(ncell, start, perm);
-}
-
-__global__ void k_gather(const double* x, const double* y, const double* w, const int* perm, int n, SiteD* out)
-{
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int i = perm[k];
-    SiteD s;
-    s.x = x[i];
-    s.y = y[i];
-    s.w = w[i];
-    s.pad = 0.0;
-    out[k] = s;
-}
-
-void launch_gather(const double* x, const double* y, const double* w, const int* perm, int n, SiteD* out,
-                   cudaStream_t s)
-{
-    k_gather<<<(n + 255) / 256, 256, 0, s>>>(x, y, w, perm, n, out);
 }
 
 __global__ void k_update_weights(const double* w, const int* perm, int n, SiteD* sites)
@@ -392,30 +295,29 @@ struct TriVisitor {
 // K1 + K2: one Laguerre cell per thread
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ double block_gap(const SiteGrid& g, double x, double y, int cx, int cy, int r)
-{
-    double d = INFINITY;
-    bool covers = true;
-    if (cx - r > 0) { covers = false; d = fmin(d, x - (g.gx0 + (cx - r) * g.gcw)); }
-    if (cx + r < g.gnx - 1) { covers = false; d = fmin(d, (g.gx0 + (cx + r + 1) * g.gcw) - x); }
-    if (cy - r > 0) { covers = false; d = fmin(d, y - (g.gy0 + (cy - r) * g.gch)); }
-    if (cy + r < g.gny - 1) { covers = false; d = fmin(d, (g.gy0 + (cy + r + 1) * g.gch) - y); }
-    if (covers) return INFINITY;
-    // cell boundaries are fuzzy by the rounding of the cell assignment
-    d -= 1e-12 * (fabs(g.gx0) + fabs(g.gy0) + g.gnx * g.gcw + g.gny * g.gch);
-    return d < 0 ? 0 : d;
-}
+// per-site workspace: a local variable in the main kernel, a slice of global
+// scratch in the large-capacity kernel
+template <int CAP>
+struct Work {
+    Slot slots[CAP];
+    Poly<CAP> PA, PB;
+    double hv[CAP];
+    Nb64 nb[CAP];
+    int map[CAP];
+    int cols[CAP];
+    double vals[CAP];
+};
 
 template <int CAP>
-__device__ __forceinline__ void compact_slots(Poly<CAP>& P, Slot* slots, int& ns)
+__device__ __forceinline__ void compact_slots(Poly<CAP>& P, Slot* slots, int* map, int& ns)
 {
-    uint64_t used = 0;
+    Bits<CAP> used;
+    used.clear();
     for (int e = 0; e < P.n; e++)
-        if (P.lab[e] >= 0) used |= 1ull << P.lab[e];
-    int map[CAP];
+        if (P.lab[e] >= 0) used.set(P.lab[e]);
     int m = 0;
     for (int s = 0; s < ns; s++) {
-        if ((used >> s) & 1ull) {
+        if (used.get(s)) {
             map[s] = m;
             if (m != s) slots[m] = slots[s];
             m++;
@@ -428,8 +330,43 @@ __device__ __forceinline__ void compact_slots(Poly<CAP>& P, Slot* slots, int& ns
     ns = m;
 }
 
+// Can no site of internal node nd cut polygon P?  With phi_j >= alpha + beta.x_j
+// over the node and the node's box [c - h, c + h]:
+//   pi_ij(p) / 2 = p.(x_j - x_i) + phi_i - phi_j
+//              <= (p - beta).(c - x_i) + |p_x - beta_x| h_x + |p_y - beta_y| h_y - K,
+//   K = alpha + beta.x_i - phi_i,
+// convex in p, so it suffices that it is negative at every vertex of P.  FP64
+// node terms, FP32 per-vertex loop with a bound on every rounding and on the
+// vertex radii.
+template <int CAP>
+__device__ __forceinline__ bool node_harmless(const Poly<CAP>& P, const Owner& o, double phi_o, const double4 bx,
+                                              const double4 ab)
+{
+    if (!(ab.x > -INFINITY)) return false;
+    double ex = o.x - ab.y, ey = o.y - ab.z;
+    double cx = 0.5 * (bx.x + bx.z) - o.x, cy = 0.5 * (bx.y + bx.w) - o.y;
+    double hx = 0.5 * (bx.z - bx.x), hy = 0.5 * (bx.w - bx.y);
+    double t1 = ab.y * o.x, t2 = ab.z * o.y;
+    double K = ab.x + t1 + t2 - phi_o;
+    double kerr = 1e-15 * (fabs(ab.x) + fabs(t1) + fabs(t2) + fabs(phi_o));
+    double cerr = 1e-15 * (fabs(bx.x) + fabs(bx.z) + fabs(bx.y) + fabs(bx.w) + fabs(o.x) + fabs(o.y));
+    float fex = (float)ex, fey = (float)ey, fcx = (float)cx, fcy = (float)cy;
+    float fhx = (float)hx * 1.000001f + 1e-38f, fhy = (float)hy * 1.000001f + 1e-38f;
+    float fK = (float)K, fke = (float)kerr * 1.0001f, fce = (float)cerr * 1.0001f;
+    float L = fabsf(fcx) + fabsf(fcy) + fhx + fhy;
+    float e0 = 1.2e-7f * (fabsf(fex) + fabsf(fey));
+    for (int v = 0; v < P.n; v++) {
+        float qx = fex + P.ux[v], qy = fey + P.uy[v];
+        float T = qx * fcx + qy * fcy + fabsf(qx) * fhx + fabsf(qy) * fhy - fK;
+        float S = fabsf(qx * fcx) + fabsf(qy * fcy) + fabsf(qx) * fhx + fabsf(qy) * fhy + fabsf(fK);
+        float err = 1e-6f * S + (P.ur[v] + e0) * L * 1.0001f + fke + (fabsf(qx) + fabsf(qy)) * fce + 1e-36f;
+        if (!(T + err < 0.0f)) return false;
+    }
+    return true;
+}
+
 template <int CAP, bool MOM, class Mesh>
-__device__ void process_site(const CellArgs& A, const Mesh& M, int k)
+__device__ void process_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>& W, int big_slot)
 {
     const SiteD S = A.sites[k];
     const int gi = A.perm[k];
@@ -438,11 +375,10 @@ __device__ void process_site(const CellArgs& A, const Mesh& M, int k)
     bool overflow = false;
     bool empty = false;
 
-    Slot slots[CAP];
+    Slot* slots = W.slots;
     int ns = 0;
-    Poly<CAP> PA, PB;
-    Poly<CAP>* P = &PA;
-    Poly<CAP>* Q = &PB;
+    Poly<CAP>* P = &W.PA;
+    Poly<CAP>* Q = &W.PB;
 
     Fixed box;
     box.n = 4;
@@ -462,70 +398,84 @@ __device__ void process_site(const CellArgs& A, const Mesh& M, int k)
         empty = true;
     }
 
-    const SiteGrid& g = A.grid;
-    const int cx = grid_cx(g, S.x), cy = grid_cy(g, S.y);
-    const double dwmax = *A.wmax - S.w;
-
-    // ---------------- cell stage ----------------
-    for (int r = 0; !empty; r++) {
-        bool any = false;
-        for (int yy = cy - r; yy <= cy + r && !empty; yy++) {
-            if (yy < 0 || yy >= g.gny) continue;
-            const bool full_row = (yy == cy - r) || (yy == cy + r);
-            const int stepx = full_row ? 1 : (r > 0 ? 2 * r : 1);
-            for (int xx = cx - r; xx <= cx + r && !empty; xx += stepx) {
-                if (xx < 0 || xx >= g.gnx) continue;
-                any = true;
-                const int c = yy * g.gnx + xx;
-                const int qa = g.cell_start[c], qb = g.cell_start[c + 1];
-                for (int q = qa; q < qb; q++) {
-                    if (q == k) continue;
-                    const SiteD C = A.sites[q];
-                    if (C.x == S.x && C.y == S.y) {
-                        // coincident sites: the larger weight, then the lower index, keeps the cell
-                        int gj = A.perm[q];
-                        if (C.w > S.w || (C.w == S.w && gj < gi)) {
-                            empty = true;
-                            break;
-                        }
-                        continue;
-                    }
-                    if (ns == CAP) {
-                        compact_slots(*P, slots, ns);
-                        if (ns == CAP) {
-                            overflow = true;
-                            goto cell_done;
-                        }
-                    }
-                    slots[ns] = make_slot(q, C, o);
-                    if (clip_poly(*P, *Q, ns, slots, box, o, A.sites, st, overflow)) {
-                        if (overflow) goto cell_done;
-                        Poly<CAP>* t = P;
-                        P = Q;
-                        Q = t;
-                        ns++;
-                        if (P->n == 0) {
-                            empty = true;
-                            break;
-                        }
-                    }
+    // ---------------- cell stage: branch and bound over the site tree ----------------
+    {
+        const SiteTree& T = A.tree;
+        const double phi_o = 0.5 * (S.x * S.x + S.y * S.y - S.w);
+        const float ox = (float)S.x, oy = (float)S.y;
+        constexpr int kStack = 80;
+        constexpr int kBucket = 8;
+        int stack[kStack];
+        int sp = 0;
+        if (T.n >= 2 && !empty) stack[sp++] = 0;
+        auto visit = [&](int q) -> bool {  // clip by sorted site q; false when the cell became empty
+            if (q == k) return true;
+            const SiteD C = A.sites[q];
+            if (C.x == S.x && C.y == S.y) {
+                // coincident sites: the larger weight, then the lower index, keeps the cell
+                int gj = A.perm[q];
+                if (C.w > S.w || (C.w == S.w && gj < gi)) return false;
+                return true;
+            }
+            if (ns == CAP) {
+                compact_slots(*P, slots, W.map, ns);
+                if (ns == CAP) {
+                    overflow = true;
+                    return true;
                 }
             }
+            slots[ns] = make_slot(q, C, o);
+            if (clip_poly(*P, *Q, ns, slots, box, o, A.sites, st, overflow)) {
+                if (overflow) return true;
+                Poly<CAP>* t = P;
+                P = Q;
+                Q = t;
+                ns++;
+                if (P->n == 0) return false;
+            }
+            return true;
+        };
+        auto dist2 = [&](int c) -> float {
+            if (c < 0) {
+                float2 p = T.posf[c & 0x7fffffff];
+                float dx = p.x - ox, dy = p.y - oy;
+                return dx * dx + dy * dy;
+            }
+            float4 b = T.boxf[c];
+            float dx = fmaxf(fmaxf(b.x - ox, ox - b.z), 0.0f), dy = fmaxf(fmaxf(b.y - oy, oy - b.w), 0.0f);
+            return dx * dx + dy * dy;
+        };
+        while (sp > 0 && !empty && !overflow) {
+            int nd = stack[--sp];
+            if (nd < 0) {
+                if (!visit(nd & 0x7fffffff)) empty = true;
+                continue;
+            }
+            int2 rg = T.range[nd];
+            bool contains = rg.x <= k && k <= rg.y;
+            if (!contains && node_harmless(*P, o, phi_o, T.box[nd], T.ab[nd])) continue;
+            if (rg.y - rg.x < kBucket) {
+                for (int q = rg.x; q <= rg.y && !empty && !overflow; q++)
+                    if (!visit(q)) empty = true;
+                continue;
+            }
+            int2 ch = T.child[nd];
+            if (sp > kStack - 2) {
+                overflow = true;
+                break;
+            }
+            // nearer child on top
+            if (dist2(ch.x) <= dist2(ch.y)) {
+                stack[sp++] = ch.y;
+                stack[sp++] = ch.x;
+            } else {
+                stack[sp++] = ch.x;
+                stack[sp++] = ch.y;
+            }
         }
-        if (empty || !any) break;
-        // security radius: farther sites cannot cut when gap^2 - 2 gap R >= wmax - w_i
-        float R = 0.0f;
-        for (int e = 0; e < P->n; e++) {
-            float ux = P->ux[e], uy = P->uy[e];
-            float rr = sqrtf(ux * ux + uy * uy) * 1.000001f + 2.0f * P->ur[e];
-            R = fmaxf(R, rr);
-        }
-        double gap = block_gap(g, S.x, S.y, cx, cy, r);
-        if (gap == INFINITY) break;
-        double Rd = (double)R * (1.0 + 1e-6) + 1e-300;
-        if (gap > Rd && gap * gap - 2.0 * gap * Rd >= dwmax * (1.0 + 1e-9) + 1e-300) break;
+        if (empty) P->n = 0;
     }
-cell_done:
+
     if (overflow) {
         if (A.redo) {
             int p = atomicAdd(A.nredo, 1);
@@ -536,12 +486,13 @@ cell_done:
     }
 
     Acc acc{0, 0, 0, 0, 0, 0, 0};
-    double hv[CAP];
-    Nb64 nb[CAP];
-    uint64_t touched = 0;
+    double* hv = W.hv;
+    Nb64* nb = W.nb;
+    Bits<CAP> touched;
+    touched.clear();
     int m = 0;
     if (!empty && P->n > 0) {
-        compact_slots(*P, slots, ns);
+        compact_slots(*P, slots, W.map, ns);
         m = ns;
         for (int s = 0; s < m; s++) {
             nb[s] = make_nb64(A.sites[slots[s].site], o);
@@ -567,27 +518,27 @@ cell_done:
         }
 
         // ---------------- triangle stage ----------------
-        Poly<CAP>* W = P;
-        Poly<CAP>* V = Q;
+        Poly<CAP>* Wp = P;
+        Poly<CAP>* Vp = Q;
         M.visit(o, bx0, by0, bx1, by1, [&](const Fixed& T, double c0, double gx, double gy) {
             if (overflow) return;
-            W->n = 3;
+            Wp->n = 3;
             for (int e = 0; e < 3; e++) {
-                W->lab[e] = -1 - e;
-                W->ux[e] = T.ux[e];
-                W->uy[e] = T.uy[e];
-                W->ur[e] = T.ur[e];
+                Wp->lab[e] = -1 - e;
+                Wp->ux[e] = T.ux[e];
+                Wp->uy[e] = T.uy[e];
+                Wp->ur[e] = T.ur[e];
             }
             for (int s = 0; s < m; s++) {
-                if (clip_poly(*W, *V, s, slots, T, o, A.sites, st, overflow)) {
+                if (clip_poly(*Wp, *Vp, s, slots, T, o, A.sites, st, overflow)) {
                     if (overflow) return;
-                    Poly<CAP>* t = W;
-                    W = V;
-                    V = t;
-                    if (W->n == 0) return;
+                    Poly<CAP>* t = Wp;
+                    Wp = Vp;
+                    Vp = t;
+                    if (Wp->n == 0) return;
                 }
             }
-            integrate_piece<CAP, MOM>(*W, nb, T, c0, gx, gy, acc, hv, touched);
+            integrate_piece<CAP, MOM>(*Wp, nb, T, c0, gx, gy, acc, hv, touched);
         });
         if (overflow) {
             if (A.redo) {
@@ -613,12 +564,12 @@ cell_done:
     }
     if (A.rowcnt) {
         // off-diagonal entries sorted by original index, diagonal in place
-        int cols[CAP];
-        double vals[CAP];
+        int* cols = W.cols;
+        double* vals = W.vals;
         int cnt = 0;
         double diag = 0.0;
         for (int s = 0; s < m; s++) {
-            if (!((touched >> s) & 1ull)) continue;
+            if (!touched.get(s)) continue;
             double d2 = nb[s].dx * nb[s].dx + nb[s].dy * nb[s].dy;
             double v = -hv[s] / (2.0 * d2);
             diag -= v;
@@ -635,11 +586,18 @@ cell_done:
         }
         int total = cnt > 0 ? cnt + 1 : 0;
         A.rowcnt[gi] = total;
-        if (total > A.scap) {
-            st |= ST_ROW_OVERFLOW;
-        } else if (total > 0) {
-            int* oc = A.st_col + (size_t)gi * A.scap;
-            double* ov = A.st_val + (size_t)gi * A.scap;
+        int* oc;
+        double* ov;
+        if (big_slot >= 0) {
+            // large rows go to the side buffer of the large-capacity pass
+            oc = A.big_col + (size_t)big_slot * A.big_cap;
+            ov = A.big_val + (size_t)big_slot * A.big_cap;
+            A.big_index[gi] = big_slot;
+        } else {
+            oc = A.st_col + (size_t)gi * A.scap;
+            ov = A.st_val + (size_t)gi * A.scap;
+        }
+        if (total > 0) {
             int w = 0;
             bool placed = false;
             for (int j = 0; j < cnt; j++) {
@@ -663,87 +621,74 @@ cell_done:
 }
 
 constexpr int kCapSmall = 48;
-constexpr int kCapLarge = 64;
+constexpr int kCapLarge = 256;
 
-template <int CAP, bool MOM>
-__global__ void __launch_bounds__(128) k_cells_grid(CellArgs A, GridVisitor M)
+template <int CAP, bool MOM, class Mesh>
+__global__ void __launch_bounds__(128) k_cells_small(CellArgs A, Mesh M)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int k;
-    if (A.work) {
-        if (t >= A.nwork) return;
-        k = A.work[t];
-    } else {
-        if (t >= A.n) return;
-        k = t;
-    }
-    process_site<CAP, MOM>(A, M, k);
+    if (t >= A.n) return;
+    Work<CAP> W;
+    process_site<CAP, MOM>(A, M, t, W, -1);
 }
 
-template <int CAP, bool MOM>
-__global__ void __launch_bounds__(128) k_cells_tri(CellArgs A, TriVisitor M)
+// the sites listed in A.work, each with a workspace in global scratch
+template <int CAP, bool MOM, class Mesh>
+__global__ void __launch_bounds__(64) k_cells_large(CellArgs A, Mesh M)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int k;
-    if (A.work) {
-        if (t >= A.nwork) return;
-        k = A.work[t];
+    if (t >= A.nwork) return;
+    Work<CAP>* W = reinterpret_cast<Work<CAP>*>(A.scratch) + t;
+    process_site<CAP, MOM>(A, M, A.work[t], *W, t);
+}
+
+size_t large_work_bytes() { return sizeof(Work<kCapLarge>); }
+int large_row_cap() { return kCapLarge + 1; }
+int small_row_cap() { return kCapSmall + 1; }
+
+template <class Mesh>
+static void launch_cells_any(const CellArgs& a, const Mesh& v, int cap_kind, bool mom, cudaStream_t s)
+{
+    if (cap_kind == 0) {
+        if (a.n <= 0) return;
+        int b = 128, g = (a.n + b - 1) / b;
+        if (mom)
+            k_cells_small<kCapSmall, true><<<g, b, 0, s>>>(a, v);
+        else
+            k_cells_small<kCapSmall, false><<<g, b, 0, s>>>(a, v);
     } else {
-        if (t >= A.n) return;
-        k = t;
+        if (a.nwork <= 0) return;
+        int b = 64, g = (a.nwork + b - 1) / b;
+        if (mom)
+            k_cells_large<kCapLarge, true><<<g, b, 0, s>>>(a, v);
+        else
+            k_cells_large<kCapLarge, false><<<g, b, 0, s>>>(a, v);
     }
-    process_site<CAP, MOM>(A, M, k);
 }
 
 void launch_cells_grid(const CellArgs& a, const MeshGridDev& m, int cap_kind, bool mom, cudaStream_t s)
 {
-    int n = a.work ? a.nwork : a.n;
-    if (n <= 0) return;
-    int b = 128, g = (n + b - 1) / b;
-    GridVisitor v{m};
-    if (cap_kind == 0) {
-        if (mom)
-            k_cells_grid<kCapSmall, true><<<g, b, 0, s>>>(a, v);
-        else
-            k_cells_grid<kCapSmall, false><<<g, b, 0, s>>>(a, v);
-    } else {
-        if (mom)
-            k_cells_grid<kCapLarge, true><<<g, b, 0, s>>>(a, v);
-        else
-            k_cells_grid<kCapLarge, false><<<g, b, 0, s>>>(a, v);
-    }
+    launch_cells_any(a, GridVisitor{m}, cap_kind, mom, s);
 }
 
 void launch_cells_tri(const CellArgs& a, const MeshTriDev& m, int cap_kind, bool mom, cudaStream_t s)
 {
-    int n = a.work ? a.nwork : a.n;
-    if (n <= 0) return;
-    int b = 128, g = (n + b - 1) / b;
-    TriVisitor v{m};
-    if (cap_kind == 0) {
-        if (mom)
-            k_cells_tri<kCapSmall, true><<<g, b, 0, s>>>(a, v);
-        else
-            k_cells_tri<kCapSmall, false><<<g, b, 0, s>>>(a, v);
-    } else {
-        if (mom)
-            k_cells_tri<kCapLarge, true><<<g, b, 0, s>>>(a, v);
-        else
-            k_cells_tri<kCapLarge, false><<<g, b, 0, s>>>(a, v);
-    }
+    launch_cells_any(a, TriVisitor{m}, cap_kind, mom, s);
 }
 
 // ---------------------------------------------------------------------------
 // K4: CSR compaction
 // ---------------------------------------------------------------------------
 __global__ void k_csr_compact(int n, const int* rowptr, const int* rowcnt, const int* st_col, const double* st_val,
-                              int scap, int* col, double* val)
+                              int scap, const int* big_index, const int* big_col, const double* big_val, int big_cap,
+                              int* col, double* val)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int c = rowcnt[i], o = rowptr[i];
-    const int* sc = st_col + (size_t)i * scap;
-    const double* sv = st_val + (size_t)i * scap;
+    int b = big_index[i];
+    const int* sc = b >= 0 ? big_col + (size_t)b * big_cap : st_col + (size_t)i * scap;
+    const double* sv = b >= 0 ? big_val + (size_t)b * big_cap : st_val + (size_t)i * scap;
     for (int j = 0; j < c; j++) {
         col[o + j] = sc[j];
         val[o + j] = sv[j];
@@ -751,9 +696,11 @@ __global__ void k_csr_compact(int n, const int* rowptr, const int* rowcnt, const
 }
 
 void launch_csr_compact(int n, const int* rowptr, const int* rowcnt, const int* st_col, const double* st_val,
-                        int scap, int* col, double* val, cudaStream_t s)
+                        int scap, const int* big_index, const int* big_col, const double* big_val, int big_cap,
+                        int* col, double* val, cudaStream_t s)
 {
-    k_csr_compact<<<(n + 255) / 256, 256, 0, s>>>(n, rowptr, rowcnt, st_col, st_val, scap, col, val);
+    k_csr_compact<<<(n + 255) / 256, 256, 0, s>>>(n, rowptr, rowcnt, st_col, st_val, scap, big_index, big_col,
+                                                  big_val, big_cap, col, val);
 }
 
 // ---------------------------------------------------------------------------

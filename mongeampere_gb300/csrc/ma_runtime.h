@@ -68,18 +68,23 @@ struct Ctx {
 
     // inputs (when given in host memory)
     DevBuf hx, hy, hw, hnu;
-    // site grid
+    // site index: Morton-sorted sites and their radix tree
     int n = 0;
-    SiteGrid grid{};
-    DevBuf cell, count, fill, start, perm, sites, scan_scratch;
+    DevBuf mkeys, mkeys_tmp, hist, hist_scan, perm, sites, posf, scan_scratch, fill;
+    DevBuf t_child, t_range, t_parent, t_leaf_parent, t_flag, t_box, t_boxf, t_mom, t_ab;
     DevBuf keys, bboxd;  // ordered keys and their doubles
     // evaluation outputs
     DevBuf mass, vpart, mom, rowcnt, st_col, st_val, rowptr, col, val, status, redo, nredo, stat_partial, stat_out;
+    DevBuf big_index, big_col, big_val, big_work;  // large-capacity pass
     DevBuf info;  // status, nredo, nnz
     int64_t nnz = 0;
     bool have_h = false;
     // solver work vectors
     DevBuf wcur, w0, dirn, g, cg_r, cg_z, cg_p, cg_q, cg_dinv, cg_scal, cg_part;
+    // profiling (CUDA events around the main kernels)
+    bool prof = false;
+    ma_profile profile{};
+    cudaEvent_t pev[2] = {nullptr, nullptr};
     // pinned host mirror of small results
     double* hstat = nullptr;  // 16 doubles
     int* hinfo = nullptr;     // 8 ints
@@ -96,13 +101,34 @@ ma_status cuda_fail(Ctx* c, cudaError_t e, const char* what);
     } while (0)
 
 // evaluation pipeline (device pointers)
-ma_status build_site_grid(Ctx* c, const Mesh* m, int n, const double* x, const double* y, const double* w);
+ma_status build_site_index(Ctx* c, const Mesh* m, int n, const double* x, const double* y, const double* w);
 struct EvalFlags {
     bool hessian = true;
     int moments = 0;  // 0 none, 1 first, 2 second
     const double* nu = nullptr;  // when given, stat_out[0] = value - <nu, w>
 };
 ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlags& f);
+
+// bracket an enqueue with profiling events; the elapsed time is added after a sync
+struct ProfScope {
+    Ctx* c;
+    double* ms;
+    int64_t* cnt;
+    ProfScope(Ctx* c_, double* ms_, int64_t* cnt_) : c(c_), ms(ms_), cnt(cnt_)
+    {
+        if (c->prof) cudaEventRecord(c->pev[0], c->stream);
+    }
+    ~ProfScope()
+    {
+        if (!c->prof) return;
+        cudaEventRecord(c->pev[1], c->stream);
+        cudaEventSynchronize(c->pev[1]);
+        float t = 0;
+        cudaEventElapsedTime(&t, c->pev[0], c->pev[1]);
+        *ms += t;
+        (*cnt)++;
+    }
+};
 
 }  // namespace ma
 

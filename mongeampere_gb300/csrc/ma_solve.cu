@@ -235,11 +235,15 @@ static ma_status pcg_solve(Ctx* c, int n, const double* b, double* x, double rto
     a.rtol = rtol;
     a.maxiter = maxiter;
     void* args[] = {&a};
-    MA_CUDA(c, cudaLaunchCooperativeKernel((void*)k_pcg, dim3(nb), dim3(kPcgThreads), args, 0, s));
+    {
+        ProfScope ps(c, &c->profile.pcg_ms, &c->profile.pcg_launches);
+        MA_CUDA(c, cudaLaunchCooperativeKernel((void*)k_pcg, dim3(nb), dim3(kPcgThreads), args, 0, s));
+    }
     c->launches += 2;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat + 8, c->cg_scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaStreamSynchronize(s));
     if (iters) *iters = (int)c->hstat[8];
+    c->profile.pcg_iters += (int64_t)c->hstat[8];
     if (relres) *relres = c->hstat[10] > 0 ? c->hstat[9] / c->hstat[10] : 0.0;
     return MA_OK;
 }
@@ -258,7 +262,7 @@ void ma_solve_opts_default(ma_solve_opts* o)
     o->stop_rule = MA_STOP_GRAD_NORM;
     o->precision = MA_FP64;
     o->verbose = 0;
-    o->cg_rtol = 1e-10;
+    o->cg_rtol = 0.0;  // adaptive forcing
     o->cg_maxiter = 20000;
 }
 
@@ -299,7 +303,7 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     ma_solve_opts o;
     ma_solve_opts_default(&o);
     if (opts) o = *opts;
-    if (o.cg_rtol <= 0) o.cg_rtol = 1e-10;
+    const bool adaptive = !(o.cg_rtol > 0);
     if (o.cg_maxiter <= 0) o.cg_maxiter = 20000;
     const int n = (int)n64;
     cudaSetDevice(c->device);
@@ -325,7 +329,7 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     double* w = c->wcur.as<double>();
     MA_CUDA(c, cudaMemcpyAsync(w, w_inout, sizeof(double) * n,
                                mem == MA_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
-    ma_status st = build_site_grid(c, m, n, dx, dy, w);
+    ma_status st = build_site_index(c, m, n, dx, dy, w);
     if (st != MA_OK) return st;
 
     cudaEvent_t e0, e1;
@@ -372,6 +376,7 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
             goto done;
         }
         int64_t niter = 0;
+        const double g0 = gn > 0 ? gn : 1.0;
         while (!converged(gn, mr)) {
             if (niter > o.maxiter) {
                 result = MA_MAXITER;
@@ -384,7 +389,9 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
             cudaEventRecord(e0, s);
             int it = 0;
             double rr = 0;
-            if ((st = pcg_solve(c, n, c->g.as<double>(), c->dirn.as<double>(), o.cg_rtol, (int)o.cg_maxiter, &it,
+            // inexact Newton: the linear solve only needs to beat the current residual
+            double rtol = adaptive ? std::fmin(1e-3, std::fmax(1e-12, 0.1 * gn / g0)) : o.cg_rtol;
+            if ((st = pcg_solve(c, n, c->g.as<double>(), c->dirn.as<double>(), rtol, (int)o.cg_maxiter, &it,
                                 &rr)) != MA_OK) {
                 result = st;
                 break;

@@ -157,6 +157,66 @@ static int rd_sign(rd a)
 }
 
 /* ------------------------------------------------------------------------- */
+/* double-double arithmetic (about 106 significant bits)                     */
+/* ------------------------------------------------------------------------- */
+/* The reference builds polygon vertices and integrals in FP64 from absolute
+ * coordinates (CGAL EPICK constructions).  Their rounding is large enough that a
+ * mere translation of the input moves short-edge Hessian entries by ~1e-10, so the
+ * oracle can also run those constructions and integrals in double-double
+ * (Dekker 1971; Hida, Li, Bailey 2001), with the same formulas and the same
+ * quadrature rules.  Combinatorics (predicates) are exact either way. */
+
+typedef struct { double hi, lo; } dd;
+
+static dd dd_c(double a) { dd r = {a, 0.0}; return r; }
+static dd dd_norm(double s, double e)
+{
+    dd r;
+    r.hi = s + e;
+    r.lo = e - (r.hi - s);
+    return r;
+}
+static dd dd_add(dd a, dd b)
+{
+    double s, e, t, f;
+    two_sum(a.hi, b.hi, &s, &e);
+    two_sum(a.lo, b.lo, &t, &f);
+    e += t;
+    dd r = dd_norm(s, e);
+    e = r.lo + f;
+    return dd_norm(r.hi, e);
+}
+static dd dd_neg(dd a) { dd r = {-a.hi, -a.lo}; return r; }
+static dd dd_sub(dd a, dd b) { return dd_add(a, dd_neg(b)); }
+static dd dd_mul(dd a, dd b)
+{
+    double p, e;
+    two_prod(a.hi, b.hi, &p, &e);
+    e += a.hi * b.lo + a.lo * b.hi;
+    return dd_norm(p, e);
+}
+static dd dd_muld(dd a, double b) { return dd_mul(a, dd_c(b)); }
+static dd dd_div(dd a, dd b)
+{
+    double q1 = a.hi / b.hi;
+    dd r = dd_sub(a, dd_muld(b, q1));
+    double q2 = r.hi / b.hi;
+    r = dd_sub(r, dd_muld(b, q2));
+    double q3 = r.hi / b.hi;
+    dd q = dd_norm(q1, q2);
+    return dd_add(q, dd_c(q3));
+}
+static dd dd_sqrt(dd a)
+{
+    if (a.hi <= 0.0) return dd_c(0.0);
+    double x = sqrt(a.hi);
+    dd xx = dd_mul(dd_c(x), dd_c(x));
+    dd corr = dd_div(dd_sub(a, xx), dd_c(2.0 * x));
+    return dd_add(dd_c(x), corr);
+}
+static double dd_d(dd a) { return a.hi + a.lo; }
+
+/* ------------------------------------------------------------------------- */
 /* weighted points and the three predicates of predicates.hpp                */
 /* ------------------------------------------------------------------------- */
 
@@ -210,6 +270,18 @@ static int side1(const site_t *v, const site_t *w, double ex, double ey, pred_st
         s = ex_sign(hl, h);
     }
     return s < 0;
+}
+
+/* sign of pow(E,v) - pow(E,w): -1 closer to v, 0 tie, +1 closer to w */
+static int pi_sign(const site_t *v, const site_t *w, double ex, double ey)
+{
+    int s = rd_sign(rd_pi(v, w, ex, ey));
+    if (s == 0) {
+        double h[32];
+        int hl = ex_pi(v, w, ex, ey, h);
+        s = ex_sign(hl, h);
+    }
+    return s;
 }
 
 /* Side3 (predicates.hpp:117-135): E = line(p,q) ∩ radical_axis(v,u);
@@ -555,6 +627,13 @@ typedef struct {
     /* regular-triangulation neighbours restricted to B' */
     int *nstart, *nlist;
     int keep_pieces;
+    /* candidate neighbour lists (a superset of the regular-triangulation neighbours) */
+    const int *cstart, *clist;
+    /* cell bounding boxes and a bin grid over them, for point location */
+    double *cbox;
+    int bnx, bny;
+    double bx0b, by0b, bcwb, bchb;
+    int *bstart, *blist;
 } prob_t;
 
 /* ------------------------------------------------------------------------- */
@@ -691,6 +770,110 @@ static int site_neighbors(prob_t *P, int i, int *nb, pred_stats *st)
     return m;
 }
 
+/* power cell of site i clipped to the box B' by its candidate list (exact); the
+ * polygon's bounding box goes to cbox[4i..4i+3] */
+static int site_neighbors_cand(prob_t *P, int i, int *nb, pred_stats *st)
+{
+    geo_t G = {P->ptx, P->pty, P->s, {0, 0}};
+    pedge A[PMAX], B[PMAX];
+    int c0 = P->nv;
+    int n = 4;
+    for (int k = 0; k < 4; k++) { A[k].t = 0; A[k].a = c0 + k; A[k].b = c0 + (k + 1) % 4; }
+    pedge *cur = A, *nxt = B;
+    const site_t *si = &P->s[i];
+    for (int q = P->cstart[i]; q < P->cstart[i + 1] && n > 0; q++) {
+        int j = P->clist[q];
+        if (j == i) continue;
+        const site_t *sj = &P->s[j];
+        if (sj->x == si->x && sj->y == si->y) {
+            if (sj->w > si->w || (sj->w == si->w && j < i)) n = 0;
+            continue;
+        }
+        int m = clip(&G, cur, n, i, j, nxt);
+        pedge *t = cur; cur = nxt; nxt = t;
+        n = m;
+    }
+    double bx0 = INFINITY, by0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY;
+    for (int k = 0; k < n; k++) {
+        double x, y;
+        vertex_to_point(&G, cur[(k + n - 1) % n], cur[k], &x, &y);
+        if (x < bx0) bx0 = x;
+        if (x > bx1) bx1 = x;
+        if (y < by0) by0 = y;
+        if (y > by1) by1 = y;
+    }
+    double mg = 1e-9 * (P->bx1 - P->bx0 + P->by1 - P->by0);
+    P->cbox[4 * i] = bx0 - mg;
+    P->cbox[4 * i + 1] = by0 - mg;
+    P->cbox[4 * i + 2] = bx1 + mg;
+    P->cbox[4 * i + 3] = by1 + mg;
+    *st = G.st;
+    int m = 0;
+    for (int k = 0; k < n; k++)
+        if (cur[k].t == 1) nb[m++] = cur[k].b;
+    return m;
+}
+
+/* bin grid over the cell bounding boxes */
+static void build_cell_bins(prob_t *P)
+{
+    int g = (int)ceil(sqrt((double)P->n));
+    if (g < 1) g = 1;
+    P->bnx = g;
+    P->bny = g;
+    P->bx0b = P->bx0;
+    P->by0b = P->by0;
+    P->bcwb = (P->bx1 - P->bx0) / g;
+    P->bchb = (P->by1 - P->by0) / g;
+    int nb = g * g;
+    P->bstart = calloc(nb + 1, sizeof(int));
+    for (int pass = 0; pass < 2; pass++) {
+        int *fill = pass ? malloc(sizeof(int) * nb) : NULL;
+        if (pass) memcpy(fill, P->bstart, sizeof(int) * nb);
+        for (int i = 0; i < P->n; i++) {
+            const double *b = &P->cbox[4 * i];
+            if (!(b[2] >= b[0])) continue; /* empty cell */
+            int x0 = (int)floor((b[0] - P->bx0b) / P->bcwb), x1 = (int)floor((b[2] - P->bx0b) / P->bcwb);
+            int y0 = (int)floor((b[1] - P->by0b) / P->bchb), y1 = (int)floor((b[3] - P->by0b) / P->bchb);
+            if (x0 < 0) x0 = 0;
+            if (y0 < 0) y0 = 0;
+            if (x1 >= g) x1 = g - 1;
+            if (y1 >= g) y1 = g - 1;
+            for (int yy = y0; yy <= y1; yy++)
+                for (int xx = x0; xx <= x1; xx++) {
+                    if (pass == 0) P->bstart[yy * g + xx + 1]++;
+                    else P->blist[fill[yy * g + xx]++] = i;
+                }
+        }
+        if (pass == 0) {
+            for (int b = 0; b < nb; b++) P->bstart[b + 1] += P->bstart[b];
+            P->blist = malloc(sizeof(int) * (P->bstart[nb] > 0 ? P->bstart[nb] : 1));
+        }
+        free(fill);
+    }
+}
+
+/* the sites whose closed power cell contains (x, y), by exact point location */
+static int locate(const prob_t *P, double x, double y, int *out, int cap)
+{
+    int bx = (int)floor((x - P->bx0b) / P->bcwb), by = (int)floor((y - P->by0b) / P->bchb);
+    if (bx < 0) bx = 0;
+    if (by < 0) by = 0;
+    if (bx >= P->bnx) bx = P->bnx - 1;
+    if (by >= P->bny) by = P->bny - 1;
+    int b = by * P->bnx + bx, m = 0;
+    for (int q = P->bstart[b]; q < P->bstart[b + 1]; q++) {
+        int i = P->blist[q];
+        const double *c = &P->cbox[4 * i];
+        if (x < c[0] || x > c[2] || y < c[1] || y > c[3]) continue;
+        int inside = 1;
+        for (int k = P->nstart[i]; k < P->nstart[i + 1] && inside; k++)
+            if (pi_sign(&P->s[i], &P->s[P->nlist[k]], x, y) > 0) inside = 0;
+        if (inside && m < cap) out[m++] = i;
+    }
+    return m;
+}
+
 /* sites whose power distance at (x, y) is within tol of the minimum */
 static int seeds_at(const prob_t *P, double x, double y, int *out, int cap)
 {
@@ -805,6 +988,198 @@ static void emit_piece(prob_t *P, piece_buf *B, geo_t *G, int f, int v, const pe
     }
     B->p = grow_buf(B->p, &B->cap, B->n + 1, sizeof(piece_t));
     B->p[B->n++] = pc;
+}
+
+/* ---- the same constructions and rules in double-double ---- */
+
+typedef struct { dd a, b, c; } dd_lin;
+
+static void edge_line_dd(const geo_t *G, pedge e, dd *a, dd *b, dd *c)
+{
+    if (e.t == 0) {
+        double px = G->px[e.a], py = G->py[e.a], qx = G->px[e.b], qy = G->py[e.b];
+        *a = dd_sub(dd_c(py), dd_c(qy));
+        *b = dd_sub(dd_c(qx), dd_c(px));
+        *c = dd_sub(dd_mul(dd_c(px), dd_c(qy)), dd_mul(dd_c(py), dd_c(qx)));
+    } else {
+        const site_t *v = &G->s[e.a], *w = &G->s[e.b];
+        *a = dd_muld(dd_sub(dd_c(w->x), dd_c(v->x)), 2.0);
+        *b = dd_muld(dd_sub(dd_c(w->y), dd_c(v->y)), 2.0);
+        dd pv = dd_sub(dd_add(dd_mul(dd_c(v->x), dd_c(v->x)), dd_mul(dd_c(v->y), dd_c(v->y))), dd_c(v->w));
+        dd pw = dd_sub(dd_add(dd_mul(dd_c(w->x), dd_c(w->x)), dd_mul(dd_c(w->y), dd_c(w->y))), dd_c(w->w));
+        *c = dd_sub(pv, pw);
+    }
+}
+
+static void vertex_to_point_dd(const geo_t *G, pedge e1, pedge e2, dd *x, dd *y)
+{
+    dd a1, b1, c1, a2, b2, c2;
+    edge_line_dd(G, e1, &a1, &b1, &c1);
+    edge_line_dd(G, e2, &a2, &b2, &c2);
+    dd den = dd_sub(dd_mul(a1, b2), dd_mul(a2, b1));
+    *x = dd_div(dd_sub(dd_mul(b1, c2), dd_mul(b2, c1)), den);
+    *y = dd_div(dd_sub(dd_mul(a2, c1), dd_mul(a1, c2)), den);
+}
+
+static dd extrapolate_dd(double px, double py, double ax, double ay, double fa, double bx, double by, double fb,
+                         double cx, double cy, double fc)
+{
+    dd v0x = dd_sub(dd_c(bx), dd_c(ax)), v0y = dd_sub(dd_c(by), dd_c(ay));
+    dd v1x = dd_sub(dd_c(cx), dd_c(ax)), v1y = dd_sub(dd_c(cy), dd_c(ay));
+    dd v2x = dd_sub(dd_c(px), dd_c(ax)), v2y = dd_sub(dd_c(py), dd_c(ay));
+    dd d00 = dd_add(dd_mul(v0x, v0x), dd_mul(v0y, v0y)), d01 = dd_add(dd_mul(v0x, v1x), dd_mul(v0y, v1y));
+    dd d11 = dd_add(dd_mul(v1x, v1x), dd_mul(v1y, v1y));
+    dd d20 = dd_add(dd_mul(v2x, v0x), dd_mul(v2y, v0y)), d21 = dd_add(dd_mul(v2x, v1x), dd_mul(v2y, v1y));
+    dd den = dd_sub(dd_mul(d00, d11), dd_mul(d01, d01));
+    dd v = dd_div(dd_sub(dd_mul(d11, d20), dd_mul(d01, d21)), den);
+    dd w = dd_div(dd_sub(dd_mul(d00, d21), dd_mul(d01, d20)), den);
+    dd u = dd_sub(dd_sub(dd_c(1.0), v), w);
+    return dd_add(dd_add(dd_muld(u, fa), dd_muld(v, fb)), dd_muld(w, fc));
+}
+
+static dd_lin make_linfn_dd(const prob_t *P, int f)
+{
+    const int *t = &P->tri[3 * f];
+    double px = P->vx[t[0]], py = P->vy[t[0]], fp = P->vval[t[0]];
+    double qx = P->vx[t[1]], qy = P->vy[t[1]], fq = P->vval[t[1]];
+    double rx = P->vx[t[2]], ry = P->vy[t[2]], fr = P->vval[t[2]];
+    dd_lin L;
+    L.c = extrapolate_dd(0, 0, px, py, fp, qx, qy, fq, rx, ry, fr);
+    L.a = dd_sub(extrapolate_dd(1, 0, px, py, fp, qx, qy, fq, rx, ry, fr), L.c);
+    L.b = dd_sub(extrapolate_dd(0, 1, px, py, fp, qx, qy, fq, rx, ry, fr), L.c);
+    return L;
+}
+
+static dd lf_dd(const dd_lin *L, dd x, dd y) { return dd_add(dd_add(dd_mul(L->a, x), dd_mul(L->b, y)), L->c); }
+
+static dd tri_area_dd(dd ax, dd ay, dd bx, dd by, dd cx, dd cy)
+{
+    dd t = dd_sub(dd_mul(dd_sub(bx, ax), dd_sub(cy, ay)), dd_mul(dd_sub(cx, ax), dd_sub(by, ay)));
+    return dd_muld(t, 0.5);
+}
+
+static void integrand_dd(const dd_lin *L, double sx, double sy, dd x, dd y, dd *out)
+{
+    dd r = lf_dd(L, x, y);
+    dd dx = dd_sub(x, dd_c(sx)), dy = dd_sub(y, dd_c(sy));
+    out[0] = dd_mul(r, dd_add(dd_mul(dx, dx), dd_mul(dy, dy)));
+    out[1] = r;
+    out[2] = dd_mul(r, x);
+    out[3] = dd_mul(r, y);
+    out[4] = dd_mul(dd_mul(r, x), x);
+    out[5] = dd_mul(dd_mul(r, y), y);
+    out[6] = dd_mul(dd_mul(r, x), y);
+}
+
+static void albrecht_collatz_dd(const dd_lin *L, double sx, double sy, dd ax, dd ay, dd bx, dd by, dd cx, dd cy,
+                                dd *acc)
+{
+    dd ux = dd_sub(bx, ax), uy = dd_sub(by, ay), vx = dd_sub(cx, ax), vy = dd_sub(cy, ay);
+    /* 1/2, 1/6, 2/3 and the weights 1/30, 9/30 as double-double constants */
+    dd h = dd_c(0.5);
+    dd s6 = dd_div(dd_c(1.0), dd_c(6.0)), t3 = dd_div(dd_c(2.0), dd_c(3.0));
+    dd w1 = dd_div(dd_c(1.0), dd_c(30.0)), w9 = dd_div(dd_c(9.0), dd_c(30.0));
+    dd cu[6][2] = {{h, h}, {h, dd_c(0)}, {dd_c(0), h}, {s6, t3}, {t3, s6}, {s6, s6}};
+    dd wt[6] = {w1, w1, w1, w9, w9, w9};
+    dd sum[NQ];
+    for (int j = 0; j < NQ; j++) sum[j] = dd_c(0.0);
+    for (int k = 0; k < 6; k++) {
+        dd qx = dd_add(ax, dd_add(dd_mul(cu[k][0], ux), dd_mul(cu[k][1], vx)));
+        dd qy = dd_add(ay, dd_add(dd_mul(cu[k][0], uy), dd_mul(cu[k][1], vy)));
+        dd f[NQ];
+        integrand_dd(L, sx, sy, qx, qy, f);
+        for (int j = 0; j < NQ; j++) sum[j] = dd_add(sum[j], dd_mul(wt[k], f[j]));
+    }
+    dd A = tri_area_dd(ax, ay, bx, by, cx, cy);
+    for (int j = 0; j < NQ; j++) acc[j] = dd_add(acc[j], dd_mul(A, sum[j]));
+}
+
+/* emit_piece with the constructions and rules evaluated in double-double */
+static void emit_piece_dd(prob_t *P, piece_buf *B, geo_t *G, int f, int v, const pedge *R, int n)
+{
+    if (n == 0) return;
+    dd px[PMAX], py[PMAX];
+    int adj[PMAX];
+    for (int i = 0; i < n; i++) {
+        int ii = (i == 0) ? n - 1 : i - 1;
+        vertex_to_point_dd(G, R[i], R[ii], &px[i], &py[i]);
+        adj[i] = (R[i].t == 1) ? R[i].b : -1;
+    }
+    dd_lin L = make_linfn_dd(P, f);
+    const site_t *sv = &P->s[v];
+    for (int i = 0; i < n; i++) {
+        if (adj[i] < 0) continue;
+        int w = adj[i];
+        int i1 = (i + 1) % n;
+        dd ex = dd_sub(px[i1], px[i]), ey = dd_sub(py[i1], py[i]);
+        dd len = dd_sqrt(dd_add(dd_mul(ex, ex), dd_mul(ey, ey)));
+        dd mx = dd_muld(dd_add(px[i], px[i1]), 0.5), my = dd_muld(dd_add(py[i], py[i1]), 0.5);
+        dd r = dd_mul(len, lf_dd(&L, mx, my));
+        dd dx = dd_sub(dd_c(sv->x), dd_c(P->s[w].x)), dy = dd_sub(dd_c(sv->y), dd_c(P->s[w].y));
+        dd d = dd_muld(dd_sqrt(dd_add(dd_mul(dx, dx), dd_mul(dy, dy))), 2.0);
+        double q = dd_d(dd_div(r, d));
+        B->t = grow_buf(B->t, &B->capt, B->nt + 2, sizeof(trip_t));
+        trip_t t1 = {v, w, f, -1, -q};
+        trip_t t2 = {v, v, f, w, q};
+        B->t[B->nt++] = t1;
+        B->t[B->nt++] = t2;
+    }
+    piece_t pc;
+    memset(&pc, 0, sizeof(pc));
+    pc.face = f;
+    pc.site = v;
+    pc.nv = n;
+    dd warea = dd_c(0.0), area = dd_c(0.0);
+    dd acc[NQ], acm[NQ];
+    for (int j = 0; j < NQ; j++) {
+        acc[j] = dd_c(0.0);
+        acm[j] = dd_c(0.0);
+    }
+    if (n > 2) {
+        dd third = dd_div(dd_c(1.0), dd_c(3.0));
+        for (int i = 1; i < n - 1; i++) {
+            dd A = tri_area_dd(px[0], py[0], px[i], py[i], px[i + 1], py[i + 1]);
+            dd gx = dd_mul(dd_add(dd_add(px[0], px[i]), px[i + 1]), third);
+            dd gy = dd_mul(dd_add(dd_add(py[0], py[i]), py[i + 1]), third);
+            warea = dd_add(warea, dd_mul(A, lf_dd(&L, gx, gy)));
+            area = dd_add(area, A);
+        }
+        for (int i = 1; i < n - 1; i++)
+            albrecht_collatz_dd(&L, sv->x, sv->y, px[0], py[0], px[i], py[i], px[i + 1], py[i + 1], acc);
+        for (int i = 1; i < n - 1; i++) {
+            int a = 1 % n, b = (i + 1) % n, c = (i + 2) % n;
+            albrecht_collatz_dd(&L, sv->x, sv->y, px[a], py[a], px[b], py[b], px[c], py[c], acm);
+        }
+    }
+    pc.mass = dd_d(warea);
+    pc.area = dd_d(area);
+    pc.second = dd_d(acc[0]);
+    for (int j = 0; j < 6; j++) pc.mom[j] = dd_d(acm[1 + j]);
+    if (P->keep_pieces) {
+        B->pxy = grow_buf(B->pxy, &B->cappv, 2 * (B->npv + n), sizeof(double));
+        B->plab = grow_buf(B->plab, &B->cappl, B->npv + n, sizeof(int));
+        pc.poly_off = B->npv;
+        for (int i = 0; i < n; i++) {
+            B->pxy[2 * (B->npv + i)] = dd_d(px[i]);
+            B->pxy[2 * (B->npv + i) + 1] = dd_d(py[i]);
+            B->plab[B->npv + i] = adj[i];
+        }
+        B->npv += n;
+    }
+    B->p = grow_buf(B->p, &B->cap, B->n + 1, sizeof(piece_t));
+    B->p[B->n++] = pc;
+}
+
+static int g_dd = 0;
+
+void ora_set_precision(int double_double) { g_dd = double_double; }
+
+static void emit(prob_t *P, piece_buf *B, geo_t *G, int f, int v, const pedge *R, int n)
+{
+    if (g_dd)
+        emit_piece_dd(P, B, G, f, v, R, n);
+    else
+        emit_piece(P, B, G, f, v, R, n);
 }
 
 /* clip triangle f by the neighbours of v (vti.hpp:255-274) */
@@ -981,13 +1356,15 @@ int ora_max_threads(void)
  */
 ora_result *ora_kantorovich(int nv, const double *vx, const double *vy, const double *vval, int nt,
                             const int *tri, int n, const double *x, const double *y, const double *w,
-                            int mode, int keep_pieces)
+                            int mode, int keep_pieces, const int *cand_start, const int *cand_list)
 {
     prob_t P;
     memset(&P, 0, sizeof(P));
     P.nv = nv; P.nt = nt; P.n = n;
     P.vx = vx; P.vy = vy; P.vval = vval; P.tri = tri;
     P.keep_pieces = keep_pieces;
+    P.cstart = cand_start;
+    P.clist = cand_list;
 #ifdef _OPENMP
     if (g_threads > 0) omp_set_num_threads(g_threads);
 #endif
@@ -1020,12 +1397,13 @@ ora_result *ora_kantorovich(int nv, const double *vx, const double *vy, const do
     /* regular-triangulation neighbours (restricted to B') */
     int **nbl = malloc(sizeof(int *) * (n > 0 ? n : 1));
     int *nbc = calloc(n > 0 ? n : 1, sizeof(int));
+    P.cbox = malloc(sizeof(double) * 4 * (n > 0 ? n : 1));
     long fc = 0, ec = 0;
 #pragma omp parallel for schedule(dynamic, 64) reduction(+ : fc, ec) if (mode == 1)
     for (int i = 0; i < n; i++) {
         int tmp[PMAX];
         pred_stats st = {0, 0};
-        int m = site_neighbors(&P, i, tmp, &st);
+        int m = P.cstart ? site_neighbors_cand(&P, i, tmp, &st) : site_neighbors(&P, i, tmp, &st);
         nbl[i] = malloc(sizeof(int) * (m > 0 ? m : 1));
         memcpy(nbl[i], tmp, sizeof(int) * m);
         nbc[i] = m;
@@ -1042,6 +1420,7 @@ ora_result *ora_kantorovich(int nv, const double *vx, const double *vy, const do
     }
     free(nbl);
     free(nbc);
+    if (P.cstart) build_cell_bins(&P);
 
     int nthreads = 1;
 #ifdef _OPENMP
@@ -1061,7 +1440,8 @@ ora_result *ora_kantorovich(int nv, const double *vx, const double *vy, const do
         int seeds[256];
         for (int f0 = 0; f0 < nt; f0++) {
             if (covered[f0]) continue;
-            int ns = seeds_at(&P, vx[tri[3 * f0]], vy[tri[3 * f0]], seeds, 256);
+            int ns = P.cstart ? locate(&P, vx[tri[3 * f0]], vy[tri[3 * f0]], seeds, 256)
+                              : seeds_at(&P, vx[tri[3 * f0]], vy[tri[3 * f0]], seeds, 256);
             for (int k = 0; k < ns; k++) {
                 uint64_t key = (uint64_t)seeds[k] * (uint64_t)nt + f0;
                 if (hs_insert(&vis, key)) {
@@ -1090,7 +1470,7 @@ ora_result *ora_kantorovich(int nv, const double *vx, const double *vy, const do
                     if (qt >= qcap) { qcap *= 2; Q = realloc(Q, sizeof(uint64_t) * qcap); }
                     Q[qt++] = nk;
                 }
-                emit_piece(&P, &bufs[0], &G, f, v, R, m);
+                emit(&P, &bufs[0], &G, f, v, R, m);
             }
         }
         bufs[0].st.filter_calls += G.st.filter_calls;
@@ -1115,7 +1495,8 @@ ora_result *ora_kantorovich(int nv, const double *vx, const double *vy, const do
             hset seen = {0, 0, 0, 0, 0};
 #pragma omp for schedule(dynamic, 16)
             for (int f = 0; f < nt; f++) {
-                int ns = seeds_at(&P, vx[tri[3 * f]], vy[tri[3 * f]], seeds, 256);
+                int ns = P.cstart ? locate(&P, vx[tri[3 * f]], vy[tri[3 * f]], seeds, 256)
+                                  : seeds_at(&P, vx[tri[3 * f]], vy[tri[3 * f]], seeds, 256);
                 long nsk = 0;
                 hs_clear(&seen);
                 for (int k = 0; k < ns; k++) {
@@ -1133,7 +1514,7 @@ ora_result *ora_kantorovich(int nv, const double *vx, const double *vy, const do
                         stack = grow_buf(stack, &scap, nsk + 1, sizeof(int));
                         stack[nsk++] = u;
                     }
-                    emit_piece(&P, B, &G, f, v, R, m);
+                    emit(&P, B, &G, f, v, R, m);
                 }
             }
             B->st.filter_calls += G.st.filter_calls;
@@ -1226,6 +1607,7 @@ ora_result *ora_kantorovich(int nv, const double *vx, const double *vy, const do
     free(all);
     free(tr);
     free(P.ptx); free(P.pty); free(P.s); free(P.fnbr); free(P.fn); free(P.gstart); free(P.gidx);
+    free(P.cbox); free(P.bstart); free(P.blist);
     return res;
 }
 

@@ -44,7 +44,7 @@ def lib():
         L = ctypes.CDLL(path)
         L.ora_kantorovich.restype = ctypes.c_void_p
         L.ora_kantorovich.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, ctypes.c_int,
-                                      _dp, _dp, _dp, ctypes.c_int, ctypes.c_int]
+                                      _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, _ip, _ip]
         for name in ("ora_value", "ora_total_mass", "ora_total_area"):
             getattr(L, name).restype = ctypes.c_double
             getattr(L, name).argtypes = [ctypes.c_void_p]
@@ -62,6 +62,7 @@ def lib():
         L.ora_free.argtypes = [ctypes.c_void_p]
         L.ora_set_threads.argtypes = [ctypes.c_int]
         L.ora_max_threads.restype = ctypes.c_int
+        L.ora_set_precision.argtypes = [ctypes.c_int]
         L.ora_side1.restype = ctypes.c_int
         L.ora_side1.argtypes = [_dp, _dp, ctypes.c_double, ctypes.c_double]
         L.ora_side2.restype = ctypes.c_int
@@ -124,14 +125,75 @@ def max_threads() -> int:
     return int(lib().ora_max_threads())
 
 
-def kantorovich(mesh, x, y, w, mode: int = 1, keep_pieces: bool = False) -> KResult:
+def candidates(x, y, w, ring: int = 2):
+    """Candidate neighbour lists (CSR) for every site: its regular-triangulation
+    neighbours, the lower convex hull of the lifted sites (x, y, x^2 + y^2 - w)
+    (the reference builds the same triangulation with CGAL, kantorovich.hpp:65-72).
+
+    ``ring=2`` adds the neighbours' neighbours, so that a near-degenerate quad that
+    qhull triangulated along the other diagonal cannot hide a true neighbour.  A site
+    that is not a hull vertex (hidden, or dropped by qhull's merging) gets the
+    vertices of the hull facet below it and their neighbours.  Extra candidates never
+    change a cell: the clipping is exact."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    w = np.asarray(w, np.float64)
+    n = x.shape[0]
+    if n <= 64:
+        lists = [np.array([j for j in range(n) if j != i], np.int32) for i in range(n)]
+    else:
+        import scipy.sparse as sp
+        from scipy.spatial import ConvexHull
+        cx, cy = x.mean(), y.mean()
+        pts = np.c_[x - cx, y - cy, (x - cx) ** 2 + (y - cy) ** 2 - w]
+        hull = ConvexHull(pts)
+        low = hull.equations[:, 2] < 0
+        simp = hull.simplices[low]
+        eqs = hull.equations[low]
+        r = np.r_[simp[:, 0], simp[:, 1], simp[:, 2], simp[:, 1], simp[:, 2], simp[:, 0]]
+        c = np.r_[simp[:, 1], simp[:, 2], simp[:, 0], simp[:, 0], simp[:, 1], simp[:, 2]]
+        A = sp.csr_matrix((np.ones(r.size, np.int8), (r, c)), shape=(n, n))
+        on = np.zeros(n, bool)
+        on[np.unique(simp)] = True
+        extra_r, extra_c = [], []
+        for i in np.nonzero(~on)[0]:
+            # the lower-hull surface is the max of its facet planes
+            z = -(eqs[:, 0] * pts[i, 0] + eqs[:, 1] * pts[i, 1] + eqs[:, 3]) / eqs[:, 2]
+            f = simp[int(np.argmax(z))]
+            s = set(int(v) for v in f)
+            for v in f:
+                s |= set(A.indices[A.indptr[v]:A.indptr[v + 1]].tolist())
+            extra_r += [i] * len(s)
+            extra_c += list(s)
+        if extra_r:
+            A = A + sp.csr_matrix((np.ones(len(extra_r), np.int8), (extra_r, extra_c)), shape=(n, n))
+        A = (A != 0).astype(np.int8).tocsr()
+        if ring >= 2:
+            A = ((A + A @ A) != 0).astype(np.int8).tocsr()
+        A.setdiag(0)
+        A.eliminate_zeros()
+        A.sort_indices()
+        return A.indptr.astype(np.int32), A.indices.astype(np.int32)
+    start = np.zeros(n + 1, np.int32)
+    start[1:] = np.cumsum([len(l) for l in lists])
+    flat = np.concatenate(lists).astype(np.int32) if n else np.zeros(0, np.int32)
+    return start, flat
+
+
+def kantorovich(mesh, x, y, w, mode: int = 1, keep_pieces: bool = False, arith: str = "dd",
+                ring: int = 2) -> KResult:
     """One evaluation of ``MA::kantorovich`` (+ moments) on the CPU.
 
     ``mode=0`` runs the reference's global flood fill on one thread
     (voronoi_triangulation_intersection.hpp:219-313); ``mode=1`` finds the same
     pieces triangle by triangle on all OpenMP threads.  Both give identical bits.
+
+    ``arith="fp64"`` builds vertices and integrals in FP64 from absolute coordinates,
+    as the reference does; ``arith="dd"`` uses the same formulas in double-double,
+    which removes that rounding (the parity anchor).  The pieces are the same.
     """
     L = lib()
+    L.ora_set_precision(1 if arith == "dd" else 0)
     m = mesh.explicit()
     vx, pvx = _d(m.vx)
     vy, pvy = _d(m.vy)
@@ -141,7 +203,10 @@ def kantorovich(mesh, x, y, w, mode: int = 1, keep_pieces: bool = False) -> KRes
     y, py = _d(y)
     w, pw = _d(w)
     n = x.shape[0]
-    h = L.ora_kantorovich(m.nv, pvx, pvy, pvv, m.nt, ptri, n, px, py, pw, int(mode), int(keep_pieces))
+    cs, cl = candidates(x, y, w, ring)
+    cs, pcs = _i(cs)
+    cl, pcl = _i(cl if cl.size else np.zeros(1, np.int32))
+    h = L.ora_kantorovich(m.nv, pvx, pvy, pvv, m.nt, ptri, n, px, py, pw, int(mode), int(keep_pieces), pcs, pcl)
     if not h:
         raise RuntimeError("oracle failed")
     try:
@@ -233,7 +298,8 @@ def solve_laplacian_matrix(h, g):
 
 
 def ot_solve(mesh, x, y, nu, w=None, eps_g: float = 1e-7, maxiter: int = 100,
-             tol_rel: float | None = None, mode: int = 1, verbose: bool = False) -> SolveResult:
+             tol_rel: float | None = None, mode: int = 1, verbose: bool = False, arith: str = "dd",
+             ring: int = 2) -> SolveResult:
     """``MA::ot_solve`` restated.  The stop rule is the reference's
     ``|m - nu|_2 < eps_g`` unless ``tol_rel`` is given, in which case it is
     ``max_i |m_i - nu_i| / nu_i <= tol_rel``."""
@@ -245,7 +311,7 @@ def ot_solve(mesh, x, y, nu, w=None, eps_g: float = 1e-7, maxiter: int = 100,
 
     def f(wv):
         stats["neval"] += 1
-        r = kantorovich(mesh, x, y, wv, mode=mode)
+        r = kantorovich(mesh, x, y, wv, mode=mode, arith=arith, ring=ring)
         m = r.g
         g = m - nu
         return r.value - nu @ wv, m, g, r.hessian()

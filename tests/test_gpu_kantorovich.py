@@ -136,24 +136,51 @@ def test_large_invariants(ctx):
     assert (g > 0).all()
 
 
-def _lattice(k, jitter, seed):
+def _lattice(k):
     g = (np.arange(k) + 0.5) / k
     X, Y = np.meshgrid(g, g)
-    x, y = X.ravel().copy(), Y.ravel().copy()
-    if jitter:
-        rng = np.random.default_rng(seed)
-        x += rng.integers(-2, 3, x.size) * np.spacing(x)
-        y += rng.integers(-2, 3, y.size) * np.spacing(y)
+    return X.ravel().copy(), Y.ravel().copy()
+
+
+def _cocircular_quadruples(nq, seed):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.08, 0.92, (nq, 2))
+    r = rng.uniform(0.01, 0.04, nq)
+    ang = rng.uniform(0, 2 * np.pi, (nq, 4))
+    x = (c[:, 0, None] + r[:, None] * np.cos(ang)).ravel()
+    y = (c[:, 1, None] + r[:, None] * np.sin(ang)).ravel()
     return x, y
 
 
-def test_near_degenerate_lattice_parity(ctx, oracle):
-    # sites a few ulps off a lattice: four sites are almost co-circular everywhere,
-    # so most decisions go past the FP32 and FP64 filters to exact arithmetic
+def test_near_degenerate_parity(ctx, oracle):
+    # groups of four sites on a common circle, rounded to doubles: every group is
+    # co-circular up to rounding, so its decisions go past the FP32 and FP64
+    # filters to exact arithmetic, yet no group is exactly co-circular (checked in
+    # rational arithmetic by the oracle tests), so the answer does not depend on
+    # the clipping order
     from mongeampere_gb300.mesh import unit_grid
-    x, y = _lattice(20, True, 1)
+    x, y = _cocircular_quadruples(150, 3)
     mesh = unit_grid(16, np.random.default_rng(2).uniform(0.5, 1.5, (16, 16)))
+    r = oracle.kantorovich(mesh, x, y, np.zeros(x.size))
+    assert r.exact_calls > 100
     _compare(ctx, oracle, mesh, x, y, np.zeros(x.size))
+
+
+def test_many_neighbour_cells(ctx, oracle):
+    # one heavy site surrounded by a ring of light ones: its cell has ~150 edges,
+    # more than the main kernel holds, so it is redone by the large-capacity pass
+    from mongeampere_gb300.mesh import unit_grid
+    k = 150
+    t = np.arange(k) * 2 * np.pi / k + 0.01
+    far = np.random.default_rng(1).uniform(0, 1, (600, 2))
+    far = far[np.hypot(far[:, 0] - 0.5, far[:, 1] - 0.5) > 0.36][:200]
+    x = np.r_[0.5, 0.5 + 0.3 * np.cos(t), far[:, 0]]
+    y = np.r_[0.5, 0.5 + 0.3 * np.sin(t), far[:, 1]]
+    w = np.zeros(x.size)
+    w[0] = 0.06
+    mesh = unit_grid(24, np.random.default_rng(3).uniform(0.5, 1.5, (24, 24)))
+    v, g, h, r = _compare(ctx, oracle, mesh, x, y, w)
+    assert h.rowptr[1] - h.rowptr[0] > 100
 
 
 def test_exactly_degenerate_lattice_conserves_mass(ctx):
@@ -162,7 +189,7 @@ def test_exactly_degenerate_lattice_conserves_mass(ctx):
     # the domain
     from mongeampere_gb300 import api
     from mongeampere_gb300.mesh import unit_grid
-    x, y = _lattice(16, False, 0)
+    x, y = _lattice(16)
     mesh = unit_grid(9, np.ones((9, 9)))
     v, g, h = api.kantorovich(mesh, np.c_[x, y], np.zeros(x.size), ctx=ctx)
     np.testing.assert_allclose(np.asarray(g), 1.0 / x.size, rtol=1e-12)

@@ -205,3 +205,52 @@ def test_empty_cell_is_reported(oracle):
     w = np.array([0.0, 0.0, -1.0])
     with pytest.raises(oracle.EmptyCellError):
         oracle.ot_solve(mesh, x, y, np.full(3, 1 / 3), w=w)
+
+
+def test_double_double_oracle_is_translation_invariant(oracle):
+    # the reference's FP64 absolute-coordinate constructions move short-edge
+    # Hessian entries under a translation of the input; the double-double mode
+    # (the parity anchor) does not, and both modes find the same pieces
+    from mongeampere_gb300.mesh import GridMesh
+    p = W.make_problem(64, 2000, "gauss", "uniform", "random", seed=3)
+    w = np.random.default_rng(6).uniform(-5e-5, 5e-5, p.n)
+    a = oracle.kantorovich(p.mesh, p.x, p.y, w)
+    f = oracle.kantorovich(p.mesh, p.x, p.y, w, arith="fp64")
+    assert np.array_equal(a.rows, f.rows) and np.array_equal(a.cols, f.cols)
+    scale = np.abs(a.vals).max()
+    assert np.abs(a.vals - f.vals).max() <= 1e-8 * scale
+    sh = 0.375
+    m2 = GridMesh(p.mesh.gx + sh, p.mesh.gy + sh, p.mesh.values)
+    b = oracle.kantorovich(m2, p.x + sh, p.y + sh, w)
+    assert np.array_equal(a.rows, b.rows) and np.array_equal(a.cols, b.cols)
+    assert np.all(np.abs(a.vals - b.vals) <= 1e-12 * (np.abs(a.vals) + scale))
+    assert np.all(np.abs(a.g - b.g) <= 1e-13 * np.abs(a.g).max())
+
+
+def test_cocircular_quadruples_have_no_exact_ties(oracle):
+    # the near-degenerate input of the GPU parity test: co-circular up to rounding,
+    # never exactly (so adjacency does not depend on the order of the input)
+    from mongeampere_gb300.mesh import unit_grid
+    rng = np.random.default_rng(3)
+    nq = 150
+    c = rng.uniform(0.08, 0.92, (nq, 2))
+    r = rng.uniform(0.01, 0.04, nq)
+    ang = rng.uniform(0, 2 * np.pi, (nq, 4))
+    x = (c[:, 0, None] + r[:, None] * np.cos(ang)).ravel()
+    y = (c[:, 1, None] + r[:, None] * np.sin(ang)).ravel()
+    for q in range(nq):
+        P = [(Fr(x[4 * q + t]), Fr(y[4 * q + t])) for t in range(4)]
+        a = P[0]
+        rows = [(p[0] - a[0], p[1] - a[1], (p[0] - a[0]) ** 2 + (p[1] - a[1]) ** 2) for p in P[1:]]
+        det = (rows[0][0] * (rows[1][1] * rows[2][2] - rows[1][2] * rows[2][1])
+               - rows[0][1] * (rows[1][0] * rows[2][2] - rows[1][2] * rows[2][0])
+               + rows[0][2] * (rows[1][0] * rows[2][1] - rows[1][1] * rows[2][0]))
+        assert det != 0
+    mesh = unit_grid(16, np.random.default_rng(2).uniform(0.5, 1.5, (16, 16)))
+    a = oracle.kantorovich(mesh, x, y, np.zeros(x.size))
+    assert a.exact_calls > 100
+    perm = np.random.default_rng(0).permutation(x.size)
+    b = oracle.kantorovich(mesh, x[perm], y[perm], np.zeros(x.size))
+    A = {(int(i), int(j)) for i, j in zip(a.rows, a.cols)}
+    B = {(int(perm[i]), int(perm[j])) for i, j in zip(b.rows, b.cols)}
+    assert A == B
