@@ -33,6 +33,12 @@
  *     "Adaptive precision floating-point arithmetic and fast robust geometric
  *     predicates").  Ties count as "not inside", the reference's strict SMALLER.
  *
+ * Parity unpinned against reference outputs: the reference cannot be compiled
+ * here (CGAL, Eigen and GMP are absent) and its tests hold no golden vectors.  The
+ * oracle is pinned instead to exact-rational fixtures (tests/golden) and to the
+ * invariants the reference's drivers print (total area, mass conservation,
+ * finite-difference consistency).
+ *
  * Build: gcc -O2 -fPIC -shared -ffp-contract=off -fopenmp (oracle/build.py).
  */
 #include <math.h>
