@@ -156,6 +156,25 @@ ma_status ma_ot_solve(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double*
 ma_status ma_laplacian_solve(ma_ctx* ctx, const double* g, double* d, ma_mem mem, double rtol,
                              int64_t maxiter, int64_t* iters);
 
+/* Newton linear solve that allocates nothing.  No counterpart in the reference: it is
+ * for callers that cannot let a library allocate device memory -- applications whose
+ * own pool or arena owns all device memory, and latency-critical loops that cannot
+ * afford the device-wide synchronisation of cudaMalloc / cudaFree.  It solves
+ * H[:n-1,:n-1] d = g[:n-1], d[n-1] = 0 (the system of ma_laplacian_solve) for a CSR
+ * Hessian the caller passes in; rowptr, col, val, g and d are device memory of the
+ * current device, `stream` is a cudaStream_t (NULL: the default stream), *iters (host)
+ * receives the CG iteration count.
+ *  - The CG work vectors live in one fixed device array of the library (10.1 MB, held
+ *    by every GPU that loads the library until the process exits); n is limited to
+ *    262,144 and larger systems return MA_ERR_BUFFER_TOO_SMALL.
+ *  - The first call on a device looks up that array's address; make it before any
+ *    stream capture.
+ *  - Every call shares the array: calls that overlap on the GPU (from several threads
+ *    or streams) race and corrupt each other's result. */
+ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                                    const double* g, double* d, double rtol, int64_t maxiter, int64_t* iters,
+                                    void* stream);
+
 /* --------------------------------------------------------- moments / Lloyd */
 /* mass[n]; first[2n] = (int rho x, int rho y) per site; second[3n] (nullable) =
  * (int rho x^2, int rho y^2, int rho x y) per site. */

@@ -60,6 +60,8 @@ SIGNATURES = {
     "ma_ot_solve": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int,
                                    ctypes.POINTER(MaSolveOpts), ctypes.POINTER(MaStats)]),
     "ma_laplacian_solve": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_int64, _i64p]),
+    "ma_laplacian_solve_static": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, ctypes.c_double,
+                                                 ctypes.c_int64, _i64p, _vp]),
     "ma_moments": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp]),
     "ma_lloyd": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
 }

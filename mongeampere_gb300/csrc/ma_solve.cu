@@ -13,6 +13,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 #include "ma_runtime.h"
 
@@ -248,11 +249,119 @@ static ma_status pcg_solve(Ctx* c, int n, const double* b, double* x, double rto
     return MA_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Newton linear solve without any allocation
+// ---------------------------------------------------------------------------
+// Some callers cannot let a library allocate device memory: applications that
+// hand all device memory to their own pool or arena up front and forbid any
+// allocation outside it, and latency-critical loops where the device-wide
+// synchronisation of cudaMalloc/cudaFree is not acceptable.  For them the
+// Jacobi-PCG work vectors live in this fixed array, reserved when the library is
+// loaded and kept by every GPU that loads it until the process exits.
+constexpr int64_t kStaticMaxN = (int64_t)1 << 18;  // largest system: 262,144 sites
+constexpr int kStaticMaxBlocks = 4096;              // per-block partial sums of the CG kernel
+constexpr size_t kStaticDoubles = 5 * (size_t)kStaticMaxN + 3 * (size_t)kStaticMaxBlocks + 8;
+static __device__ __align__(256) double g_static_pcg[kStaticDoubles];  // 10.1 MB
+
+// per-device address of g_static_pcg and the co-resident block count of k_pcg,
+// looked up once per device with that device current
+struct StaticSetup {
+    bool done = false;
+    double* base = nullptr;
+    int max_blocks = 0;
+};
+static std::mutex g_static_mutex;
+static StaticSetup g_static_setup[64];
+
+static ma_status static_setup(int dev, StaticSetup* out)
+{
+    if (dev < 0 || dev >= 64) return MA_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    StaticSetup& st = g_static_setup[dev];
+    if (!st.done) {
+        void* ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_static_pcg) != cudaSuccess) {
+            cudaGetLastError();
+            return MA_ERR_CUDA;
+        }
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, kPcgThreads, 0) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return MA_ERR_CUDA;
+        }
+        st.base = static_cast<double*>(ptr);
+        st.max_blocks = per_sm * sms < kStaticMaxBlocks ? per_sm * sms : kStaticMaxBlocks;
+        st.done = true;
+    }
+    *out = st;
+    return MA_OK;
+}
+
 }  // namespace ma
 
 using namespace ma;
 
 extern "C" {
+
+ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                                    const double* g, double* d, double rtol, int64_t maxiter, int64_t* iters,
+                                    void* stream)
+{
+    if (n < 1 || !rowptr || !col || !val || !g || !d) return MA_ERR_INVALID_ARGUMENT;
+    if (n > kStaticMaxN) return MA_ERR_BUFFER_TOO_SMALL;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return MA_ERR_NO_DEVICE;
+    }
+    StaticSetup su;
+    ma_status st = static_setup(dev, &su);
+    if (st != MA_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int ni = (int)n;
+    double* base = su.base;
+    double* dinv = base;
+    double* r = base + kStaticMaxN;
+    double* z = base + 2 * kStaticMaxN;
+    double* p = base + 3 * kStaticMaxN;
+    double* q = base + 4 * kStaticMaxN;
+    double* part = base + 5 * kStaticMaxN;
+    double* out = part + 3 * kStaticMaxBlocks;
+    k_dinv<<<(ni + 255) / 256, 256, 0, s>>>(rowptr, col, val, ni, dinv);
+    int want = (ni + kPcgThreads - 1) / kPcgThreads;
+    int nb = want < su.max_blocks ? want : su.max_blocks;
+    if (nb < 1) nb = 1;
+    PcgArgs a;
+    a.n = ni;
+    a.rowptr = rowptr;
+    a.col = col;
+    a.val = val;
+    a.dinv = dinv;
+    a.b = g;
+    a.x = d;
+    a.r = r;
+    a.z = z;
+    a.p = p;
+    a.q = q;
+    a.part = part;
+    a.out = out;
+    a.rtol = rtol > 0 ? rtol : 1e-10;
+    a.maxiter = maxiter > 0 ? (int)maxiter : 20000;
+    void* args[] = {&a};
+    if (cudaLaunchCooperativeKernel((void*)k_pcg, dim3(nb), dim3(kPcgThreads), args, 0, s) != cudaSuccess) {
+        cudaGetLastError();
+        return MA_ERR_CUDA;
+    }
+    double res[3] = {0, 0, 0};
+    if (cudaMemcpyAsync(res, out, sizeof(res), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        return MA_ERR_CUDA;
+    }
+    if (iters) *iters = (int64_t)res[0];
+    return MA_OK;
+}
 
 void ma_solve_opts_default(ma_solve_opts* o)
 {
