@@ -170,6 +170,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-evals", type=int, default=0,
+                    help="profiling driver: solve once, then run this many Laguerre evaluations at the "
+                         "solution weights and print per-kernel device times (no benchmark line)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -211,6 +214,16 @@ def main():
         api.ot_solve(dmesh, x, nu, x=w, y=y, eps_g=p.tol_rel, stop="rel", precision=args.precision,
                      stats=st, ctx=ctx)
         return w, st
+
+    if args.profile_evals:
+        wsol, _ = solve_device()
+        X = torch.stack([x, y], 1)
+        ctx.profile(True)
+        for _ in range(args.profile_evals):
+            api.kantorovich(dmesh, X, wsol, ctx=ctx)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_evals": args.profile_evals, **ctx.profile_read()}))
+        return
 
     for _ in range(args.warmup):
         solve_device()

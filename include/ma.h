@@ -81,8 +81,10 @@ int64_t ma_ctx_launch_count(const ma_ctx* ctx);
 
 /* Device-time profile of the main kernels (CUDA events around each launch). */
 typedef struct ma_profile {
-    double cells_ms;          /* Laguerre cell kernel (main pass) */
+    double cells_ms;          /* Laguerre cells: site-tree search and clipping (stage 1) */
     int64_t cells_launches;
+    double pieces_ms;         /* cell-triangle pieces: clipping and FP64 integrals (stage 2) */
+    int64_t pieces_launches;
     double cells_large_ms;    /* large-capacity pass */
     int64_t cells_large_launches;
     double bounds_ms;         /* site-tree bounds, once per evaluation */
@@ -91,6 +93,9 @@ typedef struct ma_profile {
     int64_t pcg_launches;
     int64_t pcg_iters;
     int64_t large_sites;      /* sites redone by the large-capacity pass */
+    int64_t search[6];        /* stage-1 totals: tree nodes popped, node bounds tested, nodes
+                                 pruned, candidate sites clipped against, clips that cut,
+                                 final neighbours */
 } ma_profile;
 /* enable != 0: reset the profile and start recording; 0: stop. */
 ma_status ma_ctx_profile(ma_ctx* ctx, int enable);

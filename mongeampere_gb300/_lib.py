@@ -32,10 +32,11 @@ class MaStats(ctypes.Structure):
 
 class MaProfile(ctypes.Structure):
     _fields_ = [("cells_ms", ctypes.c_double), ("cells_launches", ctypes.c_int64),
+                ("pieces_ms", ctypes.c_double), ("pieces_launches", ctypes.c_int64),
                 ("cells_large_ms", ctypes.c_double), ("cells_large_launches", ctypes.c_int64),
                 ("bounds_ms", ctypes.c_double), ("bounds_launches", ctypes.c_int64),
                 ("pcg_ms", ctypes.c_double), ("pcg_launches", ctypes.c_int64), ("pcg_iters", ctypes.c_int64),
-                ("large_sites", ctypes.c_int64)]
+                ("large_sites", ctypes.c_int64), ("search", ctypes.c_int64 * 6)]
 
 
 # every symbol include/ma.h declares, with its ctypes signature

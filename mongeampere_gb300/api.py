@@ -84,7 +84,9 @@ class Context:
     def profile_read(self) -> dict:
         p = L.MaProfile()
         _check(self.lib, self.h, self.lib.ma_ctx_profile_read(self.h, ctypes.byref(p)), "ma_ctx_profile_read")
-        return {f: getattr(p, f) for f, _ in L.MaProfile._fields_}
+        out = {f: getattr(p, f) for f, _ in L.MaProfile._fields_}
+        out["search"] = list(out["search"])
+        return out
 
     def mesh(self, mesh) -> "DeviceMesh":
         return DeviceMesh(self, mesh)

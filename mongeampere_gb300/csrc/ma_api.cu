@@ -122,6 +122,7 @@ ma_status build_site_index(Ctx* c, const Mesh* m, int n, const double* x, const 
                       c->t_boxf.as<float4>(), s);
     c->launches += 1 + 8 * 5 + 1 + 2;
     c->n = n;
+    c->prev_valid = false;
     return MA_OK;
 }
 
@@ -135,6 +136,9 @@ static ma_status ensure_eval_buffers(Ctx* c, int n, bool mom)
     MA_CUDA(c, c->st_col.ensure(sizeof(int) * scap * (size_t)n));
     MA_CUDA(c, c->st_val.ensure(sizeof(double) * scap * (size_t)n));
     MA_CUDA(c, c->big_index.ensure(sizeof(int) * (size_t)n));
+    MA_CUDA(c, c->nb_cnt.ensure(sizeof(int) * (size_t)n));
+    MA_CUDA(c, c->nb_lab.ensure(sizeof(int) * (size_t)stage1_cap() * (size_t)n));
+    MA_CUDA(c, c->cell_box.ensure(sizeof(double4) * (size_t)n));
     MA_CUDA(c, c->rowptr.ensure(sizeof(int) * ((size_t)n + 1)));
     MA_CUDA(c, c->status.ensure(sizeof(uint32_t) * 4));
     MA_CUDA(c, c->redo.ensure(sizeof(int) * (size_t)n));
@@ -150,13 +154,29 @@ static ma_status ensure_eval_buffers(Ctx* c, int n, bool mom)
     return MA_OK;
 }
 
+// main pass: stage 1 (cells) then stage 2 (pieces); cap_kind 1: large-capacity pass
 static void launch_cells(Ctx* c, const Mesh* m, const CellArgs& a, int cap_kind, bool mom)
 {
-    if (m->kind == 0)
-        launch_cells_grid(a, m->grid_dev(), cap_kind, mom, c->stream);
-    else
-        launch_cells_tri(a, m->tri_dev(), cap_kind, mom, c->stream);
-    c->launches += 1;
+    if (cap_kind == 0) {
+        {
+            ProfScope ps(c, &c->profile.cells_ms, &c->profile.cells_launches);
+            launch_cells_stage1(a, c->stream);
+        }
+        {
+            ProfScope ps(c, &c->profile.pieces_ms, &c->profile.pieces_launches);
+            if (m->kind == 0)
+                launch_pieces_grid(a, m->grid_dev(), mom, c->stream);
+            else
+                launch_pieces_tri(a, m->tri_dev(), mom, c->stream);
+        }
+        c->launches += 2;
+    } else {
+        if (m->kind == 0)
+            launch_cells_large_grid(a, m->grid_dev(), mom, c->stream);
+        else
+            launch_cells_large_tri(a, m->tri_dev(), mom, c->stream);
+        c->launches += 1;
+    }
 }
 
 // One Laguerre evaluation for the sites of the current grid with weights w (device,
@@ -207,14 +227,21 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     a.work = nullptr;
     a.nwork = 0;
     a.scratch = nullptr;
+    a.prev_valid = c->prev_valid ? 1 : 0;
+    a.counters = nullptr;
+    if (c->prof) {
+        MA_CUDA(c, c->counters.ensure(8 * sizeof(unsigned long long)));
+        MA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), s));
+        a.counters = c->counters.as<unsigned long long>();
+    }
+    a.nb_cnt = c->nb_cnt.as<int>();
+    a.nb_lab = c->nb_lab.as<int>();
+    a.cell_box = c->cell_box.as<double4>();
     a.big_index = c->big_index.as<int>();
     a.big_col = nullptr;
     a.big_val = nullptr;
     a.big_cap = large_row_cap();
-    {
-        ProfScope ps(c, &c->profile.cells_ms, &c->profile.cells_launches);
-        launch_cells(c, m, a, 0, f.moments > 0);
-    }
+    launch_cells(c, m, a, 0, f.moments > 0);
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaStreamSynchronize(s));
@@ -244,7 +271,13 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         if (c->hinfo[0] > 0)
             return fail(c, MA_ERR_CAPACITY, "a Laguerre cell has more vertices than the largest kernel capacity");
     }
+    if (a.counters) {
+        unsigned long long cnt[8];
+        MA_CUDA(c, cudaMemcpy(cnt, a.counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+        for (int q = 0; q < 6; q++) c->profile.search[q] += (int64_t)cnt[q];
+    }
     uint32_t stbits = (uint32_t)c->hinfo[1];
+    c->prev_valid = true;
     if (stbits & ST_EXACT_OVERFLOW)
         return fail(c, MA_ERR_EXACT_OVERFLOW, "an exact predicate exceeded its expansion capacity");
     if (stbits & ST_BAD_INPUT) return fail(c, MA_ERR_INVALID_ARGUMENT, "non-finite site or weight");
@@ -333,7 +366,7 @@ void ma_ctx_destroy(ma_ctx* c)
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->hx, &c->hy, &c->hw, &c->hnu, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
+    DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
                       &c->perm, &c->sites, &c->posf, &c->scan_scratch, &c->fill, &c->t_child, &c->t_range,
                       &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab,
                       &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,

@@ -36,6 +36,7 @@ enum : uint32_t {
     ST_EXACT_OVERFLOW = 2u,  // an exact predicate ran out of expansion capacity
     ST_ROW_OVERFLOW = 4u,    // a Hessian row did not fit its staging slots
     ST_BAD_INPUT = 8u,       // non-finite input
+    ST_NEED_EXACT = 16u,     // a predicate needed exact arithmetic (cell redone by the exact pass)
 };
 
 struct SiteD {
@@ -188,57 +189,62 @@ MA_HD void ex_acc(Exp<CH>& h, const Exp<CF>& f, double sgn, bool& ok)
 }
 
 // Side1: is fixed point E strictly closer (power distance) to the owner than to c?
-MA_HDNI int sym_side1(const Owner& o, const SiteD& c, double ex, double ey, uint32_t& st)
+// The filter returns the sign of pi(E, owner, c) when certain, 0 otherwise.
+MA_HD int filt_side1(const Owner& o, const SiteD& c, double ex, double ey)
 {
-    int s = r_sign(r_pi(o.x, o.y, o.w, c.x, c.y, c.w, ex, ey));
-    if (s == 0) {
-        bool ok = true;
-        Exp<kExS> h;
-        ex_pi(h, o.x, o.y, o.w, c.x, c.y, c.w, ex, ey, ok);
-        if (!ok) st |= ST_EXACT_OVERFLOW;
-        s = ex_sign(h);
-    }
-    return s < 0;
+    return r_sign(r_pi(o.x, o.y, o.w, c.x, c.y, c.w, ex, ey));
+}
+
+MA_HDNI int exact_side1(const Owner& o, const SiteD& c, double ex, double ey, uint32_t& st)
+{
+    bool ok = true;
+    Exp<kExS> h;
+    ex_pi(h, o.x, o.y, o.w, c.x, c.y, c.w, ex, ey, ok);
+    if (!ok) st |= ST_EXACT_OVERFLOW;
+    return ex_sign(h);
 }
 
 // Side3: E = segment line (p, q) crossing the radical axis of (owner, u).
 // With A = pi(., owner, u), B = pi(., owner, c):
 //   pi(E, owner, c) = (A(p) B(q) - A(q) B(p)) / (A(p) - A(q)).
-MA_HDNI int sym_side3(const Owner& o, const SiteD& u, double px, double py, double qx, double qy,
-                      const SiteD& c, uint32_t& st)
+// FP64 filter: +1 / -1 for a certain sign of pi(E, owner, c), 0 when undecided
+MA_HD int filt_side3(const Owner& o, const SiteD& u, double px, double py, double qx, double qy, const SiteD& c)
 {
     R Ap = r_pi(o.x, o.y, o.w, u.x, u.y, u.w, px, py), Aq = r_pi(o.x, o.y, o.w, u.x, u.y, u.w, qx, qy);
     R Bp = r_pi(o.x, o.y, o.w, c.x, c.y, c.w, px, py), Bq = r_pi(o.x, o.y, o.w, c.x, c.y, c.w, qx, qy);
     int sd = r_sign(r_sub(r_mul(Ap, Bq), r_mul(Aq, Bp)));
     int sn = r_sign(r_sub(Ap, Aq));
-    if (sd == 0 || sn == 0) {
-        bool ok = true;
-        Exp<kExS> eAp, eAq, eBp, eBq;
-        ex_pi(eAp, o.x, o.y, o.w, u.x, u.y, u.w, px, py, ok);
-        ex_pi(eAq, o.x, o.y, o.w, u.x, u.y, u.w, qx, qy, ok);
-        ex_pi(eBp, o.x, o.y, o.w, c.x, c.y, c.w, px, py, ok);
-        ex_pi(eBq, o.x, o.y, o.w, c.x, c.y, c.w, qx, qy, ok);
-        Exp<kExL> t1, t2;
-        ex_mul2(t1, eAp, eBq, ok);
-        ex_mul2(t2, eAq, eBp, ok);
-        ex_acc(t1, t2, -1.0, ok);
-        sd = ex_sign(t1);
-        Exp<kExL> dn;
-        ex_set(dn, 0.0);
-        ex_acc(dn, eAp, 1.0, ok);
-        ex_acc(dn, eAq, -1.0, ok);
-        sn = ex_sign(dn);
-        if (!ok) st |= ST_EXACT_OVERFLOW;
-    }
-    if (sn == 0) return 0;
-    return sd * sn < 0;
+    return sd * sn;
+}
+
+MA_HDNI int exact_side3(const Owner& o, const SiteD& u, double px, double py, double qx, double qy, const SiteD& c,
+                        uint32_t& st)
+{
+    bool ok = true;
+    Exp<kExS> eAp, eAq, eBp, eBq;
+    ex_pi(eAp, o.x, o.y, o.w, u.x, u.y, u.w, px, py, ok);
+    ex_pi(eAq, o.x, o.y, o.w, u.x, u.y, u.w, qx, qy, ok);
+    ex_pi(eBp, o.x, o.y, o.w, c.x, c.y, c.w, px, py, ok);
+    ex_pi(eBq, o.x, o.y, o.w, c.x, c.y, c.w, qx, qy, ok);
+    Exp<kExL> t1, t2;
+    ex_mul2(t1, eAp, eBq, ok);
+    ex_mul2(t2, eAq, eBp, ok);
+    ex_acc(t1, t2, -1.0, ok);
+    int sd = ex_sign(t1);
+    Exp<kExL> dn;
+    ex_set(dn, 0.0);
+    ex_acc(dn, eAp, 1.0, ok);
+    ex_acc(dn, eAq, -1.0, ok);
+    int sn = ex_sign(dn);
+    if (!ok) st |= ST_EXACT_OVERFLOW;
+    return sd * sn;  // sn == 0: the radical axis is parallel to the segment, no vertex
 }
 
 // Side2: E = weighted circumcentre of (owner, a, b).  Relative to the owner, with
 // d_k = x_k - x_o and z_k = |d_k|^2 - (w_k - w_o):
 //   pi(E, owner, c) = M / D,  D = d_a x d_b,
 //   M = d_c.x (z_a d_b.y - z_b d_a.y) + d_c.y (d_a.x z_b - d_b.x z_a) - z_c D.
-MA_HDNI int sym_side2(const Owner& o, const SiteD& a, const SiteD& b, const SiteD& c, uint32_t& st)
+MA_HD int filt_side2(const Owner& o, const SiteD& a, const SiteD& b, const SiteD& c)
 {
     R dax = r_sub(rv(a.x), rv(o.x)), day = r_sub(rv(a.y), rv(o.y));
     R dbx = r_sub(rv(b.x), rv(o.x)), dby = r_sub(rv(b.y), rv(o.y));
@@ -250,76 +256,85 @@ MA_HDNI int sym_side2(const Owner& o, const SiteD& a, const SiteD& b, const Site
     R M = r_mul(dcx, r_sub(r_mul(za, dby), r_mul(zb, day)));
     M = r_add(M, r_mul(dcy, r_sub(r_mul(dax, zb), r_mul(dbx, za))));
     M = r_sub(M, r_mul(zc, D));
-    int sm = r_sign(M), sd = r_sign(D);
-    if (sm == 0 || sd == 0) {
-        bool ok = true;
-        Exp<4> ax, ay, bx, by, cx, cy;
-        ex_diff(ax, a.x, o.x);
-        ex_diff(ay, a.y, o.y);
-        ex_diff(bx, b.x, o.x);
-        ex_diff(by, b.y, o.y);
-        ex_diff(cx, c.x, o.x);
-        ex_diff(cy, c.y, o.y);
-        Exp<kExS> Z[3];
-        const Exp<4>* px[3] = {&ax, &bx, &cx};
-        const Exp<4>* py[3] = {&ay, &by, &cy};
-        const SiteD* ps[3] = {&a, &b, &c};
-        for (int k = 0; k < 3; k++) {
-            Exp<kExS> sq;
-            ex_mul2(Z[k], *px[k], *px[k], ok);
-            ex_mul2(sq, *py[k], *py[k], ok);
-            ex_acc(Z[k], sq, 1.0, ok);
-            Exp<4> dw;
-            ex_diff(dw, ps[k]->w, o.w);
-            ex_acc(Z[k], dw, -1.0, ok);
-        }
-        Exp<kExS> Dx, t;
-        ex_mul2(Dx, ax, by, ok);
-        ex_mul2(t, ay, bx, ok);
-        ex_acc(Dx, t, -1.0, ok);
-        sd = ex_sign(Dx);
-        Exp<kExL> Mx, u1, u2, v;
-        // za*dby - zb*day
-        ex_mul2(u1, Z[0], by, ok);
-        ex_mul2(u2, Z[1], ay, ok);
-        ex_acc(u1, u2, -1.0, ok);
-        ex_mul2(Mx, u1, cx, ok);
-        // dax*zb - dbx*za
-        ex_mul2(u1, ax, Z[1], ok);
-        ex_mul2(u2, bx, Z[0], ok);
-        ex_acc(u1, u2, -1.0, ok);
-        ex_mul2(v, u1, cy, ok);
-        ex_acc(Mx, v, 1.0, ok);
-        ex_mul2(v, Z[2], Dx, ok);
-        ex_acc(Mx, v, -1.0, ok);
-        sm = ex_sign(Mx);
-        if (!ok) st |= ST_EXACT_OVERFLOW;
+    return r_sign(M) * r_sign(D);
+}
+
+MA_HDNI int exact_side2(const Owner& o, const SiteD& a, const SiteD& b, const SiteD& c, uint32_t& st)
+{
+    int sm, sd;
+    bool ok = true;
+    Exp<4> ax, ay, bx, by, cx, cy;
+    ex_diff(ax, a.x, o.x);
+    ex_diff(ay, a.y, o.y);
+    ex_diff(bx, b.x, o.x);
+    ex_diff(by, b.y, o.y);
+    ex_diff(cx, c.x, o.x);
+    ex_diff(cy, c.y, o.y);
+    Exp<kExS> Z[3];
+    const Exp<4>* px[3] = {&ax, &bx, &cx};
+    const Exp<4>* py[3] = {&ay, &by, &cy};
+    const SiteD* ps[3] = {&a, &b, &c};
+    for (int k = 0; k < 3; k++) {
+        Exp<kExS> sq;
+        ex_mul2(Z[k], *px[k], *px[k], ok);
+        ex_mul2(sq, *py[k], *py[k], ok);
+        ex_acc(Z[k], sq, 1.0, ok);
+        Exp<4> dw;
+        ex_diff(dw, ps[k]->w, o.w);
+        ex_acc(Z[k], dw, -1.0, ok);
     }
-    if (sd == 0) return 0;
-    return sm * sd < 0;
+    Exp<kExS> Dx, t;
+    ex_mul2(Dx, ax, by, ok);
+    ex_mul2(t, ay, bx, ok);
+    ex_acc(Dx, t, -1.0, ok);
+    sd = ex_sign(Dx);
+    Exp<kExL> Mx, u1, u2, v;
+    // za*dby - zb*day
+    ex_mul2(u1, Z[0], by, ok);
+    ex_mul2(u2, Z[1], ay, ok);
+    ex_acc(u1, u2, -1.0, ok);
+    ex_mul2(Mx, u1, cx, ok);
+    // dax*zb - dbx*za
+    ex_mul2(u1, ax, Z[1], ok);
+    ex_mul2(u2, bx, Z[0], ok);
+    ex_acc(u1, u2, -1.0, ok);
+    ex_mul2(v, u1, cy, ok);
+    ex_acc(Mx, v, 1.0, ok);
+    ex_mul2(v, Z[2], Dx, ok);
+    ex_acc(Mx, v, -1.0, ok);
+    sm = ex_sign(Mx);
+    if (!ok) st |= ST_EXACT_OVERFLOW;
+    return sm * sd;  // sd == 0: collinear sites, no weighted circumcentre
 }
 
 // Is the vertex between edges `prev` and `cur` strictly closer to the owner than
-// to slot c's site?  (Tri_intersector::inside, vti.hpp:129-166.)
-template <int CAP>
-MA_HDNI int sym_inside(int prev, int cur, const Slot* slots, const Fixed& fx, const Owner& o,
-                       const SiteD* sites, int csite, uint32_t& st)
+// to slot c's site?  (Tri_intersector::inside, vti.hpp:129-166.)  Without EXACT an
+// undecided filter sets `undecided` (the caller redoes the cell with EXACT).
+template <int CAP, bool EXACT>
+MA_HDNI bool sym_inside(int prev, int cur, const Slot* slots, const Fixed& fx, const Owner& o, const SiteD* sites,
+                        int csite, uint32_t& st, bool& undecided)
 {
     const SiteD c = sites[csite];
+    int s;
     if (prev < 0 && cur < 0) {
         int e = -1 - cur;
-        return sym_side1(o, c, fx.ax[e], fx.ay[e], st);
-    }
-    if (prev >= 0 && cur >= 0) {
+        s = filt_side1(o, c, fx.ax[e], fx.ay[e]);
+        if (s == 0 && EXACT) s = exact_side1(o, c, fx.ax[e], fx.ay[e], st);
+    } else if (prev >= 0 && cur >= 0) {
         const SiteD a = sites[slots[prev].site];
         const SiteD b = sites[slots[cur].site];
-        return sym_side2(o, a, b, c, st);
+        s = filt_side2(o, a, b, c);
+        if (s == 0 && EXACT) s = exact_side2(o, a, b, c, st);
+    } else {
+        int e = (prev < 0) ? -1 - prev : -1 - cur;
+        int u = (prev < 0) ? cur : prev;
+        int e1 = (e + 1 == fx.n) ? 0 : e + 1;
+        const SiteD us = sites[slots[u].site];
+        s = filt_side3(o, us, fx.ax[e], fx.ay[e], fx.ax[e1], fx.ay[e1], c);
+        if (s == 0 && EXACT) s = exact_side3(o, us, fx.ax[e], fx.ay[e], fx.ax[e1], fx.ay[e1], c, st);
     }
-    int e = (prev < 0) ? -1 - prev : -1 - cur;
-    int u = (prev < 0) ? cur : prev;
-    int e1 = (e + 1 == fx.n) ? 0 : e + 1;
-    const SiteD us = sites[slots[u].site];
-    return sym_side3(o, us, fx.ax[e], fx.ay[e], fx.ax[e1], fx.ay[e1], c, st);
+    if (s == 0 && !EXACT) undecided = true;
+    return s < 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -380,8 +395,9 @@ MA_HD void new_vertex(int edge, int cslot, const Slot* slots, const Fixed& fx, f
 
 // Sutherland-Hodgman clip of P by the half-plane of slot `cs` (vti.hpp:168-198).
 // Returns false (and leaves Q untouched) when no vertex lies outside.  Sets
-// `overflow` when the result would exceed CAP.
-template <int CAP>
+// `overflow` when the result would exceed CAP, or (without EXACT) when a vertex
+// needs exact arithmetic.
+template <int CAP, bool EXACT>
 MA_HD bool clip_poly(const Poly<CAP>& P, Poly<CAP>& Q, int cs, const Slot* slots, const Fixed& fx,
                      const Owner& o, const SiteD* sites, uint32_t& st, bool& overflow)
 {
@@ -397,7 +413,14 @@ MA_HD bool clip_poly(const Poly<CAP>& P, Poly<CAP>& Q, int cs, const Slot* slots
             out = t > 0;
         } else {
             int prev = P.lab[k == 0 ? n - 1 : k - 1];
-            out = !sym_inside<CAP>(prev, P.lab[k], slots, fx, o, sites, c.site, st);
+            bool undecided = false;
+            out = !sym_inside<CAP, EXACT>(prev, P.lab[k], slots, fx, o, sites, c.site, st, undecided);
+            if (undecided) {
+                // an exact decision is needed: the cell is redone by the exact pass
+                st |= ST_NEED_EXACT;
+                overflow = true;
+                return true;
+            }
         }
         if (out) {
             outm.set(k);
@@ -485,7 +508,7 @@ MA_HD void vtx64(int prev, int cur, const Nb64* nb, const Fixed& fx, double& X, 
     Y = py + t * ey;
 }
 
-// per-site FP64 accumulators
+// per-site FP64 accumulators (u = x - x_site)
 struct Acc {
     double mass, second;
     double m1x, m1y;         // int rho u
@@ -499,6 +522,8 @@ struct Acc {
 //   int u          = cr (a + b) / 6
 //   int u u^T      = cr/12 (a a^T + b b^T) + cr/24 (a b^T + b a^T)
 //   int u |u|^2    = cr/60 [a (3|a|^2 + 2 a.b + |b|^2) + b (|a|^2 + 2 a.b + 3|b|^2)]
+//   int u_x^3      = cr/20 (a_x^3 + a_x^2 b_x + a_x b_x^2 + b_x^3)
+//   int u_x^2 u_y  = cr/60 (3 a_x^2 a_y + a_x^2 b_y + 2 a_x b_x a_y + 2 a_x b_x b_y + b_x^2 a_y + 3 b_x^2 b_y)
 // (monomial integrals over a simplex).  These are exact for the integrands of
 // kantorovich.hpp:125-131 and lloyd.hpp:57-62, as are the reference's
 // centroid and Albrecht-Collatz rules.  Each DT edge adds |e x d| rho(mid) to
@@ -513,6 +538,7 @@ MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, 
     vtx64(P.lab[n - 1], P.lab[0], nb, fx, x0, y0);
     double ax = x0, ay = y0;
     double m0 = 0, m1x = 0, m1y = 0, q2 = 0, c3x = 0, c3y = 0, sxx = 0, syy = 0, sxy = 0;
+    double t30 = 0, t21 = 0, t12 = 0, t03 = 0;
     for (int k = 0; k < n; k++) {
         double bx, by;
         if (k + 1 < n)
@@ -534,6 +560,13 @@ MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, 
             sxx += cr * (2.0 * (ax * ax + bx * bx) + 2.0 * ax * bx);
             syy += cr * (2.0 * (ay * ay + by * by) + 2.0 * ay * by);
             sxy += cr * (2.0 * (ax * ay + bx * by) + ax * by + bx * ay);
+            // third moments over the triangle (0, a, b): int u_x^3, u_x^2 u_y, u_x u_y^2, u_y^3
+            t30 += cr * 3.0 * (ax * ax * ax + ax * ax * bx + ax * bx * bx + bx * bx * bx);
+            t21 += cr * (3.0 * ax * ax * ay + ax * ax * by + 2.0 * ax * bx * ay + 2.0 * ax * bx * by + bx * bx * ay +
+                         3.0 * bx * bx * by);
+            t12 += cr * (3.0 * ay * ay * ax + ay * ay * bx + 2.0 * ay * by * ax + 2.0 * ay * by * bx + by * by * ax +
+                         3.0 * by * by * bx);
+            t03 += cr * 3.0 * (ay * ay * ay + ay * ay * by + ay * by * by + by * by * by);
         }
         int lab = P.lab[k];
         if (lab >= 0) {
@@ -556,10 +589,12 @@ MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, 
     acc.second += c0 * Iq + gx * Icx + gy * Icy;
     if (MOM) {
         double Sxx = sxx * (1.0 / 24.0), Syy = syy * (1.0 / 24.0), Sxy = sxy * (1.0 / 24.0);
+        double T30 = t30 * (1.0 / 60.0), T21 = t21 * (1.0 / 60.0), T12 = t12 * (1.0 / 60.0), T03 = t03 * (1.0 / 60.0);
         acc.m1x += c0 * Iux + gx * Sxx + gy * Sxy;
         acc.m1y += c0 * Iuy + gx * Sxy + gy * Syy;
-        // int rho u u^T needs third moments: int u_a u_b u_c
-        // (accumulated by the caller through integrate_piece_m2 when requested)
+        acc.sxx += c0 * Sxx + gx * T30 + gy * T21;
+        acc.syy += c0 * Syy + gx * T12 + gy * T03;
+        acc.sxy += c0 * Sxy + gx * T21 + gy * T12;
     }
 }
 

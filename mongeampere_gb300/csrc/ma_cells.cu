@@ -1,0 +1,850 @@
+// ma_cells.cu -- Laguerre cells and their pieces (the hot path of one evaluation).
+//
+// Reference behaviour: voronoi_triangulation_intersection_raw / Tri_intersector
+// (include/MA/voronoi_triangulation_intersection.hpp:42-313) produce every
+// non-empty (site, triangle) piece; kantorovich's callback
+// (include/MA/kantorovich.hpp:87-136) integrates it.  Here the same pieces are
+// produced cell by cell in two kernels:
+//
+//   stage 1, k_cells_stage1 (one thread per site): branch and bound over the site
+//     tree; Sutherland-Hodgman clips of the mesh's bounding box give the cell and
+//     its neighbour list, written out with the cell's bounding box;
+//   stage 2, k_pieces_* (one warp per site): the neighbour slots go to shared
+//     memory, the lanes take the mesh triangles under the cell's box, each lane
+//     clips its triangle by the neighbours and integrates the piece in FP64, and
+//     warp reductions (fixed order, so results are reproducible) assemble the
+//     mass, the value part and the Hessian row.
+//
+// Cells that outgrow the 48 slots of stage 1 are redone end to end by
+// k_cells_large, one thread per cell with a 256-slot workspace in global scratch.
+#include "ma_internal.h"
+
+namespace ma {
+
+// ---------------------------------------------------------------------------
+// mesh access
+// ---------------------------------------------------------------------------
+
+// largest i in [0, n-2] with g[i] <= x (clamped)
+__device__ __forceinline__ int find_square(const double* g, int n, double x)
+{
+    if (!(x > g[0])) return 0;
+    if (x >= g[n - 1]) return n - 2;
+    int lo = 0, hi = n - 2;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (g[mid] <= x)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// square (i, j) of the grid mesh, triangle tt (0: (i,j) (i+1,j) (i+1,j+1);
+// 1: (i,j) (i+1,j+1) (i,j+1)), owner-relative; rho(u) = c0 + g . u
+__device__ __forceinline__ void grid_triangle(const MeshGridDev& m, int i, int j, int tt, const Owner& o, Fixed& T,
+                                              double& c0, double& gx, double& gy)
+{
+    double X0 = m.gx[i], X1 = m.gx[i + 1], Y0 = m.gy[j], Y1 = m.gy[j + 1];
+    const double* row0 = m.val + (size_t)j * m.nx;
+    const double* row1 = row0 + m.nx;
+    double v00 = row0[i], v10 = row0[i + 1], v01 = row1[i], v11 = row1[i + 1];
+    T.n = 3;
+    set_fixed(T, 0, X0, Y0, o);
+    if (tt == 0) {
+        set_fixed(T, 1, X1, Y0, o);
+        set_fixed(T, 2, X1, Y1, o);
+        gx = (v10 - v00) * m.ihx[i];
+        gy = (v11 - v10) * m.ihy[j];
+    } else {
+        set_fixed(T, 1, X1, Y1, o);
+        set_fixed(T, 2, X0, Y1, o);
+        gx = (v11 - v01) * m.ihx[i];
+        gy = (v01 - v00) * m.ihy[j];
+    }
+    c0 = v00 - gx * T.rx[0] - gy * T.ry[0];
+}
+
+__device__ __forceinline__ void tri_triangle(const MeshTriDev& m, int t, const Owner& o, Fixed& T, double& c0,
+                                             double& gx, double& gy)
+{
+    int a0 = m.tri[3 * t], a1 = m.tri[3 * t + 1], a2 = m.tri[3 * t + 2];
+    T.n = 3;
+    set_fixed(T, 0, m.vx[a0], m.vy[a0], o);
+    set_fixed(T, 1, m.vx[a1], m.vy[a1], o);
+    set_fixed(T, 2, m.vx[a2], m.vy[a2], o);
+    double l0 = m.lin[3 * t];
+    gx = m.lin[3 * t + 1];
+    gy = m.lin[3 * t + 2];
+    c0 = l0 - gx * T.rx[0] - gy * T.ry[0];
+}
+
+struct GridVisitor {
+    MeshGridDev m;
+    template <class Fn>
+    __device__ __forceinline__ void visit(const Owner& o, double bx0, double by0, double bx1, double by1,
+                                          Fn&& fn) const
+    {
+        if (bx1 < m.gx[0] || bx0 > m.gx[m.nx - 1] || by1 < m.gy[0] || by0 > m.gy[m.ny - 1]) return;
+        int i0 = find_square(m.gx, m.nx, bx0), i1 = find_square(m.gx, m.nx, bx1);
+        int j0 = find_square(m.gy, m.ny, by0), j1 = find_square(m.gy, m.ny, by1);
+        Fixed T;
+        for (int j = j0; j <= j1; j++)
+            for (int i = i0; i <= i1; i++)
+                for (int tt = 0; tt < 2; tt++) {
+                    double c0, gx, gy;
+                    grid_triangle(m, i, j, tt, o, T, c0, gx, gy);
+                    fn(T, c0, gx, gy);
+                }
+    }
+};
+
+// bin range of a box; false when it misses the mesh
+__device__ __forceinline__ bool tri_bins(const MeshTriDev& m, double bx0, double by0, double bx1, double by1,
+                                         int& cx0, int& cy0, int& cx1, int& cy1)
+{
+    cx0 = (int)floor((bx0 - m.bx0) / m.bcw);
+    cx1 = (int)floor((bx1 - m.bx0) / m.bcw);
+    cy0 = (int)floor((by0 - m.by0) / m.bch);
+    cy1 = (int)floor((by1 - m.by0) / m.bch);
+    if (cx1 < 0 || cy1 < 0 || cx0 >= m.bnx || cy0 >= m.bny) return false;
+    cx0 = max(cx0, 0);
+    cy0 = max(cy0, 0);
+    cx1 = min(cx1, m.bnx - 1);
+    cy1 = min(cy1, m.bny - 1);
+    return true;
+}
+
+struct TriVisitor {
+    MeshTriDev m;
+    template <class Fn>
+    __device__ __forceinline__ void visit(const Owner& o, double bx0, double by0, double bx1, double by1,
+                                          Fn&& fn) const
+    {
+        int cx0, cy0, cx1, cy1;
+        if (!tri_bins(m, bx0, by0, bx1, by1, cx0, cy0, cx1, cy1)) return;
+        Fixed T;
+        for (int by = cy0; by <= cy1; by++) {
+            for (int bx = cx0; bx <= cx1; bx++) {
+                int b = by * m.bnx + bx;
+                for (int q = m.bin_start[b]; q < m.bin_start[b + 1]; q++) {
+                    int t = m.bin_tri[q];
+                    int4 r = m.tbin[t];
+                    // visit each triangle once: from the first bin shared with the box
+                    if (bx != max(r.x, cx0) || by != max(r.y, cy0)) continue;
+                    double c0, gx, gy;
+                    tri_triangle(m, t, o, T, c0, gx, gy);
+                    fn(T, c0, gx, gy);
+                }
+            }
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// workspaces
+// ---------------------------------------------------------------------------
+template <int CAP>
+struct Work {  // the whole cell in one thread (large-capacity pass)
+    Slot slots[CAP];
+    Poly<CAP> PA, PB;
+    double hv[CAP];
+    Nb64 nb[CAP];
+    int map[CAP];
+    int cols[CAP];
+    double vals[CAP];
+};
+
+template <int CAP>
+struct Work1 {  // stage 1: cell only
+    Slot slots[CAP];
+    Poly<CAP> PA, PB;
+    int map[CAP];
+};
+
+template <int CAP>
+__device__ __forceinline__ void compact_slots(Poly<CAP>& P, Slot* slots, int* map, int& ns)
+{
+    Bits<CAP> used;
+    used.clear();
+    for (int e = 0; e < P.n; e++)
+        if (P.lab[e] >= 0) used.set(P.lab[e]);
+    int m = 0;
+    for (int s = 0; s < ns; s++) {
+        if (used.get(s)) {
+            map[s] = m;
+            if (m != s) slots[m] = slots[s];
+            m++;
+        } else {
+            map[s] = -1;
+        }
+    }
+    for (int e = 0; e < P.n; e++)
+        if (P.lab[e] >= 0) P.lab[e] = map[P.lab[e]];
+    ns = m;
+}
+
+// Can no site of internal node nd cut polygon P?  With phi_j >= alpha + beta.x_j
+// over the node and the node's box [c - h, c + h]:
+//   pi_ij(p) / 2 = p.(x_j - x_i) + phi_i - phi_j
+//              <= (p - beta).(c - x_i) + |p_x - beta_x| h_x + |p_y - beta_y| h_y - K,
+//   K = alpha + beta.x_i - phi_i,
+// convex in p, so it suffices that it is negative at every vertex of P.  K and
+// x_i - beta are formed in FP64; the box enters through its FP32 copy (rounded
+// outwards, so it contains the node's sites) relative to the FP32 site position,
+// with the conversion errors absorbed into a wider box; every FP32 rounding of the
+// per-vertex loop is bounded.
+template <int CAP>
+__device__ __forceinline__ bool node_harmless(const Poly<CAP>& P, const Owner& o, double phi_o, float ox, float oy,
+                                              const float4 bf, const double4 ab)
+{
+    if (!(ab.x > -INFINITY)) return false;
+    double t = fma(ab.y, o.x, fma(ab.z, o.y, ab.x));
+    double K = t - phi_o;
+    float fK = (float)K;
+    float fke = 1.2e-16f * (fabsf((float)ab.x) + fabsf((float)t) + fabsf((float)phi_o)) * 8.0f + 1e-37f;
+    float fex = (float)(o.x - ab.y), fey = (float)(o.y - ab.z);
+    // box relative to the FP32 owner position; widen by the FP32 errors of the
+    // owner position and of the subtraction
+    float cx = 0.5f * (bf.x + bf.z) - ox, cy = 0.5f * (bf.y + bf.w) - oy;
+    float hx = 0.5f * (bf.z - bf.x), hy = 0.5f * (bf.w - bf.y);
+    float wx = 1.2e-7f * (fabsf(bf.x) + fabsf(bf.z) + 2.0f * fabsf(ox)) + 1e-37f;
+    float wy = 1.2e-7f * (fabsf(bf.y) + fabsf(bf.w) + 2.0f * fabsf(oy)) + 1e-37f;
+    hx = hx * 1.000001f + wx;
+    hy = hy * 1.000001f + wy;
+    float L = fabsf(cx) + fabsf(cy) + hx + hy;
+    float e0 = 1.2e-7f * (fabsf(fex) + fabsf(fey));
+    for (int v = 0; v < P.n; v++) {
+        float qx = fex + P.ux[v], qy = fey + P.uy[v];
+        float T = qx * cx + qy * cy + fabsf(qx) * hx + fabsf(qy) * hy - fK;
+        float S = fabsf(qx * cx) + fabsf(qy * cy) + fabsf(qx) * hx + fabsf(qy) * hy + fabsf(fK);
+        float err = 1e-6f * S + (P.ur[v] + e0) * L * 1.0001f + fke + 1e-36f;
+        if (!(T + err < 0.0f)) return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// the cell stage: branch and bound over the site tree
+// ---------------------------------------------------------------------------
+constexpr int kCapSmall = 48;
+constexpr int kSeedCap = kCapSmall;  // neighbour-list stride between the stages
+
+struct CellOut {
+    bool overflow;
+    bool empty;
+    uint32_t st;
+    int ns;  // neighbour slots after compaction
+    int popped, tested, pruned, visited, cuts;
+};
+
+template <int CAP, bool EXACT>
+__device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Owner& o, Slot* slots, int* map,
+                              Poly<CAP>*& P, Poly<CAP>*& Q)
+{
+    CellOut r{false, false, 0u, 0, 0, 0, 0, 0, 0};
+    const int gi = A.perm[k];
+    Fixed box;
+    box.n = 4;
+    set_fixed(box, 0, A.X0, A.Y0, o);
+    set_fixed(box, 1, A.X1, A.Y0, o);
+    set_fixed(box, 2, A.X1, A.Y1, o);
+    set_fixed(box, 3, A.X0, A.Y1, o);
+    P->n = 4;
+    for (int e = 0; e < 4; e++) {
+        P->lab[e] = -1 - e;
+        P->ux[e] = box.ux[e];
+        P->uy[e] = box.uy[e];
+        P->ur[e] = box.ur[e];
+    }
+    if (!(isfinite(S.x) && isfinite(S.y) && isfinite(S.w))) {
+        r.st |= ST_BAD_INPUT;
+        r.empty = true;
+        P->n = 0;
+        return r;
+    }
+    int ns = 0;
+    const SiteTree& T = A.tree;
+    const double phi_o = 0.5 * (S.x * S.x + S.y * S.y - S.w);
+    const float ox = (float)S.x, oy = (float)S.y;
+    constexpr int kStack = 80;
+    constexpr int kBucket = 8;
+    constexpr int kWindow = 8;
+    int stack[kStack];
+    int sp = 0;
+    if (T.n >= 2) stack[sp++] = 0;
+    // Seeds, clipped first so that the walk below starts from a nearly final cell:
+    // the previous evaluation's neighbours (same sites, nearby weights), or else the
+    // Morton-order window around the site.  The walk skips the seeds.
+    int nseed = 0;
+    int seeds[kSeedCap];
+    if (A.prev_valid && A.nb_cnt[k] > 0 && A.nb_cnt[k] <= kSeedCap) {
+        nseed = A.nb_cnt[k];
+        const int* pl = A.nb_lab + (size_t)k * kSeedCap;
+        for (int s = 0; s < nseed; s++) seeds[s] = pl[s];
+    }
+    const bool windowed = nseed == 0;
+    auto is_seed = [&](int q) -> bool {
+        if (windowed) return q >= k - kWindow && q <= k + kWindow;
+        for (int s = 0; s < nseed; s++)
+            if (seeds[s] == q) return true;
+        return false;
+    };
+    auto visit = [&](int q) -> bool {  // clip by sorted site q; false when the cell became empty
+        if (q == k) return true;
+        const SiteD C = A.sites[q];
+        if (C.x == S.x && C.y == S.y) {
+            // coincident sites: the larger weight, then the lower index, keeps the cell
+            int gj = A.perm[q];
+            if (C.w > S.w || (C.w == S.w && gj < gi)) return false;
+            return true;
+        }
+        if (ns == CAP) {
+            compact_slots(*P, slots, map, ns);
+            if (ns == CAP) {
+                r.overflow = true;
+                return true;
+            }
+        }
+        slots[ns] = make_slot(q, C, o);
+        r.visited++;
+        if (clip_poly<CAP, EXACT>(*P, *Q, ns, slots, box, o, A.sites, r.st, r.overflow)) {
+            if (r.overflow) return true;
+            r.cuts++;
+            Poly<CAP>* t = P;
+            P = Q;
+            Q = t;
+            ns++;
+            if (P->n == 0) return false;
+        }
+        return true;
+    };
+    auto dist2 = [&](int c) -> float {
+        if (c < 0) {
+            float2 p = T.posf[c & 0x7fffffff];
+            float dx = p.x - ox, dy = p.y - oy;
+            return dx * dx + dy * dy;
+        }
+        float4 b = T.boxf[c];
+        float dx = fmaxf(fmaxf(b.x - ox, ox - b.z), 0.0f), dy = fmaxf(fmaxf(b.y - oy, oy - b.w), 0.0f);
+        return dx * dx + dy * dy;
+    };
+    if (windowed) {
+        for (int q = max(k - kWindow, 0); q <= min(k + kWindow, A.n - 1) && !r.empty && !r.overflow; q++)
+            if (!visit(q)) r.empty = true;
+    } else {
+        for (int s = 0; s < nseed && !r.empty && !r.overflow; s++)
+            if (!visit(seeds[s])) r.empty = true;
+    }
+    while (sp > 0 && !r.empty && !r.overflow) {
+        int nd = stack[--sp];
+        r.popped++;
+        if (nd < 0) {
+            int q = nd & 0x7fffffff;
+            if (!is_seed(q) && !visit(q)) r.empty = true;
+            continue;
+        }
+        int2 rg = T.range[nd];
+        bool contains = rg.x <= k && k <= rg.y;
+        if (!contains) {
+            r.tested++;
+            if (node_harmless(*P, o, phi_o, ox, oy, T.boxf[nd], T.ab[nd])) {
+                r.pruned++;
+                continue;
+            }
+        }
+        if (rg.y - rg.x < kBucket) {
+            for (int q = rg.x; q <= rg.y && !r.empty && !r.overflow; q++)
+                if (!is_seed(q) && !visit(q)) r.empty = true;
+            continue;
+        }
+        int2 ch = T.child[nd];
+        if (sp > kStack - 2) {
+            r.overflow = true;
+            break;
+        }
+        // nearer child on top
+        if (dist2(ch.x) <= dist2(ch.y)) {
+            stack[sp++] = ch.y;
+            stack[sp++] = ch.x;
+        } else {
+            stack[sp++] = ch.x;
+            stack[sp++] = ch.y;
+        }
+    }
+    if (r.empty) P->n = 0;
+    if (!r.empty && !r.overflow && P->n > 0) compact_slots(*P, slots, map, ns);
+    r.ns = ns;
+    return r;
+}
+
+// conservative absolute bounding box of polygon P (owner-relative FP32 + radii)
+template <int CAP>
+__device__ __forceinline__ double4 cell_box(const Poly<CAP>& P, const SiteD& S, const CellArgs& A)
+{
+    float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+    for (int e = 0; e < P.n; e++) {
+        float r = P.ur[e] * 1.0001f;
+        mnx = fminf(mnx, P.ux[e] - r);
+        mxx = fmaxf(mxx, P.ux[e] + r);
+        mny = fminf(mny, P.uy[e] - r);
+        mxy = fmaxf(mxy, P.uy[e] + r);
+    }
+    if (!(mxx - mnx < INFINITY && mxy - mny < INFINITY)) return make_double4(A.X0, A.Y0, A.X1, A.Y1);
+    double sx = fmax(fabs((double)mnx), fabs((double)mxx)), sy = fmax(fabs((double)mny), fabs((double)mxy));
+    return make_double4(S.x + (double)mnx - 1e-6 * sx - 1e-300, S.y + (double)mny - 1e-6 * sy - 1e-300,
+                        S.x + (double)mxx + 1e-6 * sx + 1e-300, S.y + (double)mxy + 1e-6 * sy + 1e-300);
+}
+
+// ---------------------------------------------------------------------------
+// outputs of one site
+// ---------------------------------------------------------------------------
+template <bool MOM>
+__device__ void write_site(const CellArgs& A, int gi, const SiteD& S, const Acc& acc, int m, const Slot* slots,
+                           const Nb64* nb, const double* hvtot, const uint64_t* touched_words, int* cols,
+                           double* vals, int big_slot)
+{
+    A.mass[gi] = acc.mass;
+    A.vpart[gi] = S.w * acc.mass - acc.second;
+    if (MOM && A.mom) {
+        double* mo = A.mom + 6 * (size_t)gi;
+        double M = acc.mass;
+        mo[0] = M;
+        mo[1] = acc.m1x + S.x * M;
+        mo[2] = acc.m1y + S.y * M;
+        // int rho x x^T = int rho u u^T + x_i (int rho u)^T + (int rho u) x_i^T + M x_i x_i^T
+        mo[3] = acc.sxx + 2.0 * S.x * acc.m1x + S.x * S.x * M;
+        mo[4] = acc.syy + 2.0 * S.y * acc.m1y + S.y * S.y * M;
+        mo[5] = acc.sxy + S.x * acc.m1y + S.y * acc.m1x + S.x * S.y * M;
+    }
+    if (!A.rowcnt) return;
+    // off-diagonal entries sorted by original index, diagonal in place
+    int cnt = 0;
+    double diag = 0.0;
+    for (int s = 0; s < m; s++) {
+        if (!((touched_words[s >> 6] >> (s & 63)) & 1ull)) continue;
+        double d2 = nb[s].dx * nb[s].dx + nb[s].dy * nb[s].dy;
+        double v = -hvtot[s] / (2.0 * d2);
+        diag -= v;
+        int c = A.perm[slots[s].site];
+        int j = cnt - 1;
+        while (j >= 0 && cols[j] > c) {
+            cols[j + 1] = cols[j];
+            vals[j + 1] = vals[j];
+            j--;
+        }
+        cols[j + 1] = c;
+        vals[j + 1] = v;
+        cnt++;
+    }
+    int total = cnt > 0 ? cnt + 1 : 0;
+    A.rowcnt[gi] = total;
+    int* oc;
+    double* ov;
+    if (big_slot >= 0) {
+        oc = A.big_col + (size_t)big_slot * A.big_cap;
+        ov = A.big_val + (size_t)big_slot * A.big_cap;
+        A.big_index[gi] = big_slot;
+    } else {
+        oc = A.st_col + (size_t)gi * A.scap;
+        ov = A.st_val + (size_t)gi * A.scap;
+    }
+    if (total == 0) return;
+    int w = 0;
+    bool placed = false;
+    for (int j = 0; j < cnt; j++) {
+        if (!placed && cols[j] > gi) {
+            oc[w] = gi;
+            ov[w] = diag;
+            w++;
+            placed = true;
+        }
+        oc[w] = cols[j];
+        ov[w] = vals[j];
+        w++;
+    }
+    if (!placed) {
+        oc[w] = gi;
+        ov[w] = diag;
+    }
+}
+
+__device__ __forceinline__ void write_empty(const CellArgs& A, int gi, bool mom)
+{
+    A.mass[gi] = 0.0;
+    A.vpart[gi] = 0.0;
+    if (mom && A.mom)
+        for (int q = 0; q < 6; q++) A.mom[6 * (size_t)gi + q] = 0.0;
+    if (A.rowcnt) A.rowcnt[gi] = 0;
+}
+
+// clip triangle T by slots 0..m-1 and integrate the piece
+template <int CAP, bool MOM, bool EXACT>
+__device__ __forceinline__ bool piece(const Fixed& T, double c0, double gx, double gy, const Slot* slots,
+                                      const Nb64* nb, int m, const Owner& o, const SiteD* sites, Poly<CAP>* Wp,
+                                      Poly<CAP>* Vp, Acc& acc, double* hv, Bits<CAP>& touched, uint32_t& st)
+{
+    bool overflow = false;
+    Wp->n = 3;
+    for (int e = 0; e < 3; e++) {
+        Wp->lab[e] = -1 - e;
+        Wp->ux[e] = T.ux[e];
+        Wp->uy[e] = T.uy[e];
+        Wp->ur[e] = T.ur[e];
+    }
+    for (int s = 0; s < m; s++) {
+        if (clip_poly<CAP, EXACT>(*Wp, *Vp, s, slots, T, o, sites, st, overflow)) {
+            if (overflow) return false;
+            Poly<CAP>* t = Wp;
+            Wp = Vp;
+            Vp = t;
+            if (Wp->n == 0) return true;
+        }
+    }
+    integrate_piece<CAP, MOM>(*Wp, nb, T, c0, gx, gy, acc, hv, touched);
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// one thread per cell, workspace in global scratch (large cells)
+// ---------------------------------------------------------------------------
+template <int CAP, bool MOM, class Mesh>
+__device__ void process_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>& W, int big_slot)
+{
+    const SiteD S = A.sites[k];
+    const int gi = A.perm[k];
+    Owner o{S.x, S.y, S.w, k};
+    Poly<CAP>* P = &W.PA;
+    Poly<CAP>* Q = &W.PB;
+    CellOut c = cell_stage<CAP, true>(A, k, S, o, W.slots, W.map, P, Q);
+    uint32_t st = c.st;
+    if (c.overflow) {
+        if (A.redo) A.redo[atomicAdd(A.nredo, 1)] = k;
+        atomicOr(A.status, ST_POLY_OVERFLOW);
+        return;
+    }
+    Acc acc{0, 0, 0, 0, 0, 0, 0};
+    Bits<CAP> touched;
+    touched.clear();
+    const int m = c.empty ? 0 : c.ns;
+    if (!c.empty && P->n > 0) {
+        for (int s = 0; s < m; s++) {
+            W.nb[s] = make_nb64(A.sites[W.slots[s].site], o);
+            W.hv[s] = 0.0;
+        }
+        double4 bb = cell_box(*P, S, A);
+        bool bad = false;
+        M.visit(o, bb.x, bb.y, bb.z, bb.w, [&](const Fixed& T, double c0, double gx, double gy) {
+            if (bad) return;
+            if (!piece<CAP, MOM, true>(T, c0, gx, gy, W.slots, W.nb, m, o, A.sites, P, Q, acc, W.hv, touched, st))
+                bad = true;
+        });
+        if (bad) {
+            if (A.redo) A.redo[atomicAdd(A.nredo, 1)] = k;
+            atomicOr(A.status, ST_POLY_OVERFLOW);
+            return;
+        }
+    }
+    write_site<MOM>(A, gi, S, acc, m, W.slots, W.nb, W.hv, touched.w, W.cols, W.vals, big_slot);
+    if (st) atomicOr(A.status, st);
+}
+
+// ---------------------------------------------------------------------------
+// stage 1: one thread per cell
+// ---------------------------------------------------------------------------
+constexpr int kCapLarge = 256;
+constexpr int kPieceCap = kCapSmall + 4;  // a triangle clipped by at most kCapSmall neighbours
+
+__global__ void __launch_bounds__(128) k_cells_stage1(CellArgs A)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.n) return;
+    const SiteD S = A.sites[k];
+    Owner o{S.x, S.y, S.w, k};
+    Work1<kCapSmall> W;
+    Poly<kCapSmall>* P = &W.PA;
+    Poly<kCapSmall>* Q = &W.PB;
+    CellOut c = cell_stage<kCapSmall, false>(A, k, S, o, W.slots, W.map, P, Q);
+    if (c.st) atomicOr(A.status, c.st & ~ST_NEED_EXACT);
+    if (A.counters) {
+        atomicAdd(&A.counters[0], (unsigned long long)c.popped);
+        atomicAdd(&A.counters[1], (unsigned long long)c.tested);
+        atomicAdd(&A.counters[2], (unsigned long long)c.pruned);
+        atomicAdd(&A.counters[3], (unsigned long long)c.visited);
+        atomicAdd(&A.counters[4], (unsigned long long)c.cuts);
+        atomicAdd(&A.counters[5], (unsigned long long)c.ns);
+    }
+    if (c.overflow) {
+        A.nb_cnt[k] = -2;  // finished by the large-capacity pass
+        A.redo[atomicAdd(A.nredo, 1)] = k;
+        atomicOr(A.status, ST_POLY_OVERFLOW);
+        return;
+    }
+    if (c.empty || P->n == 0) {
+        A.nb_cnt[k] = -1;
+        return;
+    }
+    int* lab = A.nb_lab + (size_t)k * kCapSmall;
+    for (int s = 0; s < c.ns; s++) lab[s] = W.slots[s].site;
+    A.nb_cnt[k] = c.ns;
+    A.cell_box[k] = cell_box(*P, S, A);
+}
+
+// ---------------------------------------------------------------------------
+// stage 2: one warp per cell
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <bool MOM>
+__device__ __forceinline__ void warp_reduce_acc(Acc& a)
+{
+    a.mass = warp_sum(a.mass);
+    a.second = warp_sum(a.second);
+    if (MOM) {
+        a.m1x = warp_sum(a.m1x);
+        a.m1y = warp_sum(a.m1y);
+        a.sxx = warp_sum(a.sxx);
+        a.syy = warp_sum(a.syy);
+        a.sxy = warp_sum(a.sxy);
+    }
+}
+
+constexpr int kPieceWarps = 4;
+
+struct PieceShared {
+    Slot slot[kPieceWarps][kCapSmall];
+    Nb64 nb[kPieceWarps][kCapSmall];
+    double hv[kPieceWarps][kCapSmall];
+    int cols[kPieceWarps][kCapSmall];
+    double vals[kPieceWarps][kCapSmall];
+    uint64_t touched[kPieceWarps];
+};
+
+// everything after the per-lane pieces: reductions and the outputs (lane 0)
+template <bool MOM>
+__device__ __forceinline__ void finish_warp(const CellArgs& A, PieceShared& sh, int wib, int lane, int gi, int k,
+                                            const SiteD& S, Acc& acc, int m, const double* hv,
+                                            const Bits<kPieceCap>& touched, uint32_t st)
+{
+    // a piece that needed exact arithmetic (or overflowed): the whole cell is redone
+    // by the exact pass
+    unsigned redo = __ballot_sync(0xffffffffu, (st & (ST_NEED_EXACT | ST_POLY_OVERFLOW)) != 0);
+    if (redo) {
+        if (lane == 0) {
+            A.redo[atomicAdd(A.nredo, 1)] = k;
+            atomicOr(A.status, ST_POLY_OVERFLOW);
+        }
+        return;
+    }
+    warp_reduce_acc<MOM>(acc);
+    uint64_t tw = 0;
+    for (int s = 0; s < m; s++) {
+        double t = warp_sum(hv[s]);
+        unsigned any = __ballot_sync(0xffffffffu, touched.get(s));
+        if (lane == 0) sh.hv[wib][s] = t;
+        if (any) tw |= 1ull << s;
+    }
+    if (st) atomicOr(A.status, st);
+    __syncwarp();
+    if (lane == 0)
+        write_site<MOM>(A, gi, S, acc, m, sh.slot[wib], sh.nb[wib], sh.hv[wib], &tw, sh.cols[wib], sh.vals[wib], -1);
+}
+
+template <bool MOM>
+__global__ void __launch_bounds__(32 * kPieceWarps) k_pieces_grid(CellArgs A, MeshGridDev M)
+{
+    __shared__ PieceShared sh;
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k = blockIdx.x * kPieceWarps + wib;
+    if (k >= A.n) return;
+    const int m = A.nb_cnt[k];
+    if (m == -2) return;
+    const int gi = A.perm[k];
+    if (m == -1) {
+        if (lane == 0) write_empty(A, gi, MOM);
+        return;
+    }
+    const SiteD S = A.sites[k];
+    Owner o{S.x, S.y, S.w, k};
+    Slot* slots = sh.slot[wib];
+    Nb64* nb = sh.nb[wib];
+    for (int s = lane; s < m; s += 32) {
+        int q = A.nb_lab[(size_t)k * kCapSmall + s];
+        SiteD C = A.sites[q];
+        slots[s] = make_slot(q, C, o);
+        nb[s] = make_nb64(C, o);
+    }
+    __syncwarp();
+    Acc acc{0, 0, 0, 0, 0, 0, 0};
+    double hv[kCapSmall];
+    for (int s = 0; s < m; s++) hv[s] = 0.0;
+    Bits<kPieceCap> touched;
+    touched.clear();
+    uint32_t st = 0;
+    const double4 bb = A.cell_box[k];
+    if (!(bb.z < M.gx[0] || bb.x > M.gx[M.nx - 1] || bb.w < M.gy[0] || bb.y > M.gy[M.ny - 1])) {
+        int i0 = find_square(M.gx, M.nx, bb.x), i1 = find_square(M.gx, M.nx, bb.z);
+        int j0 = find_square(M.gy, M.ny, bb.y), j1 = find_square(M.gy, M.ny, bb.w);
+        const int nsx = i1 - i0 + 1;
+        const int ntri = 2 * nsx * (j1 - j0 + 1);
+        Poly<kPieceCap> PA, PB;
+        Fixed T;
+        for (int t = lane; t < ntri; t += 32) {
+            int sq = t >> 1, tt = t & 1;
+            int i = i0 + sq % nsx, j = j0 + sq / nsx;
+            double c0, gx, gy;
+            grid_triangle(M, i, j, tt, o, T, c0, gx, gy);
+            if (!piece<kPieceCap, MOM, false>(T, c0, gx, gy, slots, nb, m, o, A.sites, &PA, &PB, acc, hv, touched,
+                                              st))
+                break;
+        }
+    }
+    finish_warp<MOM>(A, sh, wib, lane, gi, k, S, acc, m, hv, touched, st);
+}
+
+template <bool MOM>
+__global__ void __launch_bounds__(32 * kPieceWarps) k_pieces_tri(CellArgs A, MeshTriDev M)
+{
+    __shared__ PieceShared sh;
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k = blockIdx.x * kPieceWarps + wib;
+    if (k >= A.n) return;
+    const int m = A.nb_cnt[k];
+    if (m == -2) return;
+    const int gi = A.perm[k];
+    if (m == -1) {
+        if (lane == 0) write_empty(A, gi, MOM);
+        return;
+    }
+    const SiteD S = A.sites[k];
+    Owner o{S.x, S.y, S.w, k};
+    Slot* slots = sh.slot[wib];
+    Nb64* nb = sh.nb[wib];
+    for (int s = lane; s < m; s += 32) {
+        int q = A.nb_lab[(size_t)k * kCapSmall + s];
+        SiteD C = A.sites[q];
+        slots[s] = make_slot(q, C, o);
+        nb[s] = make_nb64(C, o);
+    }
+    __syncwarp();
+    Acc acc{0, 0, 0, 0, 0, 0, 0};
+    double hv[kCapSmall];
+    for (int s = 0; s < m; s++) hv[s] = 0.0;
+    Bits<kPieceCap> touched;
+    touched.clear();
+    uint32_t st = 0;
+    const double4 bb = A.cell_box[k];
+    int cx0, cy0, cx1, cy1;
+    if (tri_bins(M, bb.x, bb.y, bb.z, bb.w, cx0, cy0, cx1, cy1)) {
+        // the lanes split the flat list of (bin, entry) in order: entry f goes to
+        // lane f mod 32; each lane keeps a short queue and all lanes drain their
+        // queues together
+        constexpr int kQ = 4;
+        int queue[kQ];
+        int nq = 0;
+        int flat = 0;
+        Poly<kPieceCap> PA, PB;
+        Fixed T;
+        auto drain = [&]() {
+            for (int q = 0; q < nq; q++) {
+                double c0, gx, gy;
+                tri_triangle(M, queue[q], o, T, c0, gx, gy);
+                if (!piece<kPieceCap, MOM, false>(T, c0, gx, gy, slots, nb, m, o, A.sites, &PA, &PB, acc, hv,
+                                                  touched, st))
+                    break;
+            }
+            nq = 0;
+        };
+        for (int by = cy0; by <= cy1; by++) {
+            for (int bx = cx0; bx <= cx1; bx++) {
+                int b = by * M.bnx + bx;
+                int q0 = M.bin_start[b], q1 = M.bin_start[b + 1];
+                for (int base = q0; base < q1; base += 32) {
+                    int q = base + ((lane - flat) & 31);
+                    if (q < q1) {
+                        int t = M.bin_tri[q];
+                        int4 r = M.tbin[t];
+                        if (bx == max(r.x, cx0) && by == max(r.y, cy0)) queue[nq++] = t;
+                    }
+                    // every lane took at most one entry of this round
+                    flat += min(32, q1 - base);
+                    if (__any_sync(0xffffffffu, nq == kQ)) drain();
+                }
+            }
+        }
+        drain();
+    }
+    finish_warp<MOM>(A, sh, wib, lane, gi, k, S, acc, m, hv, touched, st);
+}
+
+// ---------------------------------------------------------------------------
+// large-capacity pass and launchers
+// ---------------------------------------------------------------------------
+template <int CAP, bool MOM, class Mesh>
+__global__ void __launch_bounds__(64) k_cells_large(CellArgs A, Mesh M)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.nwork) return;
+    Work<CAP>* W = reinterpret_cast<Work<CAP>*>(A.scratch) + t;
+    process_site<CAP, MOM>(A, M, A.work[t], *W, t);
+}
+
+size_t large_work_bytes() { return sizeof(Work<kCapLarge>); }
+int large_row_cap() { return kCapLarge + 1; }
+int small_row_cap() { return kCapSmall + 1; }
+int stage1_cap() { return kCapSmall; }
+
+void launch_cells_stage1(const CellArgs& a, cudaStream_t s)
+{
+    if (a.n <= 0) return;
+    k_cells_stage1<<<(a.n + 127) / 128, 128, 0, s>>>(a);
+}
+
+void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s)
+{
+    if (a.n <= 0) return;
+    int g = (a.n + kPieceWarps - 1) / kPieceWarps;
+    if (mom)
+        k_pieces_grid<true><<<g, 32 * kPieceWarps, 0, s>>>(a, m);
+    else
+        k_pieces_grid<false><<<g, 32 * kPieceWarps, 0, s>>>(a, m);
+}
+
+void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s)
+{
+    if (a.n <= 0) return;
+    int g = (a.n + kPieceWarps - 1) / kPieceWarps;
+    if (mom)
+        k_pieces_tri<true><<<g, 32 * kPieceWarps, 0, s>>>(a, m);
+    else
+        k_pieces_tri<false><<<g, 32 * kPieceWarps, 0, s>>>(a, m);
+}
+
+void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s)
+{
+    if (a.nwork <= 0) return;
+    int g = (a.nwork + 63) / 64;
+    GridVisitor v{m};
+    if (mom)
+        k_cells_large<kCapLarge, true><<<g, 64, 0, s>>>(a, v);
+    else
+        k_cells_large<kCapLarge, false><<<g, 64, 0, s>>>(a, v);
+}
+
+void launch_cells_large_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s)
+{
+    if (a.nwork <= 0) return;
+    int g = (a.nwork + 63) / 64;
+    TriVisitor v{m};
+    if (mom)
+        k_cells_large<kCapLarge, true><<<g, 64, 0, s>>>(a, v);
+    else
+        k_cells_large<kCapLarge, false><<<g, 64, 0, s>>>(a, v);
+}
+
+}  // namespace ma

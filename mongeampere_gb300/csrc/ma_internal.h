@@ -65,6 +65,11 @@ struct CellArgs {
     int* nredo;
     const int* work;         // large-capacity pass: the sorted positions to redo
     int nwork;
+    int prev_valid;          // nb_cnt / nb_lab hold the previous evaluation's lists for these sites
+    int* nb_cnt;             // stage 1 -> 2, sorted order: neighbour count, -1 empty cell, -2 large pass
+    int* nb_lab;             // stage 1 -> 2: neighbour sorted indices, stage1_cap() per site
+    double4* cell_box;       // stage 1 -> 2: absolute bounding box of the cell
+    unsigned long long* counters;  // optional stage-1 search counters (6)
     void* scratch;           // large-capacity pass: one workspace per work item
     int* big_index;          // per site: row slot in the side buffer, -1 otherwise
     int* big_col;
@@ -94,8 +99,13 @@ void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int*
                         int* flag, const double4* box, void* mom, double4* ab, cudaStream_t s);
 void launch_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);  // exclusive, out has n+1
 size_t scan_scratch_ints(int n);
-void launch_cells_grid(const CellArgs& a, const MeshGridDev& m, int cap_kind, bool mom, cudaStream_t s);
-void launch_cells_tri(const CellArgs& a, const MeshTriDev& m, int cap_kind, bool mom, cudaStream_t s);
+// cell kernels (ma_cells.cu)
+void launch_cells_stage1(const CellArgs& a, cudaStream_t s);
+void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s);
+void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s);
+void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s);
+void launch_cells_large_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s);
+int stage1_cap();
 void launch_csr_compact(int n, const int* rowptr, const int* rowcnt, const int* st_col, const double* st_val,
                         int scap, const int* big_index, const int* big_col, const double* big_val, int big_cap,
                         int* col, double* val, cudaStream_t s);

@@ -76,6 +76,9 @@ struct Ctx {
     // evaluation outputs
     DevBuf mass, vpart, mom, rowcnt, st_col, st_val, rowptr, col, val, status, redo, nredo, stat_partial, stat_out;
     DevBuf big_index, big_col, big_val, big_work;  // large-capacity pass
+    DevBuf nb_cnt, nb_lab, cell_box;               // stage 1 -> stage 2
+    bool prev_valid = false;                       // nb_cnt/nb_lab match the current site index
+    DevBuf counters;                               // stage-1 search counters (profiling)
     DevBuf info;  // status, nredo, nnz
     int64_t nnz = 0;
     bool have_h = false;
