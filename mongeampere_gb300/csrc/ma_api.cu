@@ -190,9 +190,9 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     launch_update_weights(w, c->perm.as<int>(), n, c->sites.as<SiteD>(), s);
     {
         ProfScope ps(c, &c->profile.bounds_ms, &c->profile.bounds_launches);
-        launch_tree_bounds(c->sites.as<SiteD>(), n, c->t_child.as<int2>(), c->t_parent.as<int>(),
-                           c->t_leaf_parent.as<int>(), c->t_flag.as<int>(), c->t_box.as<double4>(), c->t_mom.p,
-                           c->t_ab.as<double4>(), s);
+        launch_tree_bounds(c->sites.as<SiteD>(), n, c->t_child.as<int2>(), c->t_range.as<int2>(),
+                           c->t_parent.as<int>(), c->t_leaf_parent.as<int>(), c->t_flag.as<int>(),
+                           c->t_box.as<double4>(), c->t_mom.p, c->t_ab.as<double4>(), s);
     }
     c->launches += 2;
     MA_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * 4, s));

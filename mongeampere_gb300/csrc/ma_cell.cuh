@@ -529,20 +529,22 @@ struct Acc {
 // centroid and Albrecht-Collatz rules.  Each DT edge adds |e x d| rho(mid) to
 // hv[slot]; the Hessian entry is then -hv / (2 |d|^2) (kantorovich.hpp:110-121:
 // length * rho(mid) / (2 |x_i - x_j|), with length = |e x d| / |d|).
-template <int CAP, bool MOM>
-MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, double c0, double gx,
-                           double gy, Acc& acc, double* hv, Bits<CAP>& touched)
+// The polygon is given by its edge labels lab(0..n-1); edge(k, slot, v) receives the
+// Hessian part v of edge k when that edge lies on the radical axis of `slot`.
+template <bool MOM, class Lab, class Edge>
+MA_HD void integrate_labels(int n, const Lab& lab_of, const Nb64* nb, const Fixed& fx, double c0, double gx,
+                            double gy, Acc& acc, const Edge& edge)
 {
-    const int n = P.n;
     double x0, y0;
-    vtx64(P.lab[n - 1], P.lab[0], nb, fx, x0, y0);
+    vtx64(lab_of(n - 1), lab_of(0), nb, fx, x0, y0);
     double ax = x0, ay = y0;
     double m0 = 0, m1x = 0, m1y = 0, q2 = 0, c3x = 0, c3y = 0, sxx = 0, syy = 0, sxy = 0;
     double t30 = 0, t21 = 0, t12 = 0, t03 = 0;
     for (int k = 0; k < n; k++) {
         double bx, by;
+        const int lab = lab_of(k);
         if (k + 1 < n)
-            vtx64(P.lab[k], P.lab[k + 1], nb, fx, bx, by);
+            vtx64(lab, lab_of(k + 1), nb, fx, bx, by);
         else {
             bx = x0;
             by = y0;
@@ -568,14 +570,12 @@ MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, 
                          3.0 * by * by * bx);
             t03 += cr * 3.0 * (ay * ay * ay + ay * ay * by + ay * by * by + by * by * by);
         }
-        int lab = P.lab[k];
         if (lab >= 0) {
             const Nb64 d = nb[lab];
             double exv = bx - ax, eyv = by - ay;
             double crs = fabs(exv * d.dy - eyv * d.dx);
             double mx = 0.5 * (ax + bx), my = 0.5 * (ay + by);
-            hv[lab] += crs * (c0 + gx * mx + gy * my);
-            touched.set(lab);
+            edge(k, lab, crs * (c0 + gx * mx + gy * my));
         }
         ax = bx;
         ay = by;
@@ -596,6 +596,18 @@ MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, 
         acc.syy += c0 * Syy + gx * T12 + gy * T03;
         acc.sxy += c0 * Sxy + gx * T21 + gy * T12;
     }
+}
+
+template <int CAP, bool MOM>
+MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, double c0, double gx,
+                           double gy, Acc& acc, double* hv, Bits<CAP>& touched)
+{
+    integrate_labels<MOM>(
+        P.n, [&](int k) { return P.lab[k]; }, nb, fx, c0, gx, gy, acc,
+        [&](int, int lab, double v) {
+            hv[lab] += v;
+            touched.set(lab);
+        });
 }
 
 }  // namespace ma

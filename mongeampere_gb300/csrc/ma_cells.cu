@@ -9,14 +9,16 @@
 //   stage 1, k_cells_stage1 (one thread per site): branch and bound over the site
 //     tree; Sutherland-Hodgman clips of the mesh's bounding box give the cell and
 //     its neighbour list, written out with the cell's bounding box;
-//   stage 2, k_pieces_* (one warp per site): the neighbour slots go to shared
-//     memory, the lanes take the mesh triangles under the cell's box, each lane
-//     clips its triangle by the neighbours and integrates the piece in FP64, and
-//     warp reductions (fixed order, so results are reproducible) assemble the
-//     mass, the value part and the Hessian row.
+//   stage 2, k_pieces (a warp per eight consecutive cells): the lanes clip the
+//     mesh triangles under the cells' boxes by the cells' neighbours into a list of
+//     pieces in shared memory, then integrate the listed pieces one per lane in
+//     FP64, and the per-cell sums (in list order, so results are reproducible)
+//     give the mass, the value part and the Hessian row.
 //
-// Cells that outgrow the 48 slots of stage 1 are redone end to end by
-// k_cells_large, one thread per cell with a 256-slot workspace in global scratch.
+// Cells that outgrow the 48 slots of stage 1, or whose pieces need exact arithmetic
+// or more than 12 vertices, are redone end to end by k_cells_large, one thread per cell with a 256-slot workspace in global scratch.
+#include <climits>
+
 #include "ma_internal.h"
 
 namespace ma {
@@ -42,39 +44,53 @@ __device__ __forceinline__ int find_square(const double* g, int n, double x)
 }
 
 // square (i, j) of the grid mesh, triangle tt (0: (i,j) (i+1,j) (i+1,j+1);
-// 1: (i,j) (i+1,j+1) (i,j+1)), owner-relative; rho(u) = c0 + g . u
-__device__ __forceinline__ void grid_triangle(const MeshGridDev& m, int i, int j, int tt, const Owner& o, Fixed& T,
-                                              double& c0, double& gx, double& gy)
+// 1: (i,j) (i+1,j+1) (i,j+1)), owner-relative corners
+__device__ __forceinline__ void grid_fixed(const MeshGridDev& m, int i, int j, int tt, const Owner& o, Fixed& T)
 {
-    double X0 = m.gx[i], X1 = m.gx[i + 1], Y0 = m.gy[j], Y1 = m.gy[j + 1];
-    const double* row0 = m.val + (size_t)j * m.nx;
-    const double* row1 = row0 + m.nx;
-    double v00 = row0[i], v10 = row0[i + 1], v01 = row1[i], v11 = row1[i + 1];
+    const double X0 = m.gx[i], X1 = m.gx[i + 1], Y0 = m.gy[j], Y1 = m.gy[j + 1];
     T.n = 3;
     set_fixed(T, 0, X0, Y0, o);
     if (tt == 0) {
         set_fixed(T, 1, X1, Y0, o);
         set_fixed(T, 2, X1, Y1, o);
-        gx = (v10 - v00) * m.ihx[i];
-        gy = (v11 - v10) * m.ihy[j];
     } else {
         set_fixed(T, 1, X1, Y1, o);
         set_fixed(T, 2, X0, Y1, o);
+    }
+}
+
+// the same with the density on it, rho(u) = c0 + g . u
+__device__ __forceinline__ void grid_triangle(const MeshGridDev& m, int i, int j, int tt, const Owner& o, Fixed& T,
+                                              double& c0, double& gx, double& gy)
+{
+    grid_fixed(m, i, j, tt, o, T);
+    const double* row0 = m.val + (size_t)j * m.nx;
+    const double* row1 = row0 + m.nx;
+    const double v00 = row0[i], v10 = row0[i + 1], v01 = row1[i], v11 = row1[i + 1];
+    if (tt == 0) {
+        gx = (v10 - v00) * m.ihx[i];
+        gy = (v11 - v10) * m.ihy[j];
+    } else {
         gx = (v11 - v01) * m.ihx[i];
         gy = (v01 - v00) * m.ihy[j];
     }
     c0 = v00 - gx * T.rx[0] - gy * T.ry[0];
 }
 
-__device__ __forceinline__ void tri_triangle(const MeshTriDev& m, int t, const Owner& o, Fixed& T, double& c0,
-                                             double& gx, double& gy)
+__device__ __forceinline__ void tri_fixed(const MeshTriDev& m, int t, const Owner& o, Fixed& T)
 {
-    int a0 = m.tri[3 * t], a1 = m.tri[3 * t + 1], a2 = m.tri[3 * t + 2];
+    const int a0 = m.tri[3 * t], a1 = m.tri[3 * t + 1], a2 = m.tri[3 * t + 2];
     T.n = 3;
     set_fixed(T, 0, m.vx[a0], m.vy[a0], o);
     set_fixed(T, 1, m.vx[a1], m.vy[a1], o);
     set_fixed(T, 2, m.vx[a2], m.vy[a2], o);
-    double l0 = m.lin[3 * t];
+}
+
+__device__ __forceinline__ void tri_triangle(const MeshTriDev& m, int t, const Owner& o, Fixed& T, double& c0,
+                                             double& gx, double& gy)
+{
+    tri_fixed(m, t, o, T);
+    const double l0 = m.lin[3 * t];
     gx = m.lin[3 * t + 1];
     gy = m.lin[3 * t + 2];
     c0 = l0 - gx * T.rx[0] - gy * T.ry[0];
@@ -269,7 +285,7 @@ __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Ow
     const double phi_o = 0.5 * (S.x * S.x + S.y * S.y - S.w);
     const float ox = (float)S.x, oy = (float)S.y;
     constexpr int kStack = 80;
-    constexpr int kBucket = 8;
+    constexpr int kBucket = 4;
     constexpr int kWindow = 8;
     int stack[kStack];
     int sp = 0;
@@ -554,7 +570,6 @@ __device__ void process_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>&
 // stage 1: one thread per cell
 // ---------------------------------------------------------------------------
 constexpr int kCapLarge = 256;
-constexpr int kPieceCap = kCapSmall + 4;  // a triangle clipped by at most kCapSmall neighbours
 
 __global__ void __launch_bounds__(128) k_cells_stage1(CellArgs A)
 {
@@ -592,194 +607,386 @@ __global__ void __launch_bounds__(128) k_cells_stage1(CellArgs A)
 }
 
 // ---------------------------------------------------------------------------
-// stage 2: one warp per cell
+// stage 2: the pieces, batched over the cells of a warp
 // ---------------------------------------------------------------------------
+// A warp takes kWarpCells consecutive cells (neighbours in Morton order) and works
+// in rounds:
+//   A  the lanes walk the flat list of (cell, mesh triangle under the cell's box),
+//      32 entries at a time, clip each triangle by its cell's neighbours (certified
+//      FP32 side tests, FP64 filter) and append every non-empty piece -- cell,
+//      triangle, edge labels -- to a list in shared memory, in list order;
+//   B  each lane integrates one listed piece in FP64, so the lanes stay busy
+//      whatever the sizes of the cells;
+//   C  per cell the pieces' integrals and Hessian parts are summed in list order
+//      (reproducible), and every cell whose triangles are all done is written out
+//      by the whole warp.
+// A cell that needs exact arithmetic or more capacity goes to the large pass.
 __device__ __forceinline__ double warp_sum(double v)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-template <bool MOM>
-__device__ __forceinline__ void warp_reduce_acc(Acc& a)
-{
-    a.mass = warp_sum(a.mass);
-    a.second = warp_sum(a.second);
-    if (MOM) {
-        a.m1x = warp_sum(a.m1x);
-        a.m1y = warp_sum(a.m1y);
-        a.sxx = warp_sum(a.sxx);
-        a.syy = warp_sum(a.syy);
-        a.sxy = warp_sum(a.sxy);
-    }
-}
+constexpr int kPieceWarps = 2;  // warps per block
+constexpr int kWarpCells = 8;   // cells per warp
+constexpr int kSlotPool = 96;   // neighbour slots held per warp
+constexpr int kList = 64;       // listed pieces per round
+constexpr int kPV = 12;         // vertices of a listed piece
+constexpr int kClipCap = 16;    // polygon capacity while a triangle is clipped
+static_assert(kSlotPool >= kCapSmall, "the pool must hold one full cell");
+static_assert(kList >= 64, "a round needs room for one batch of 32 after 32 listed pieces");
+static_assert(kCapSmall <= 64, "two Hessian slots per lane");
 
-constexpr int kPieceWarps = 4;
-
-struct PieceShared {
-    Slot slot[kPieceWarps][kCapSmall];
-    Nb64 nb[kPieceWarps][kCapSmall];
-    double hv[kPieceWarps][kCapSmall];
-    int cols[kPieceWarps][kCapSmall];
-    double vals[kPieceWarps][kCapSmall];
-    uint64_t touched[kPieceWarps];
+struct PieceRec {
+    int tri;
+    int8_t cell, n;
+    int8_t lab[kPV];
 };
 
-// everything after the per-lane pieces: reductions and the outputs (lane 0)
-template <bool MOM>
-__device__ __forceinline__ void finish_warp(const CellArgs& A, PieceShared& sh, int wib, int lane, int gi, int k,
-                                            const SiteD& S, Acc& acc, int m, const double* hv,
-                                            const Bits<kPieceCap>& touched, uint32_t st)
-{
-    // a piece that needed exact arithmetic (or overflowed): the whole cell is redone
-    // by the exact pass
-    unsigned redo = __ballot_sync(0xffffffffu, (st & (ST_NEED_EXACT | ST_POLY_OVERFLOW)) != 0);
-    if (redo) {
-        if (lane == 0) {
-            A.redo[atomicAdd(A.nredo, 1)] = k;
-            atomicOr(A.status, ST_POLY_OVERFLOW);
-        }
-        return;
-    }
-    warp_reduce_acc<MOM>(acc);
-    uint64_t tw = 0;
-    for (int s = 0; s < m; s++) {
-        double t = warp_sum(hv[s]);
-        unsigned any = __ballot_sync(0xffffffffu, touched.get(s));
-        if (lane == 0) sh.hv[wib][s] = t;
-        if (any) tw |= 1ull << s;
-    }
-    if (st) atomicOr(A.status, st);
-    __syncwarp();
-    if (lane == 0)
-        write_site<MOM>(A, gi, S, acc, m, sh.slot[wib], sh.nb[wib], sh.hv[wib], &tw, sh.cols[wib], sh.vals[wib], -1);
-}
+struct CellInfo {
+    int k;     // sorted site index
+    int m;     // neighbour slots (-1 empty cell, -2 left to the large pass)
+    int soff;  // first slot in the pool
+    int pre;   // first flat triangle entry
+    int4 box;  // mesh-specific range of triangles under the cell's box
+};
 
 template <bool MOM>
-__global__ void __launch_bounds__(32 * kPieceWarps) k_pieces_grid(CellArgs A, MeshGridDev M)
-{
-    __shared__ PieceShared sh;
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int k = blockIdx.x * kPieceWarps + wib;
-    if (k >= A.n) return;
-    const int m = A.nb_cnt[k];
-    if (m == -2) return;
-    const int gi = A.perm[k];
-    if (m == -1) {
-        if (lane == 0) write_empty(A, gi, MOM);
-        return;
-    }
-    const SiteD S = A.sites[k];
-    Owner o{S.x, S.y, S.w, k};
-    Slot* slots = sh.slot[wib];
-    Nb64* nb = sh.nb[wib];
-    for (int s = lane; s < m; s += 32) {
-        int q = A.nb_lab[(size_t)k * kCapSmall + s];
-        SiteD C = A.sites[q];
-        slots[s] = make_slot(q, C, o);
-        nb[s] = make_nb64(C, o);
-    }
-    __syncwarp();
-    Acc acc{0, 0, 0, 0, 0, 0, 0};
-    double hv[kCapSmall];
-    for (int s = 0; s < m; s++) hv[s] = 0.0;
-    Bits<kPieceCap> touched;
-    touched.clear();
-    uint32_t st = 0;
-    const double4 bb = A.cell_box[k];
-    if (!(bb.z < M.gx[0] || bb.x > M.gx[M.nx - 1] || bb.w < M.gy[0] || bb.y > M.gy[M.ny - 1])) {
-        int i0 = find_square(M.gx, M.nx, bb.x), i1 = find_square(M.gx, M.nx, bb.z);
-        int j0 = find_square(M.gy, M.ny, bb.y), j1 = find_square(M.gy, M.ny, bb.w);
-        const int nsx = i1 - i0 + 1;
-        const int ntri = 2 * nsx * (j1 - j0 + 1);
-        Poly<kPieceCap> PA, PB;
-        Fixed T;
-        for (int t = lane; t < ntri; t += 32) {
-            int sq = t >> 1, tt = t & 1;
-            int i = i0 + sq % nsx, j = j0 + sq / nsx;
-            double c0, gx, gy;
-            grid_triangle(M, i, j, tt, o, T, c0, gx, gy);
-            if (!piece<kPieceCap, MOM, false>(T, c0, gx, gy, slots, nb, m, o, A.sites, &PA, &PB, acc, hv, touched,
-                                              st))
-                break;
-        }
-    }
-    finish_warp<MOM>(A, sh, wib, lane, gi, k, S, acc, m, hv, touched, st);
-}
+struct PieceWarp {
+    static constexpr int kAcc = MOM ? 7 : 2;
+    Slot slot[kSlotPool];
+    Nb64 nb[kSlotPool];
+    PieceRec rec[kList];
+    double out[kAcc][kList];
+    double hvc[kPV][kList];
+    CellInfo ci[kWarpCells + 1];
+};
 
-template <bool MOM>
-__global__ void __launch_bounds__(32 * kPieceWarps) k_pieces_tri(CellArgs A, MeshTriDev M)
-{
-    __shared__ PieceShared sh;
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int k = blockIdx.x * kPieceWarps + wib;
-    if (k >= A.n) return;
-    const int m = A.nb_cnt[k];
-    if (m == -2) return;
-    const int gi = A.perm[k];
-    if (m == -1) {
-        if (lane == 0) write_empty(A, gi, MOM);
-        return;
+// triangles of the grid mesh under a box: squares [i0, i0+nsx) x [j0, j0+nsy),
+// two triangles each; triangle id = ((j (nx-1) + i) << 1) | tt
+struct GridPieces {
+    MeshGridDev m;
+    __device__ __forceinline__ int setup(const double4& bb, int4& p) const
+    {
+        if (bb.z < m.gx[0] || bb.x > m.gx[m.nx - 1] || bb.w < m.gy[0] || bb.y > m.gy[m.ny - 1]) return 0;
+        int i0 = find_square(m.gx, m.nx, bb.x), i1 = find_square(m.gx, m.nx, bb.z);
+        int j0 = find_square(m.gy, m.ny, bb.y), j1 = find_square(m.gy, m.ny, bb.w);
+        p = make_int4(i0, j0, i1 - i0 + 1, j1 - j0 + 1);
+        return 2 * p.z * p.w;
     }
-    const SiteD S = A.sites[k];
-    Owner o{S.x, S.y, S.w, k};
-    Slot* slots = sh.slot[wib];
-    Nb64* nb = sh.nb[wib];
-    for (int s = lane; s < m; s += 32) {
-        int q = A.nb_lab[(size_t)k * kCapSmall + s];
-        SiteD C = A.sites[q];
-        slots[s] = make_slot(q, C, o);
-        nb[s] = make_nb64(C, o);
+    __device__ __forceinline__ int get(const int4& p, int t) const
+    {
+        int sq = t >> 1;
+        int i = p.x + sq % p.z, j = p.y + sq / p.z;
+        return ((j * (m.nx - 1) + i) << 1) | (t & 1);
     }
-    __syncwarp();
-    Acc acc{0, 0, 0, 0, 0, 0, 0};
-    double hv[kCapSmall];
-    for (int s = 0; s < m; s++) hv[s] = 0.0;
-    Bits<kPieceCap> touched;
-    touched.clear();
-    uint32_t st = 0;
-    const double4 bb = A.cell_box[k];
-    int cx0, cy0, cx1, cy1;
-    if (tri_bins(M, bb.x, bb.y, bb.z, bb.w, cx0, cy0, cx1, cy1)) {
-        // the lanes split the flat list of (bin, entry) in order: entry f goes to
-        // lane f mod 32; each lane keeps a short queue and all lanes drain their
-        // queues together
-        constexpr int kQ = 4;
-        int queue[kQ];
-        int nq = 0;
-        int flat = 0;
-        Poly<kPieceCap> PA, PB;
-        Fixed T;
-        auto drain = [&]() {
-            for (int q = 0; q < nq; q++) {
-                double c0, gx, gy;
-                tri_triangle(M, queue[q], o, T, c0, gx, gy);
-                if (!piece<kPieceCap, MOM, false>(T, c0, gx, gy, slots, nb, m, o, A.sites, &PA, &PB, acc, hv,
-                                                  touched, st))
-                    break;
+    __device__ __forceinline__ void fixed(int id, const Owner& o, Fixed& T) const
+    {
+        int sq = id >> 1;
+        grid_fixed(m, sq % (m.nx - 1), sq / (m.nx - 1), id & 1, o, T);
+    }
+    __device__ __forceinline__ void triangle(int id, const Owner& o, Fixed& T, double& c0, double& gx,
+                                             double& gy) const
+    {
+        int sq = id >> 1;
+        grid_triangle(m, sq % (m.nx - 1), sq / (m.nx - 1), id & 1, o, T, c0, gx, gy);
+    }
+};
+
+// triangles of an explicit mesh under a box: the entries of the box's bins (a row
+// of bins is contiguous in the bin lists); a triangle is taken from the first bin
+// it shares with the box, its other entries give -1
+struct TriPieces {
+    MeshTriDev m;
+    __device__ __forceinline__ int setup(const double4& bb, int4& p) const
+    {
+        int cx0, cy0, cx1, cy1;
+        if (!tri_bins(m, bb.x, bb.y, bb.z, bb.w, cx0, cy0, cx1, cy1)) return 0;
+        p = make_int4(cx0, cy0, cx1, cy1);
+        int cnt = 0;
+        for (int by = cy0; by <= cy1; by++) cnt += m.bin_start[by * m.bnx + cx1 + 1] - m.bin_start[by * m.bnx + cx0];
+        return cnt;
+    }
+    __device__ __forceinline__ int get(const int4& p, int t) const
+    {
+        for (int by = p.y; by <= p.w; by++) {
+            const int b0 = by * m.bnx + p.x;
+            const int q0 = m.bin_start[b0], r = m.bin_start[by * m.bnx + p.z + 1] - q0;
+            if (t < r) {
+                const int q = q0 + t;
+                int bx = p.x;
+                while (m.bin_start[by * m.bnx + bx + 1] <= q) bx++;
+                const int tri = m.bin_tri[q];
+                const int4 tb = m.tbin[tri];
+                if (bx != max(tb.x, p.x) || by != max(tb.y, p.y)) return -1;
+                return tri;
             }
-            nq = 0;
-        };
-        for (int by = cy0; by <= cy1; by++) {
-            for (int bx = cx0; bx <= cx1; bx++) {
-                int b = by * M.bnx + bx;
-                int q0 = M.bin_start[b], q1 = M.bin_start[b + 1];
-                for (int base = q0; base < q1; base += 32) {
-                    int q = base + ((lane - flat) & 31);
-                    if (q < q1) {
-                        int t = M.bin_tri[q];
-                        int4 r = M.tbin[t];
-                        if (bx == max(r.x, cx0) && by == max(r.y, cy0)) queue[nq++] = t;
+            t -= r;
+        }
+        return -1;
+    }
+    __device__ __forceinline__ void fixed(int id, const Owner& o, Fixed& T) const { tri_fixed(m, id, o, T); }
+    __device__ __forceinline__ void triangle(int id, const Owner& o, Fixed& T, double& c0, double& gx,
+                                             double& gy) const
+    {
+        tri_triangle(m, id, o, T, c0, gx, gy);
+    }
+};
+
+// write one finished cell: lane 0 the masses and moments, lane s (and s + 32) the
+// Hessian entry of neighbour slot s, placed by rank of its column
+template <bool MOM>
+__device__ __forceinline__ void finish_cell(const CellArgs& A, const CellInfo& C, const double* run, double h0,
+                                            double h1, bool t0, bool t1, const Slot* sl, const Nb64* nb, int lane)
+{
+    const int gi = A.perm[C.k];
+    const SiteD S = A.sites[C.k];
+    if (lane == 0) {
+        A.mass[gi] = run[0];
+        A.vpart[gi] = S.w * run[0] - run[1];
+        if (MOM && A.mom) {
+            double* mo = A.mom + 6 * (size_t)gi;
+            const double M = run[0], m1x = run[2], m1y = run[3];
+            mo[0] = M;
+            mo[1] = m1x + S.x * M;
+            mo[2] = m1y + S.y * M;
+            mo[3] = run[4] + 2.0 * S.x * m1x + S.x * S.x * M;
+            mo[4] = run[5] + 2.0 * S.y * m1y + S.y * S.y * M;
+            mo[5] = run[6] + S.x * m1y + S.y * m1x + S.x * S.y * M;
+        }
+    }
+    if (!A.rowcnt) return;
+    const bool a0 = t0 && lane < C.m, a1 = t1 && lane + 32 < C.m;
+    int col0 = INT_MAX, col1 = INT_MAX;
+    double v0 = 0.0, v1 = 0.0;
+    if (a0) {
+        const Nb64 d = nb[lane];
+        v0 = -h0 / (2.0 * (d.dx * d.dx + d.dy * d.dy));
+        col0 = A.perm[sl[lane].site];
+    }
+    if (a1) {
+        const Nb64 d = nb[lane + 32];
+        v1 = -h1 / (2.0 * (d.dx * d.dx + d.dy * d.dy));
+        col1 = A.perm[sl[lane + 32].site];
+    }
+    const double diag = -warp_sum(v0 + v1);
+    const int cnt = __popc(__ballot_sync(0xffffffffu, a0)) + __popc(__ballot_sync(0xffffffffu, a1));
+    const int total = cnt > 0 ? cnt + 1 : 0;
+    if (lane == 0) A.rowcnt[gi] = total;
+    if (total == 0) return;
+    int r0 = gi < col0 ? 1 : 0, r1 = gi < col1 ? 1 : 0, rd = 0;
+    for (int j = 0; j < 32; j++) {
+        const int c0 = __shfl_sync(0xffffffffu, col0, j), c1 = __shfl_sync(0xffffffffu, col1, j);
+        r0 += (c0 < col0) + (c1 < col0);
+        r1 += (c0 < col1) + (c1 < col1);
+        rd += (c0 < gi) + (c1 < gi);
+    }
+    int* oc = A.st_col + (size_t)gi * A.scap;
+    double* ov = A.st_val + (size_t)gi * A.scap;
+    if (a0) {
+        oc[r0] = col0;
+        ov[r0] = v0;
+    }
+    if (a1) {
+        oc[r1] = col1;
+        ov[r1] = v1;
+    }
+    if (lane == 0) {
+        oc[rd] = gi;
+        ov[rd] = diag;
+    }
+}
+
+template <bool MOM, class E>
+__global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
+{
+    constexpr int kAcc = PieceWarp<MOM>::kAcc;
+    constexpr unsigned kFull = 0xffffffffu;
+    __shared__ PieceWarp<MOM> shw[kPieceWarps];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    PieceWarp<MOM>& W = shw[wib];
+    const int kbase = (blockIdx.x * kPieceWarps + wib) * kWarpCells;
+    if (kbase >= A.n) return;
+    const int ncell = min(kWarpCells, A.n - kbase);
+    // lane c sets up cell c
+    int my_m = -2, my_cnt = 0;
+    int4 my_box = make_int4(0, 0, 0, 0);
+    if (lane < ncell) {
+        const int k = kbase + lane;
+        my_m = A.nb_cnt[k];
+        if (my_m == -1) write_empty(A, A.perm[k], MOM);
+        if (my_m >= 0) my_cnt = mesh.setup(A.cell_box[k], my_box);
+    }
+    uint32_t st = 0;
+    unsigned redo = 0;  // cells of the warp to redo (bit c)
+    for (int g0 = 0; g0 < ncell;) {
+        // a group of cells whose neighbour slots fit in the pool
+        int g1 = g0, soff = 0, pre = 0;
+        while (g1 < ncell) {
+            const int mc = __shfl_sync(kFull, my_m, g1), nc = __shfl_sync(kFull, my_cnt, g1);
+            const int4 bx = make_int4(__shfl_sync(kFull, my_box.x, g1), __shfl_sync(kFull, my_box.y, g1),
+                                      __shfl_sync(kFull, my_box.z, g1), __shfl_sync(kFull, my_box.w, g1));
+            const int used = max(mc, 0);
+            if (soff + used > kSlotPool) break;
+            if (lane == 0) W.ci[g1 - g0] = CellInfo{kbase + g1, mc, soff, pre, bx};
+            soff += used;
+            pre += nc;
+            g1++;
+        }
+        const int ng = g1 - g0, nslot = soff, total = pre;
+        if (lane == 0) W.ci[ng].pre = total;  // sentinel
+        __syncwarp();
+        for (int idx = lane; idx < nslot; idx += 32) {
+            int c = 0;
+            while (c + 1 < ng && W.ci[c + 1].soff <= idx) c++;
+            const CellInfo& C = W.ci[c];
+            const int q = A.nb_lab[(size_t)C.k * kCapSmall + (idx - C.soff)];
+            const SiteD S = A.sites[C.k];
+            const Owner o{S.x, S.y, S.w, C.k};
+            const SiteD Q = A.sites[q];
+            W.slot[idx] = make_slot(q, Q, o);
+            W.nb[idx] = make_nb64(Q, o);
+        }
+        __syncwarp();
+        int f = 0;     // next flat entry
+        int cfin = 0;  // next cell of the group to finish
+        double run[kAcc];
+        for (int q = 0; q < kAcc; q++) run[q] = 0.0;
+        double h0 = 0.0, h1 = 0.0;
+        bool t0 = false, t1 = false;
+        for (;;) {
+            // A: clip 32 entries at a time while a full batch still fits in the list
+            int L = 0;
+            while (f < total && L <= kList - 32) {
+                const int idx = f + lane;
+                bool keep = false, bad = false;
+                int cc = 0, id = -1;
+                Poly<kClipCap> PA, PB;
+                Poly<kClipCap>* P = &PA;
+                if (idx < total) {
+                    while (W.ci[cc + 1].pre <= idx) cc++;
+                    const CellInfo& C = W.ci[cc];
+                    id = mesh.get(C.box, idx - C.pre);
+                    if (id >= 0) {
+                        const SiteD S = A.sites[C.k];
+                        const Owner o{S.x, S.y, S.w, C.k};
+                        Fixed T;
+                        mesh.fixed(id, o, T);
+                        P->n = 3;
+                        for (int e = 0; e < 3; e++) {
+                            P->lab[e] = -1 - e;
+                            P->ux[e] = T.ux[e];
+                            P->uy[e] = T.uy[e];
+                            P->ur[e] = T.ur[e];
+                        }
+                        Poly<kClipCap>* Q = &PB;
+                        const Slot* sl = W.slot + C.soff;
+                        for (int s = 0; s < C.m && P->n > 0; s++) {
+                            if (clip_poly<kClipCap, false>(*P, *Q, s, sl, T, o, A.sites, st, bad)) {
+                                if (bad) break;
+                                Poly<kClipCap>* t = P;
+                                P = Q;
+                                Q = t;
+                            }
+                        }
+                        if (!bad && P->n > kPV) bad = true;
+                        keep = !bad && P->n > 0;
                     }
-                    // every lane took at most one entry of this round
-                    flat += min(32, q1 - base);
-                    if (__any_sync(0xffffffffu, nq == kQ)) drain();
+                }
+                redo |= __reduce_or_sync(kFull, bad ? (1u << (g0 + cc)) : 0u);
+                const unsigned bal = __ballot_sync(kFull, keep);
+                if (keep) {
+                    PieceRec& R = W.rec[L + __popc(bal & ((1u << lane) - 1u))];
+                    R.tri = id;
+                    R.cell = (int8_t)cc;
+                    R.n = (int8_t)P->n;
+                    for (int e = 0; e < P->n; e++) R.lab[e] = (int8_t)P->lab[e];
+                }
+                L += __popc(bal);
+                f += 32;
+            }
+            f = min(f, total);
+            __syncwarp();
+            // B: one piece per lane
+            for (int p = lane; p < L; p += 32) {
+                const PieceRec R = W.rec[p];
+                const CellInfo& C = W.ci[R.cell];
+                const SiteD S = A.sites[C.k];
+                const Owner o{S.x, S.y, S.w, C.k};
+                Fixed T;
+                double c0, gx, gy;
+                mesh.triangle(R.tri, o, T, c0, gx, gy);
+                Acc acc{0, 0, 0, 0, 0, 0, 0};
+                integrate_labels<MOM>(
+                    (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.nb + C.soff, T, c0, gx, gy, acc,
+                    [&](int e, int, double v) { W.hvc[e][p] = v; });
+                W.out[0][p] = acc.mass;
+                W.out[1][p] = acc.second;
+                if (MOM) {
+                    W.out[2 % kAcc][p] = acc.m1x;
+                    W.out[3 % kAcc][p] = acc.m1y;
+                    W.out[4 % kAcc][p] = acc.sxx;
+                    W.out[5 % kAcc][p] = acc.syy;
+                    W.out[6 % kAcc][p] = acc.sxy;
                 }
             }
+            __syncwarp();
+            // C: sums per cell in list order; finish the complete cells
+            int p0 = 0;
+            while (cfin < ng) {
+                const CellInfo& C = W.ci[cfin];
+                const int cend = W.ci[cfin + 1].pre;
+                const bool complete = cend <= f;
+                if (!complete && C.pre >= f) break;
+                int p1 = p0;
+                for (;;) {
+                    const int q = p1 + lane;
+                    const unsigned b = __ballot_sync(kFull, q < L && W.rec[q].cell == cfin);
+                    p1 += __popc(b);
+                    if (b != kFull) break;
+                }
+                for (int q = 0; q < kAcc; q++) {
+                    double v = 0.0;
+                    for (int p = p0 + lane; p < p1; p += 32) v += W.out[q][p];
+                    run[q] += warp_sum(v);
+                }
+                for (int p = p0; p < p1; p++) {
+                    const int n = W.rec[p].n;
+                    for (int e = 0; e < n; e++) {
+                        const int l = W.rec[p].lab[e];
+                        if (l == lane) {
+                            h0 += W.hvc[e][p];
+                            t0 = true;
+                        } else if (l == lane + 32) {
+                            h1 += W.hvc[e][p];
+                            t1 = true;
+                        }
+                    }
+                }
+                p0 = p1;
+                if (!complete) break;
+                if (C.m >= 0) {
+                    if ((redo >> (g0 + cfin)) & 1u) {
+                        if (lane == 0) {
+                            A.redo[atomicAdd(A.nredo, 1)] = C.k;
+                            atomicOr(A.status, ST_POLY_OVERFLOW);
+                        }
+                    } else {
+                        finish_cell<MOM>(A, C, run, h0, h1, t0, t1, W.slot + C.soff, W.nb + C.soff, lane);
+                    }
+                }
+                for (int q = 0; q < kAcc; q++) run[q] = 0.0;
+                h0 = h1 = 0.0;
+                t0 = t1 = false;
+                cfin++;
+            }
+            __syncwarp();
+            if (f >= total) break;
         }
-        drain();
+        g0 = g1;
     }
-    finish_warp<MOM>(A, sh, wib, lane, gi, k, S, acc, m, hv, touched, st);
+    st &= ~(uint32_t)ST_NEED_EXACT;
+    if (st) atomicOr(A.status, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -805,24 +1012,30 @@ void launch_cells_stage1(const CellArgs& a, cudaStream_t s)
     k_cells_stage1<<<(a.n + 127) / 128, 128, 0, s>>>(a);
 }
 
+static unsigned pieces_blocks(int n)
+{
+    const int warps = (n + kWarpCells - 1) / kWarpCells;
+    return (unsigned)((warps + kPieceWarps - 1) / kPieceWarps);
+}
+
 void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s)
 {
     if (a.n <= 0) return;
-    int g = (a.n + kPieceWarps - 1) / kPieceWarps;
+    GridPieces e{m};
     if (mom)
-        k_pieces_grid<true><<<g, 32 * kPieceWarps, 0, s>>>(a, m);
+        k_pieces<true><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else
-        k_pieces_grid<false><<<g, 32 * kPieceWarps, 0, s>>>(a, m);
+        k_pieces<false><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
 }
 
 void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s)
 {
     if (a.n <= 0) return;
-    int g = (a.n + kPieceWarps - 1) / kPieceWarps;
+    TriPieces e{m};
     if (mom)
-        k_pieces_tri<true><<<g, 32 * kPieceWarps, 0, s>>>(a, m);
+        k_pieces<true><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else
-        k_pieces_tri<false><<<g, 32 * kPieceWarps, 0, s>>>(a, m);
+        k_pieces<false><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
 }
 
 void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s)

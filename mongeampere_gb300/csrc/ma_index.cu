@@ -166,7 +166,7 @@ __global__ void k_tree_boxes(const SiteD* sites, int n, const int2* child, const
             b.w = fmax(b.w, cb.w);
         }
         box[nd] = b;
-        // single-precision copy, rounded outwards (only used to order the traversal)
+        // single-precision copy, rounded outwards (traversal order and the pruning test)
         boxf[nd] = make_float4(__double2float_rd(b.x), __double2float_rd(b.y), __double2float_ru(b.z),
                                __double2float_ru(b.w));
         nd = parent[nd];
@@ -205,16 +205,26 @@ __device__ __forceinline__ Mom mom_merge(const Mom& a, const Mom& b)
 
 __device__ __forceinline__ double phi_of(const SiteD& s) { return 0.5 * (s.x * s.x + s.y * s.y - s.w); }
 
+// phi_j - beta . x_j for one site, rounded down
+__device__ __forceinline__ double site_alpha(const SiteD& s, double bx, double by)
+{
+    double v = phi_of(s) - (bx * s.x + by * s.y);
+    return v - 1e-15 * (s.x * s.x + s.y * s.y + fabs(s.w) + fabs(bx * s.x) + fabs(by * s.y));
+}
+
+// Nodes of at most this many sites take the exact offset alpha = min over their
+// sites of phi_j - beta . x_j; larger ones combine their children's bounds, which
+// adds the spread of the child's slope over the child's box.  Propagated through
+// every level that spread compounds to several squared site spacings and lets an
+// order of magnitude more sites through the pruning test; above this size the
+// nodes are far enough from the cells that test them for it not to matter.
+constexpr int kExactAlpha = 64;
+
 // alpha bound contributed by one child for the parent's slope beta
 __device__ __forceinline__ double child_alpha(int c, const SiteD* sites, const double4* box, const double4* ab,
                                               double bx, double by)
 {
-    if (c < 0) {
-        SiteD s = sites[c & 0x7fffffff];
-        double f = phi_of(s);
-        double v = f - (bx * s.x + by * s.y);
-        return v - 1e-15 * (s.x * s.x + s.y * s.y + fabs(s.w) + fabs(bx * s.x) + fabs(by * s.y));
-    }
+    if (c < 0) return site_alpha(sites[c & 0x7fffffff], bx, by);
     double4 a = load_published(&ab[c]);
     if (!(a.x < INFINITY)) return INFINITY;
     double4 b = load_published(&box[c]);
@@ -224,7 +234,7 @@ __device__ __forceinline__ double child_alpha(int c, const SiteD* sites, const d
     return v - 1e-15 * (fabs(a.x) + fabs(mx) + fabs(my));
 }
 
-__global__ void k_tree_bounds(const SiteD* sites, int n, const int2* child, const int* parent,
+__global__ void k_tree_bounds(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
                               const int* leaf_parent, int* flag, const double4* box, Mom* mom, double4* ab)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -255,7 +265,16 @@ __global__ void k_tree_bounds(const SiteD* sites, int n, const int2* child, cons
             bx = (r.syy * r.sxf - r.sxy * r.syf) / det;
             by = (r.sxx * r.syf - r.sxy * r.sxf) / det;
         }
-        double al = fmin(child_alpha(c.x, sites, box, ab, bx, by), child_alpha(c.y, sites, box, ab, bx, by));
+        double al;
+        const int2 rg = range[nd];
+        if (rg.y - rg.x < kExactAlpha) {
+            // small node: the exact minimum over its own sites (a contiguous Morton range)
+            al = INFINITY;
+            for (int q = rg.x; q <= rg.y; q++) al = fmin(al, site_alpha(sites[q], bx, by));
+        } else {
+            // large node: from the children's bounds, widened by the child boxes
+            al = fmin(child_alpha(c.x, sites, box, ab, bx, by), child_alpha(c.y, sites, box, ab, bx, by));
+        }
         if (!(al == al)) al = -INFINITY;  // never prune a node whose bound is not finite
         ab[nd] = make_double4(al, bx, by, 0.0);
         nd = parent[nd];
@@ -331,12 +350,12 @@ void launch_perm_gather(const uint64_t* keys, const double* x, const double* y, 
 
 size_t tree_mom_bytes(int n) { return sizeof(Mom) * (size_t)(n > 1 ? n - 1 : 1); }
 
-void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int* parent, const int* leaf_parent,
-                        int* flag, const double4* box, void* mom, double4* ab, cudaStream_t s)
+void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
+                        const int* leaf_parent, int* flag, const double4* box, void* mom, double4* ab, cudaStream_t s)
 {
     if (n < 2) return;
     cudaMemsetAsync(flag, 0, sizeof(int) * (n - 1), s);
-    k_tree_bounds<<<(n + 255) / 256, 256, 0, s>>>(sites, n, child, parent, leaf_parent, flag, box, (Mom*)mom, ab);
+    k_tree_bounds<<<(n + 255) / 256, 256, 0, s>>>(sites, n, child, range, parent, leaf_parent, flag, box, (Mom*)mom, ab);
 }
 
 }  // namespace ma
