@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--profile-evals", type=int, default=0,
                     help="profiling driver: solve once, then run this many Laguerre evaluations at the "
                          "solution weights and print per-kernel device times (no benchmark line)")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="profiling driver: one solve with per-kernel device times (no benchmark line)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -223,6 +225,15 @@ def main():
             api.kantorovich(dmesh, X, wsol, ctx=ctx)
         torch.cuda.synchronize()
         print(json.dumps({"profile_evals": args.profile_evals, **ctx.profile_read()}))
+        return
+
+    if args.profile_solve:
+        solve_device()
+        ctx.profile(True)
+        _, st = solve_device()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_solve": 1, "cg_iters": st.cg_iters, "newton_iters": st.niter, "evals": st.neval,
+                          "eval_ms": st.t_eval_ms, "linsolve_ms": st.t_linsolve_ms, **ctx.profile_read()}))
         return
 
     for _ in range(args.warmup):

@@ -126,6 +126,11 @@ ma_status ma_kantorovich(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const doub
 ma_status ma_hessian_copy(ma_ctx* ctx, int32_t* rowptr, int32_t* col, double* val, ma_mem mem);
 
 /* ------------------------------------------------------------------ solver */
+typedef enum ma_precond {
+    MA_PRECOND_MULTIGRID = 0, /* one V-cycle of an aggregation multigrid (default) */
+    MA_PRECOND_JACOBI = 1     /* diagonal scaling */
+} ma_precond;
+
 typedef struct ma_solve_opts {
     double eps_g;          /* stop threshold (reference default 1e-7) */
     int64_t maxiter;       /* Newton iterations (reference default 100) */
@@ -135,6 +140,7 @@ typedef struct ma_solve_opts {
     double cg_rtol;        /* relative residual of the preconditioned CG; 0 (default): inexact Newton,
                               min(1e-3, max(1e-12, 0.1 |g| / |g0|)) at each step */
     int64_t cg_maxiter;    /* CG iteration cap (0: default 20000) */
+    int precond;           /* ma_precond: CG preconditioner of the Newton step */
 } ma_solve_opts;
 
 typedef struct ma_stats {

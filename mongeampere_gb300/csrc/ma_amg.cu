@@ -1,0 +1,735 @@
+// ma_amg.cu -- aggregation multigrid preconditioner for the Newton linear solve.
+//
+// The Newton system of solve_laplacian_matrix (include/MA/optimal_transport.hpp:41-87)
+// is the Hessian H (a weighted graph Laplacian of the Laguerre-cell adjacency) with
+// its last row and column removed.  The reference factorises it (SimplicialLLT);
+// here conjugate gradients are preconditioned by one V-cycle of an aggregation
+// multigrid built on the device at every Newton step:
+//
+//   * the fine level is H copied into Morton order (the order of the site index),
+//     so that neighbouring rows are close in memory; every level is then
+//     aggregated the same way, kAggSize consecutive rows per aggregate, which are
+//     spatially compact without any graph search;
+//   * the coarse matrices are Galerkin products P^T A P with the piecewise-constant
+//     prolongation P: a coarse entry (I, J) is the sum of the fine entries (i, j)
+//     with i in I and j in J.  Each coarse row is assembled by one warp, its
+//     duplicates summed in a fixed order (reproducible results);
+//   * smoothing is damped Jacobi (one sweep before, one after), the coarse
+//     correction is scaled by kCoarseScale (piecewise-constant prolongation
+//     underestimates the smooth error), and the coarsest level (at most kCoarsest
+//     nodes) is solved with its dense inverse;
+//   * the whole preconditioned CG -- every level of every V-cycle -- runs in one
+//     cooperative kernel with grid barriers between the phases; no host round trip
+//     per iteration.
+// Rows that are inactive (the gauge row n-1 and empty cells: zero diagonal) are
+// held at zero on every level.
+#include <cooperative_groups.h>
+
+#include "ma_runtime.h"
+
+namespace cg = cooperative_groups;
+
+namespace ma {
+
+constexpr int kAggSize = 4;         // nodes per aggregate, every level (four lanes in the kernels)
+constexpr int kCoarsest = 64;       // dense solve at or below this many nodes
+constexpr int kRowCap = 512;        // gathered entries of one coarse row
+constexpr int kRowWarps = 4;        // coarse rows per block in the setup
+constexpr double kOmega = 2.0 / 3.0;
+constexpr double kCoarseScale = 1.5;
+static_assert(kAggSize == 4, "aggregate sums use two shuffle steps");
+
+// ---------------------------------------------------------------------------
+// setup: coarse rows
+// ---------------------------------------------------------------------------
+struct CoarseSrc {
+    int n;             // fine nodes
+    const int* rp;     // fine CSR
+    const int* ci;
+    const double* va;
+    const double* dinv;  // 0 marks an inactive fine node
+};
+
+// One warp per coarse row: gather the member rows (active columns only) mapped to
+// aggregates, keep the first occurrence of each aggregate, sum its duplicates in
+// gather order, and place it by rank of its column.  FILL = false counts the
+// distinct columns into cnt[I]; FILL = true writes them at rp[I].
+template <bool FILL>
+__global__ void __launch_bounds__(32 * kRowWarps) k_coarse_rows(CoarseSrc s, int nc, int* cnt, const int* rp,
+                                                                 int* ci, double* va, int* overflow)
+{
+    __shared__ int scol[kRowWarps][kRowCap];
+    __shared__ double sval[kRowWarps][kRowCap];
+    __shared__ unsigned char slead[kRowWarps][kRowCap];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int I = blockIdx.x * kRowWarps + wib;
+    if (I >= nc) return;
+    int* col = scol[wib];
+    double* val = sval[wib];
+    unsigned char* lead = slead[wib];
+    int E = 0;
+    bool over = false;
+    for (int q = 0; q < kAggSize && !over; q++) {
+        const int i = I * kAggSize + q;
+        if (i >= s.n) break;
+        if (s.dinv[i] == 0.0) continue;
+        const int k0 = s.rp[i], k1 = s.rp[i + 1];
+        for (int b = k0; b < k1; b += 32) {
+            const int k = b + lane;
+            int c = -1;
+            double v = 0.0;
+            if (k < k1) {
+                const int j = s.ci[k];
+                if (s.dinv[j] != 0.0) {
+                    c = j / kAggSize;
+                    v = s.va[k];
+                }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, c >= 0);
+            const int pos = E + __popc(bal & ((1u << lane) - 1u));
+            if (c >= 0 && pos < kRowCap) {
+                col[pos] = c;
+                val[pos] = v;
+            }
+            E += __popc(bal);
+            if (E > kRowCap) {
+                over = true;
+                break;
+            }
+        }
+    }
+    if (over) {
+        if (lane == 0) {
+            atomicExch(overflow, 1);
+            if (!FILL) cnt[I] = 0;
+        }
+        return;
+    }
+    __syncwarp();
+    int nlead = 0;
+    for (int e = lane; e < E; e += 32) {
+        const int c = col[e];
+        bool first = true;
+        for (int f = 0; f < e; f++)
+            if (col[f] == c) {
+                first = false;
+                break;
+            }
+        lead[e] = first ? 1 : 0;
+        nlead += first ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) nlead += __shfl_xor_sync(0xffffffffu, nlead, o);
+    if (!FILL) {
+        if (lane == 0) cnt[I] = nlead;
+        return;
+    }
+    __syncwarp();
+    const int base = rp[I];
+    for (int e = lane; e < E; e += 32) {
+        if (!lead[e]) continue;
+        const int c = col[e];
+        double sum = 0.0;
+        int rank = 0;
+        for (int f = 0; f < E; f++) {
+            if (col[f] == c && f >= e) sum += val[f];
+            if (lead[f] && col[f] < c) rank++;
+        }
+        ci[base + rank] = c;
+        va[base + rank] = sum;
+    }
+}
+
+// inverse diagonal of a coarse level (0 for rows without a positive diagonal)
+__global__ void k_level_dinv(const int* rp, const int* ci, const double* va, int n, double* dinv)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = 0.0;
+    for (int k = rp[i]; k < rp[i + 1]; k++)
+        if (ci[k] == i) d = va[k];
+    dinv[i] = d > 0.0 ? 1.0 / d : 0.0;
+}
+
+// dense inverse of the coarsest level (n <= kCoarsest, SPD on its active rows;
+// inactive rows become identity rows), Gauss-Jordan in place, one block
+__global__ void __launch_bounds__(256) k_dense_inverse(const int* rp, const int* ci, const double* va,
+                                                       const double* dinv, int n, double* inv)
+{
+    __shared__ double a[kCoarsest][kCoarsest + 1];
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) a[t / n][t % n] = 0.0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        if (dinv[i] == 0.0) {
+            a[i][i] = 1.0;
+            continue;
+        }
+        for (int k = rp[i]; k < rp[i + 1]; k++)
+            if (dinv[ci[k]] != 0.0) a[i][ci[k]] = va[k];
+    }
+    __syncthreads();
+    __shared__ double fcol[kCoarsest];
+    for (int k = 0; k < n; k++) {
+        const double p = 1.0 / a[k][k];
+        // the multipliers of column k, read before any row changes
+        for (int i = threadIdx.x; i < n; i += blockDim.x) fcol[i] = a[i][k];
+        __syncthreads();
+        // row k scaled (with the pivot position replaced by 1 first)
+        for (int j = threadIdx.x; j < n; j += blockDim.x) a[k][j] = (j == k ? 1.0 : a[k][j]) * p;
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int i = t / n, j = t % n;
+            if (i == k) continue;
+            const double f = fcol[i];
+            if (j == k)
+                a[i][j] = -f * a[k][k];
+            else
+                a[i][j] -= f * a[k][j];
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int i = t / n, j = t % n;
+        inv[t] = (dinv[i] == 0.0 || dinv[j] == 0.0) ? 0.0 : a[i][j];
+    }
+}
+
+// the fine level in Morton order: row k is H's row perm[k], columns renumbered
+__global__ void k_inv_perm(const int* perm, int n, int* inv)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) inv[perm[k]] = k;
+}
+
+__global__ void k_fine_count(const int* rp, const int* perm, int n, int* cnt)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) cnt[k] = rp[perm[k] + 1] - rp[perm[k]];
+}
+
+// entries of row k, and its inverse diagonal (0 for the gauge row n-1 and for
+// empty rows)
+__global__ void k_fine_fill(const int* rp, const int* ci, const double* va, const int* perm, const int* inv, int n,
+                            const int* rpm, int* cim, double* vam, double* dinv)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = perm[k];
+    const int k0 = rp[i], k1 = rp[i + 1], base = rpm[k];
+    double d = 0.0;
+    for (int e = k0; e < k1; e++) {
+        const int j = ci[e];
+        if (j == i) d = va[e];
+        cim[base + e - k0] = inv[j];
+        vam[base + e - k0] = va[e];
+    }
+    dinv[k] = (i == n - 1 || !(d > 0.0)) ? 0.0 : 1.0 / d;
+}
+
+// sliced ELL of the Morton-ordered fine level: 32 x (longest row of the slice)
+// entries per slice of 32 rows
+__global__ void k_sell_width(const int* rp, int n, int* cnt)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int len = k < n ? rp[k + 1] - rp[k] : 0;
+    for (int o = 16; o > 0; o >>= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+    if ((k & 31) == 0 && k < n) cnt[k >> 5] = 32 * len;
+}
+
+__global__ void k_sell_fill(const int* rp, const int* ci, const double* va, int n, const int* sp, int* eci,
+                            double* eva)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int b0 = sp[k >> 5] + (k & 31), w = (sp[(k >> 5) + 1] - sp[k >> 5]) >> 5;
+    const int k0 = rp[k], len = rp[k + 1] - k0;
+    for (int e = 0; e < w; e++) {
+        eci[b0 + 32 * e] = e < len ? ci[k0 + e] : k;
+        eva[b0 + 32 * e] = e < len ? va[k0 + e] : 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the multigrid PCG kernel
+// ---------------------------------------------------------------------------
+// Level l >= 1 keeps the restricted residual b_l and the post-smoothed correction
+// xp_l; the pre-smoothed correction omega D^-1 b_l is recomputed where needed.  The
+// fine level runs one thread per row; a coarse level gives each row a team of
+// T = 1 .. 32 adjacent lanes (sized so that the grid covers the level), the lanes
+// striding over the row's entries and summing by shuffles, so that the small levels
+// are not a chain of dependent loads in a few threads.  The four members of a
+// level-l aggregate are consecutive rows of level l, hence one contiguous entry
+// range.  Grid barriers per CG iteration: 2 (nlev - 2) + 3.
+constexpr int kAmgMaxLevels = 16;
+constexpr int kAmgThreads = 256;
+
+struct AmgLevelDev {
+    int n;
+    const int* rp;
+    const int* ci;
+    const double* va;
+    const double* dinv;
+    double* b;   // restricted residual
+    double* xp;  // post-smoothed correction
+    int tr;      // team size restricting this level into the next
+    int tp;      // team size prolonging into this level
+    // level 0 only: the same matrix as sliced ELL, slices of 32 rows stored
+    // entry-major (entry e of row 32 s + r at sp[s] + 32 e + r), padded with
+    // zero entries pointing at the row itself
+    const int* sp;
+    const int* eci;
+    const double* eva;
+};
+
+struct AmgPcgArgs {
+    int nlev;  // levels 0 .. nlev-1; nlev-1 is solved densely
+    AmgLevelDev L[kAmgMaxLevels];  // level 0: H in Morton order
+    const int* perm;  // Morton position -> row of H
+    const double* cinv;
+    const double* b;  // right-hand side, rows of H (component n-1 ignored)
+    double* x;        // solution, rows of H
+    // work vectors in Morton order
+    double* xs;
+    double* r0;  // residual, double-buffered
+    double* r1;
+    double* z;
+    double* p;
+    double* q;
+    double* part;  // 3 * gridDim.x partial sums
+    double* out;   // [iterations, |r|, |b|]
+    double rtol;
+    int maxiter;
+    const int* overflow;  // set by the setup: fall back to Jacobi
+};
+
+__device__ __forceinline__ double amg_block_sum(double v, double* sh)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < kAmgThreads / 32; k++) s += sh[k];
+        sh[32] = s;
+    }
+    __syncthreads();
+    const double s = sh[32];
+    __syncthreads();
+    return s;
+}
+
+__device__ __forceinline__ double amg_grid_total(const double* part, int nb, double* sh)
+{
+    double v = 0.0;
+    for (int k = threadIdx.x; k < nb; k += kAmgThreads) v += part[k];
+    return amg_block_sum(v, sh);
+}
+
+// sum over lanes xor-adjacent below `width` (bitwise identical on all of them)
+__device__ __forceinline__ double team_sum(double v, int width)
+{
+    for (int o = width >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ int round32(int n) { return (n + 31) & ~31; }
+
+// Loop over rows [0, nrows) with teams of T lanes: calls fn(row, lane_in_team)
+// with row < nrows, or row = -1 for lanes without a row in this round (they still
+// take part in the team's shuffles).  Warp-uniform trip count.
+template <class Fn>
+__device__ __forceinline__ void team_rows(int nrows, int T, Fn&& fn)
+{
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nteams = gridDim.x * blockDim.x / T;
+    const int lane = threadIdx.x & 31;
+    const int wteam0 = (tid >> 5) * (32 / T);  // first team of this warp
+    for (int base = wteam0; base < nrows; base += nteams) {
+        const int row = base + lane / T;
+        fn(row < nrows ? row : -1, lane & (T - 1));
+    }
+}
+
+// b_{l+1} from level l >= 1: the residual of the pre-smoothed correction summed
+// over each aggregate, b_{l+1}[J] = sum_{I in J} b_l[I] - omega sum over the
+// member rows' entries a_IK D_K^-1 b_l[K]
+__device__ __forceinline__ void restrict_level(const AmgPcgArgs& a, int l)
+{
+    const AmgLevelDev& A = a.L[l];
+    const AmgLevelDev& C = a.L[l + 1];
+    const int T = A.tr;
+    team_rows(C.n, T, [&](int J, int t) {
+        double s = 0.0;
+        if (J >= 0) {
+            const int I0 = J * kAggSize, I1 = min(I0 + kAggSize, A.n);
+            if (t < I1 - I0) s = A.b[I0 + t];
+            for (int k = A.rp[I0] + t; k < A.rp[I1]; k += T) {
+                const int K = A.ci[k];
+                s -= A.va[k] * (kOmega * A.dinv[K] * A.b[K]);
+            }
+        }
+        s = team_sum(s, T);
+        if (J >= 0 && t == 0) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
+    });
+}
+
+// the coarsest level's solution cinv b, computed by every block into shared memory
+// before the phase that prolongs it
+__device__ __forceinline__ void coarsest_solve(const AmgPcgArgs& a, double* xc)
+{
+    const AmgLevelDev& C = a.L[a.nlev - 1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int r = wid; r < C.n; r += kAmgThreads / 32) {
+        double v = 0.0;
+        for (int k = lane; k < C.n; k += 32) v += a.cinv[r * C.n + k] * C.b[k];
+        v = team_sum(v, 32);
+        if (lane == 0) xc[r] = v;
+    }
+    __syncthreads();
+}
+
+// the coarse correction of aggregate J of level l, i.e. node J of level l+1
+__device__ __forceinline__ double coarse_corr(const AmgPcgArgs& a, int l, int J, const double* xc)
+{
+    return (l + 2 < a.nlev) ? a.L[l + 1].xp[J] : xc[J];
+}
+
+// xp_l for level l >= 1: pre-smoothed plus scaled coarse correction, then one
+// damped Jacobi sweep
+__device__ __forceinline__ void prolong_level(const AmgPcgArgs& a, int l, double* xc)
+{
+    const AmgLevelDev& A = a.L[l];
+    const int T = A.tp;
+    if (l + 2 == a.nlev) coarsest_solve(a, xc);
+    team_rows(A.n, T, [&](int I, int t) {
+        double s = 0.0, yI = 0.0, dI = 0.0;
+        if (I >= 0) {
+            dI = A.dinv[I];
+            if (dI != 0.0) {
+                for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) {
+                    const int K = A.ci[k];
+                    const double dK = A.dinv[K];
+                    const double yK = dK != 0.0 ? kOmega * dK * A.b[K] + kCoarseScale * coarse_corr(a, l, K / kAggSize, xc) : 0.0;
+                    s -= A.va[k] * yK;
+                }
+                if (t == 0) yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, I / kAggSize, xc);
+            }
+        }
+        s = team_sum(s, T);
+        if (I >= 0 && t == 0) A.xp[I] = dI != 0.0 ? yI + kOmega * dI * (A.b[I] + s) : 0.0;
+    });
+}
+
+__global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[40];
+    __shared__ double xc[kCoarsest];
+    const int nb = gridDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    const AmgLevelDev& F = a.L[0];
+    const int n = F.n;
+    const bool jacobi = *a.overflow != 0;
+    // three partial-sum regions, one per reduction of an iteration (rr, rz, pq):
+    // a region is rewritten only after every block has passed the barrier that
+    // follows its last read
+    double* part_rr = a.part;
+    double* part_rz = a.part + nb;
+    double* part_pq = a.part + 2 * nb;
+    double* rc = a.r0;  // current residual
+    double* rn = a.r1;  // next residual
+
+    // x = 0, p = q = 0, r = b (active rows); the first pass below is a CG update
+    // with alpha = 0
+    for (int k = tid; k < n; k += stride) {
+        a.xs[k] = 0.0;
+        a.p[k] = 0.0;
+        a.q[k] = 0.0;
+        rc[k] = F.dinv[k] != 0.0 ? a.b[a.perm[k]] : 0.0;
+    }
+    grid.sync();
+    double alpha = 0.0, rz = 0.0, rr = 0.0, bnorm = 0.0, tol = 0.0;
+    int it = 0;
+    for (;;) {
+        // ---- x += alpha p, r -= alpha q, and the fine restriction ----------------
+        {
+            double l_rr = 0.0;
+            const AmgLevelDev& C = a.L[1];
+            for (int k = tid; k < round32(n); k += stride) {
+                double s = 0.0;
+                if (k < n) {
+                    const double rk = rc[k] - alpha * a.q[k];
+                    a.xs[k] += alpha * a.p[k];
+                    rn[k] = rk;
+                    l_rr += rk * rk;
+                    const double dk = F.dinv[k];
+                    if (!jacobi && dk != 0.0) {
+                        s = rk;
+                        const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
+#pragma unroll 4
+                        for (int e = 0; e < w; e++) {
+                            const int j = F.eci[b0 + 32 * e];
+                            s -= F.eva[b0 + 32 * e] * (kOmega * F.dinv[j] * (rc[j] - alpha * a.q[j]));
+                        }
+                    }
+                }
+                if (!jacobi) {
+                    s = team_sum(s, kAggSize);
+                    const int J = k / kAggSize;
+                    if ((k & (kAggSize - 1)) == 0 && J < C.n) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
+                }
+            }
+            const double t = amg_block_sum(l_rr, sh);
+            if (threadIdx.x == 0) part_rr[blockIdx.x] = t;
+        }
+        grid.sync();
+        {
+            double* t = rc;
+            rc = rn;
+            rn = t;
+        }
+        rr = amg_grid_total(part_rr, nb, sh);
+        if (it == 0) {
+            bnorm = sqrt(rr);
+            tol = a.rtol * bnorm;
+        }
+        if (it >= a.maxiter || !(sqrt(rr) > tol)) break;
+        // ---- z = M r -------------------------------------------------------------
+        double l_rz = 0.0;
+        if (jacobi) {
+            for (int k = tid; k < n; k += stride) {
+                const double zk = F.dinv[k] * rc[k];
+                a.z[k] = zk;
+                l_rz += zk * rc[k];
+            }
+        } else {
+            for (int l = 1; l + 1 < a.nlev; l++) {
+                restrict_level(a, l);
+                grid.sync();
+            }
+            for (int l = a.nlev - 2; l >= 1; l--) {
+                prolong_level(a, l, xc);
+                grid.sync();
+            }
+            if (a.nlev == 2) coarsest_solve(a, xc);
+            for (int k = tid; k < n; k += stride) {
+                const double dk = F.dinv[k];
+                double zk = 0.0;
+                if (dk != 0.0) {
+                    const double yk = kOmega * dk * rc[k] + kCoarseScale * coarse_corr(a, 0, k / kAggSize, xc);
+                    double s = rc[k];
+                    const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
+#pragma unroll 4
+                    for (int e = 0; e < w; e++) {
+                        const int j = F.eci[b0 + 32 * e];
+                        const double dj = F.dinv[j];
+                        const double yj =
+                            dj != 0.0 ? kOmega * dj * rc[j] + kCoarseScale * coarse_corr(a, 0, j / kAggSize, xc)
+                                      : 0.0;
+                        s -= F.eva[b0 + 32 * e] * yj;
+                    }
+                    zk = yk + kOmega * dk * s;
+                }
+                a.z[k] = zk;
+                l_rz += zk * rc[k];
+            }
+        }
+        {
+            const double t = amg_block_sum(l_rz, sh);
+            if (threadIdx.x == 0) part_rz[blockIdx.x] = t;
+        }
+        grid.sync();
+        const double rz_new = amg_grid_total(part_rz, nb, sh);
+        if (!(rz_new > 0.0)) break;
+        const double beta = it == 0 ? 0.0 : rz_new / rz;
+        rz = rz_new;
+        // ---- p = z + beta p, q = A p (= A z + beta q) ------------------------------
+        double l_pq = 0.0;
+        for (int k = tid; k < n; k += stride) {
+            double w = 0.0;
+            if (F.dinv[k] != 0.0) {
+                const int b0 = F.sp[k >> 5] + (k & 31), wd = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
+#pragma unroll 4
+                for (int e = 0; e < wd; e++) w += F.eva[b0 + 32 * e] * a.z[F.eci[b0 + 32 * e]];
+            }
+            const double pk = a.z[k] + beta * a.p[k];
+            const double qk = w + beta * a.q[k];
+            a.p[k] = pk;
+            a.q[k] = qk;
+            l_pq += pk * qk;
+        }
+        {
+            const double t = amg_block_sum(l_pq, sh);
+            if (threadIdx.x == 0) part_pq[blockIdx.x] = t;
+        }
+        grid.sync();
+        const double pq = amg_grid_total(part_pq, nb, sh);
+        if (!(pq > 0.0)) break;
+        alpha = rz / pq;
+        it++;
+    }
+    // the solution back in the rows of H
+    for (int k = tid; k < n; k += stride) a.x[a.perm[k]] = a.xs[k];
+    if (tid == 0) {
+        a.out[0] = (double)it;
+        a.out[1] = sqrt(rr);
+        a.out[2] = bnorm;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int amg_levels(int n)
+{
+    int L = 1;
+    int m = n;
+    while (m > kCoarsest && L < kAmgMaxLevels) {
+        m = (m + kAggSize - 1) / kAggSize;
+        L++;
+    }
+    return L;
+}
+
+// Build the hierarchy for the Hessian in c->rowptr/col/val (n rows) and run the
+// preconditioned CG.  Matrices of level l >= 1 never have more entries than the
+// fine one, so every level is sized by the fine nnz and nothing is read back.
+ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int* iters,
+                        double* relres)
+{
+    cudaStream_t s = c->stream;
+    const int nlev = amg_levels(n);
+    if (nlev < 2 || nlev > kAmgMaxLevels) return MA_ERR_INVALID_ARGUMENT;
+    Amg& G = c->amg;
+    const size_t nnz = (size_t)(c->nnz > 0 ? c->nnz : 1);
+    MA_CUDA(c, c->cg_r.ensure(sizeof(double) * n));
+    MA_CUDA(c, c->cg_z.ensure(sizeof(double) * n));
+    MA_CUDA(c, c->cg_p.ensure(sizeof(double) * n));
+    MA_CUDA(c, c->cg_q.ensure(sizeof(double) * n));
+    MA_CUDA(c, c->cg_dinv.ensure(sizeof(double) * n));
+    MA_CUDA(c, c->cg_scal.ensure(sizeof(double) * 8));
+    MA_CUDA(c, G.r1.ensure(sizeof(double) * n));
+    MA_CUDA(c, G.xs.ensure(sizeof(double) * n));
+    MA_CUDA(c, G.inv.ensure(sizeof(int) * n));
+    MA_CUDA(c, G.cnt.ensure(sizeof(int) * (n + 2)));
+    MA_CUDA(c, G.rp0.ensure(sizeof(int) * (n + 1)));
+    MA_CUDA(c, G.ci0.ensure(sizeof(int) * nnz));
+    MA_CUDA(c, G.va0.ensure(sizeof(double) * nnz));
+    MA_CUDA(c, G.flag.ensure(sizeof(int) * 4));
+    MA_CUDA(c, cudaMemsetAsync(G.flag.p, 0, sizeof(int) * 4, s));
+    const int* perm = c->perm.as<int>();
+    const unsigned g1 = (unsigned)((n + 255) / 256);
+    k_inv_perm<<<g1, 256, 0, s>>>(perm, n, G.inv.as<int>());
+    k_fine_count<<<g1, 256, 0, s>>>(c->rowptr.as<int>(), perm, n, G.cnt.as<int>());
+    launch_scan(G.cnt.as<int>(), G.rp0.as<int>(), n, c->scan_scratch.as<int>(), s);
+    k_fine_fill<<<g1, 256, 0, s>>>(c->rowptr.as<int>(), c->col.as<int>(), c->val.as<double>(), perm,
+                                   G.inv.as<int>(), n, G.rp0.as<int>(), G.ci0.as<int>(), G.va0.as<double>(),
+                                   c->cg_dinv.as<double>());
+    const int nslice = (n + 31) / 32;
+    size_t ell_cap = nnz + 32 * (size_t)nslice * 8;  // grown below if a slice is wider
+    MA_CUDA(c, G.sp.ensure(sizeof(int) * (nslice + 1)));
+    k_sell_width<<<(unsigned)((nslice * 32 + 255) / 256), 256, 0, s>>>(G.rp0.as<int>(), n, G.cnt.as<int>());
+    launch_scan(G.cnt.as<int>(), G.sp.as<int>(), nslice, c->scan_scratch.as<int>(), s);
+    {
+        int total = 0;
+        MA_CUDA(c, cudaMemcpyAsync(&total, G.sp.as<int>() + nslice, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MA_CUDA(c, cudaStreamSynchronize(s));
+        if ((size_t)total > ell_cap) ell_cap = (size_t)total;
+    }
+    MA_CUDA(c, G.eci.ensure(sizeof(int) * ell_cap));
+    MA_CUDA(c, G.eva.ensure(sizeof(double) * ell_cap));
+    k_sell_fill<<<g1, 256, 0, s>>>(G.rp0.as<int>(), G.ci0.as<int>(), G.va0.as<double>(), n, G.sp.as<int>(),
+                                   G.eci.as<int>(), G.eva.as<double>());
+    c->launches += 9;
+
+    AmgPcgArgs a{};
+    a.nlev = nlev;
+    a.L[0] = AmgLevelDev{n,       G.rp0.as<int>(), G.ci0.as<int>(), G.va0.as<double>(), c->cg_dinv.as<double>(),
+                         nullptr, nullptr,         1,               1,                 G.sp.as<int>(),
+                         G.eci.as<int>(), G.eva.as<double>()};
+    int nl = n;
+    for (int l = 1; l < nlev; l++) {
+        const int nc = (nl + kAggSize - 1) / kAggSize;
+        AmgBuf& B = G.lev[l];
+        MA_CUDA(c, B.rp.ensure(sizeof(int) * (nc + 1)));
+        MA_CUDA(c, B.ci.ensure(sizeof(int) * nnz));
+        MA_CUDA(c, B.va.ensure(sizeof(double) * nnz));
+        MA_CUDA(c, B.dinv.ensure(sizeof(double) * nc));
+        MA_CUDA(c, B.b.ensure(sizeof(double) * nc));
+        MA_CUDA(c, B.xp.ensure(sizeof(double) * nc));
+        const AmgLevelDev& A = a.L[l - 1];
+        CoarseSrc src{nl, A.rp, A.ci, A.va, A.dinv};
+        const unsigned g = (unsigned)((nc + kRowWarps - 1) / kRowWarps);
+        k_coarse_rows<false><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), nullptr, nullptr, nullptr,
+                                                           G.flag.as<int>());
+        launch_scan(G.cnt.as<int>(), B.rp.as<int>(), nc, c->scan_scratch.as<int>(), s);
+        k_coarse_rows<true><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), B.rp.as<int>(), B.ci.as<int>(),
+                                                          B.va.as<double>(), G.flag.as<int>());
+        k_level_dinv<<<(nc + 255) / 256, 256, 0, s>>>(B.rp.as<int>(), B.ci.as<int>(), B.va.as<double>(), nc,
+                                                      B.dinv.as<double>());
+        c->launches += 5;
+        a.L[l] = AmgLevelDev{nc, B.rp.as<int>(), B.ci.as<int>(), B.va.as<double>(), B.dinv.as<double>(),
+                             B.b.as<double>(), B.xp.as<double>(), 1, 1, nullptr, nullptr, nullptr};
+        nl = nc;
+    }
+    const AmgLevelDev& C = a.L[nlev - 1];
+    MA_CUDA(c, G.cinv.ensure(sizeof(double) * kCoarsest * kCoarsest));
+    k_dense_inverse<<<1, 256, 0, s>>>(C.rp, C.ci, C.va, C.dinv, C.n, G.cinv.as<double>());
+    c->launches += 1;
+
+    // the co-resident grid, at most kBlocksPerSm blocks per SM: every grid barrier
+    // waits for all blocks, and the coarse levels' teams want the lanes
+    constexpr int kBlocksPerSm = 4;
+    static int max_blocks = 0;
+    if (max_blocks == 0) {
+        int per_sm = 0, sms = 0;
+        MA_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_amg, kAmgThreads, 0));
+        MA_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+        max_blocks = (per_sm < kBlocksPerSm ? per_sm : kBlocksPerSm) * sms;
+    }
+    int want = (n + kAmgThreads / 4 - 1) / (kAmgThreads / 4);
+    int nb = want < max_blocks ? want : max_blocks;
+    if (nb < 1) nb = 1;
+    MA_CUDA(c, c->cg_part.ensure(sizeof(double) * 3 * nb));
+    // lanes per coarse row: enough teams to cover the level with the launched grid
+    const int threads = nb * kAmgThreads;
+    auto team = [&](int rows) {
+        int t = 1;
+        while (t < 32 && (int64_t)rows * t * 2 <= threads) t <<= 1;
+        return t;
+    };
+    for (int l = 1; l < nlev; l++) {
+        a.L[l].tp = team(a.L[l].n);
+        if (l + 1 < nlev) a.L[l].tr = team(a.L[l + 1].n);
+    }
+    a.perm = perm;
+    a.cinv = G.cinv.as<double>();
+    a.b = b;
+    a.x = x;
+    a.xs = G.xs.as<double>();
+    a.r0 = c->cg_r.as<double>();
+    a.r1 = G.r1.as<double>();
+    a.z = c->cg_z.as<double>();
+    a.p = c->cg_p.as<double>();
+    a.q = c->cg_q.as<double>();
+    a.part = c->cg_part.as<double>();
+    a.out = c->cg_scal.as<double>();
+    a.rtol = rtol;
+    a.maxiter = maxiter;
+    a.overflow = G.flag.as<int>();
+    void* args[] = {&a};
+    {
+        ProfScope ps(c, &c->profile.pcg_ms, &c->profile.pcg_launches);
+        MA_CUDA(c, cudaLaunchCooperativeKernel((void*)k_pcg_amg, dim3(nb), dim3(kAmgThreads), args, 0, s));
+    }
+    c->launches += 1;
+    MA_CUDA(c, cudaMemcpyAsync(c->hstat + 8, c->cg_scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaStreamSynchronize(s));
+    if (iters) *iters = (int)c->hstat[8];
+    c->profile.pcg_iters += (int64_t)c->hstat[8];
+    if (relres) *relres = c->hstat[10] > 0 ? c->hstat[9] / c->hstat[10] : 0.0;
+    return MA_OK;
+}
+
+}  // namespace ma

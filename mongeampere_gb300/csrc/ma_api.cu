@@ -374,6 +374,13 @@ void ma_ctx_destroy(ma_ctx* c)
                       &c->stat_partial, &c->stat_out, &c->info, &c->big_index, &c->big_col, &c->big_val, &c->big_work, &c->wcur, &c->w0, &c->dirn, &c->g, &c->cg_r,
                       &c->cg_z, &c->cg_p, &c->cg_q, &c->cg_dinv, &c->cg_scal, &c->cg_part};
     for (DevBuf* b : bufs) b->release();
+    for (AmgBuf& l : c->amg.lev) {
+        DevBuf* lb[] = {&l.rp, &l.ci, &l.va, &l.dinv, &l.b, &l.xp};
+        for (DevBuf* b : lb) b->release();
+    }
+    DevBuf* ab[] = {&c->amg.r1, &c->amg.xs, &c->amg.inv, &c->amg.cnt, &c->amg.rp0, &c->amg.ci0, &c->amg.va0, &c->amg.sp, &c->amg.eci, &c->amg.eva,
+                    &c->amg.flag, &c->amg.cinv};
+    for (DevBuf* b : ab) b->release();
     if (c->pev[0]) cudaEventDestroy(c->pev[0]);
     if (c->pev[1]) cudaEventDestroy(c->pev[1]);
     if (c->hstat) cudaFreeHost(c->hstat);

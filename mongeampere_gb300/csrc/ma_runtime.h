@@ -59,6 +59,15 @@ struct Mesh {
     MeshTriDev tri_dev() const;
 };
 
+// aggregation multigrid hierarchy (levels 1.. of the Newton system)
+struct AmgBuf {
+    DevBuf rp, ci, va, dinv, b, xp;
+};
+struct Amg {
+    AmgBuf lev[16];
+    DevBuf r1, xs, inv, cnt, rp0, ci0, va0, sp, eci, eva, flag, cinv;
+};
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -84,6 +93,7 @@ struct Ctx {
     bool have_h = false;
     // solver work vectors
     DevBuf wcur, w0, dirn, g, cg_r, cg_z, cg_p, cg_q, cg_dinv, cg_scal, cg_part;
+    Amg amg;
     // profiling (CUDA events around the main kernels)
     bool prof = false;
     ma_profile profile{};
@@ -111,6 +121,10 @@ struct EvalFlags {
     const double* nu = nullptr;  // when given, stat_out[0] = value - <nu, w>
 };
 ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlags& f);
+// Newton linear solve H[:n-1,:n-1] x = b with the multigrid-preconditioned CG (ma_amg.cu)
+int amg_levels(int n);
+ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int* iters,
+                        double* relres);
 
 // bracket an enqueue with profiling events; the elapsed time is added after a sync
 struct ProfScope {

@@ -4,8 +4,9 @@
 //   * f(w) = kantorovich(w) - <nu, w>, gradient m(w) - nu, Hessian H(w);
 //   * eps0 = min(min m(w0), min nu) / 2; a non-positive eps0 is MA_EMPTY_CELL (:137-148);
 //   * Newton direction of solve_laplacian_matrix (:41-87): H with its last row and
-//     column removed, d[n-1] = 0 -- here by Jacobi-preconditioned conjugate
-//     gradients in one cooperative kernel (no host round trip per iteration);
+//     column removed, d[n-1] = 0 -- here by conjugate gradients in one cooperative
+//     kernel (no host round trip per iteration), preconditioned by an aggregation
+//     multigrid V-cycle (ma_amg.cu) or by the diagonal;
 //   * backtracking: accept w0 + a d when min m >= eps0 and |g| <= (1 - a/2) |g0|,
 //     else halve a (:158-176), bounded at a = 2^-40;
 //   * stop when |g|_2 < eps_g (:150), or max_i |g_i| / nu_i <= eps_g.
@@ -197,8 +198,10 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs a)
 
 // solve H[:n-1,:n-1] x = b (b, x device vectors of length n; x[n-1] = 0)
 static ma_status pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int* iters,
-                           double* relres)
+                           double* relres, int precond)
 {
+    if (precond == MA_PRECOND_MULTIGRID && amg_levels(n) >= 2)
+        return amg_pcg_solve(c, n, b, x, rtol, maxiter, iters, relres);
     cudaStream_t s = c->stream;
     MA_CUDA(c, c->cg_r.ensure(sizeof(double) * n));
     MA_CUDA(c, c->cg_z.ensure(sizeof(double) * n));
@@ -373,6 +376,7 @@ void ma_solve_opts_default(ma_solve_opts* o)
     o->verbose = 0;
     o->cg_rtol = 0.0;  // adaptive forcing
     o->cg_maxiter = 20000;
+    o->precond = MA_PRECOND_MULTIGRID;
 }
 
 ma_status ma_laplacian_solve(ma_ctx* cp, const double* g, double* d, ma_mem mem, double rtol, int64_t maxiter,
@@ -393,7 +397,8 @@ ma_status ma_laplacian_solve(ma_ctx* cp, const double* g, double* d, ma_mem mem,
     double* dd = (mem == MA_MEM_HOST) ? c->dirn.as<double>() : d;
     int it = 0;
     double rr = 0;
-    ma_status st = pcg_solve(c, n, dg, dd, rtol > 0 ? rtol : 1e-10, maxiter > 0 ? (int)maxiter : 20000, &it, &rr);
+    ma_status st = pcg_solve(c, n, dg, dd, rtol > 0 ? rtol : 1e-10, maxiter > 0 ? (int)maxiter : 20000, &it, &rr,
+                             MA_PRECOND_MULTIGRID);
     if (st != MA_OK) return st;
     if (mem == MA_MEM_HOST) {
         MA_CUDA(c, cudaMemcpyAsync(d, dd, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
@@ -501,7 +506,7 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
             // inexact Newton: the linear solve only needs to beat the current residual
             double rtol = adaptive ? std::fmin(1e-3, std::fmax(1e-12, 0.1 * gn / g0)) : o.cg_rtol;
             if ((st = pcg_solve(c, n, c->g.as<double>(), c->dirn.as<double>(), rtol, (int)o.cg_maxiter, &it,
-                                &rr)) != MA_OK) {
+                                &rr, o.precond)) != MA_OK) {
                 result = st;
                 break;
             }

@@ -79,3 +79,41 @@ def test_warm_start(ctx):
     st2 = api.Statistics()
     api.ot_solve(p.mesh, np.c_[p.x, p.y], p.nu, x=w, eps_g=1e-9, stop="rel", stats=st2, ctx=ctx)
     assert st2.niter == 0 and st2.neval == 1
+
+
+def test_multigrid_and_jacobi_solves_agree(ctx):
+    # the aggregation-multigrid preconditioner changes the CG iterations, not the
+    # Newton iterates' limit: both reach the same weights
+    from mongeampere_gb300 import api
+    p = W.make_problem(128, 20000, "gauss", "uniform", "random", seed=7)
+    X = np.c_[p.x, p.y]
+    st_mg, st_j = api.Statistics(), api.Statistics()
+    w_mg = api.ot_solve(p.mesh, X, p.nu, eps_g=1e-10, stop="rel", stats=st_mg, precond="multigrid", ctx=ctx)
+    w_j = api.ot_solve(p.mesh, X, p.nu, eps_g=1e-10, stop="rel", stats=st_j, precond="jacobi", ctx=ctx)
+    assert st_mg.max_rel_err <= 1e-10 and st_j.max_rel_err <= 1e-10
+    np.testing.assert_allclose(w_mg, w_j, rtol=0, atol=1e-9 * np.abs(w_j).max())
+    # five multigrid levels here; far fewer CG iterations per Newton step
+    assert st_mg.cg_iters * 4 < st_j.cg_iters
+
+
+def test_multigrid_laplacian_solve_with_empty_cells(ctx, oracle):
+    # empty cells give zero rows; they stay at zero on every level and the
+    # remaining system is solved as the direct solve of its active part
+    from mongeampere_gb300 import api
+    p = W.make_problem(40, 3000, seed=4)
+    x, y = p.x.copy(), p.y.copy()
+    w = np.zeros(p.n)
+    w[:3000:97] = -0.05  # sites that lose their cells entirely
+    v, g, h = api.kantorovich(p.mesh, np.c_[x, y], w, ctx=ctx)
+    g = np.asarray(g)
+    empty = g == 0
+    assert empty.sum() >= 10 and not empty[-1]
+    rhs = g - p.nu
+    d, it = api.solve_laplacian_matrix(rhs, rtol=1e-13, ctx=ctx)
+    H = h.to_scipy().tocsr()
+    act = np.flatnonzero(~empty[:-1])
+    import scipy.sparse.linalg as spla
+    d_ref = np.zeros(p.n)
+    d_ref[act] = spla.spsolve(H[act][:, act].tocsc(), rhs[act])
+    assert np.all(d[empty] == 0.0) and d[-1] == 0.0
+    np.testing.assert_allclose(d, d_ref, rtol=0, atol=1e-9 * np.abs(d_ref).max())
