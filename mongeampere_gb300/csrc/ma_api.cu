@@ -229,6 +229,13 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     a.scratch = nullptr;
     a.prev_valid = c->prev_valid ? 1 : 0;
     a.counters = nullptr;
+    a.abort_flag = nullptr;
+    c->aborted = false;
+    if (f.abort_on_empty) {
+        MA_CUDA(c, c->abortf.ensure(sizeof(int) * 4));
+        MA_CUDA(c, cudaMemsetAsync(c->abortf.p, 0, sizeof(int), s));
+        a.abort_flag = c->abortf.as<int>();
+    }
     if (c->prof) {
         MA_CUDA(c, c->counters.ensure(8 * sizeof(unsigned long long)));
         MA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), s));
@@ -244,11 +251,21 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     launch_cells(c, m, a, 0, f.moments > 0);
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    c->hinfo[3] = 0;
+    if (a.abort_flag)
+        MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 3, a.abort_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaStreamSynchronize(s));
+    if (c->hinfo[3]) {
+        // a line-search trial with an empty cell: nothing else is computed
+        c->aborted = true;
+        c->have_h = false;
+        return MA_OK;
+    }
     int nredo = c->hinfo[0];
     if (nredo > 0) {
         // sites whose cell outgrew the small capacity: redo them with the large one
         CellArgs b = a;
+        b.abort_flag = nullptr;  // every redone cell must complete: its mass is used
         b.work = c->redo.as<int>();
         b.nwork = nredo;
         MA_CUDA(c, c->fill.ensure(sizeof(int) * ((size_t)n + 4)));
@@ -366,7 +383,7 @@ void ma_ctx_destroy(ma_ctx* c)
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
+    DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->abortf, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
                       &c->perm, &c->sites, &c->posf, &c->scan_scratch, &c->fill, &c->t_child, &c->t_range,
                       &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab,
                       &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,

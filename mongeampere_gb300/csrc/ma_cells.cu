@@ -250,6 +250,7 @@ constexpr int kSeedCap = kCapSmall;  // neighbour-list stride between the stages
 struct CellOut {
     bool overflow;
     bool empty;
+    bool aborted;  // another cell was found empty and the evaluation is abandoned
     uint32_t st;
     int ns;  // neighbour slots after compaction
     int popped, tested, pruned, visited, cuts;
@@ -259,7 +260,7 @@ template <int CAP, bool EXACT>
 __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Owner& o, Slot* slots, int* map,
                               Poly<CAP>*& P, Poly<CAP>*& Q)
 {
-    CellOut r{false, false, 0u, 0, 0, 0, 0, 0, 0};
+    CellOut r{false, false, false, 0u, 0, 0, 0, 0, 0, 0};
     const int gi = A.perm[k];
     Fixed box;
     box.n = 4;
@@ -354,6 +355,10 @@ __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Ow
             if (!visit(seeds[s])) r.empty = true;
     }
     while (sp > 0 && !r.empty && !r.overflow) {
+        if (A.abort_flag && (r.popped & 7) == 0 && *(volatile const int*)A.abort_flag) {
+            r.aborted = true;
+            break;
+        }
         int nd = stack[--sp];
         r.popped++;
         if (nd < 0) {
@@ -389,7 +394,11 @@ __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Ow
             stack[sp++] = ch.y;
         }
     }
-    if (r.empty) P->n = 0;
+    if (r.empty) {
+        P->n = 0;
+        if (A.abort_flag) atomicExch(A.abort_flag, 1);
+    }
+    if (r.aborted) return r;
     if (!r.empty && !r.overflow && P->n > 0) compact_slots(*P, slots, map, ns);
     r.ns = ns;
     return r;
@@ -581,6 +590,7 @@ __global__ void __launch_bounds__(128) k_cells_stage1(CellArgs A)
     Poly<kCapSmall>* P = &W.PA;
     Poly<kCapSmall>* Q = &W.PB;
     CellOut c = cell_stage<kCapSmall, false>(A, k, S, o, W.slots, W.map, P, Q);
+    if (c.aborted) return;
     if (c.st) atomicOr(A.status, c.st & ~ST_NEED_EXACT);
     if (A.counters) {
         atomicAdd(&A.counters[0], (unsigned long long)c.popped);
@@ -807,6 +817,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
     PieceWarp<MOM>& W = shw[wib];
     const int kbase = (blockIdx.x * kPieceWarps + wib) * kWarpCells;
     if (kbase >= A.n) return;
+    if (A.abort_flag && *(volatile const int*)A.abort_flag) return;
     const int ncell = min(kWarpCells, A.n - kbase);
     // lane c sets up cell c
     int my_m = -2, my_cnt = 0;

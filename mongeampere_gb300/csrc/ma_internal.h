@@ -70,6 +70,7 @@ struct CellArgs {
     int* nb_lab;             // stage 1 -> 2: neighbour sorted indices, stage1_cap() per site
     double4* cell_box;       // stage 1 -> 2: absolute bounding box of the cell
     unsigned long long* counters;  // optional stage-1 search counters (6)
+    int* abort_flag;         // optional: set at the first empty cell, and every cell then stops
     void* scratch;           // large-capacity pass: one workspace per work item
     int* big_index;          // per site: row slot in the side buffer, -1 otherwise
     int* big_col;

@@ -87,6 +87,8 @@ struct Ctx {
     DevBuf big_index, big_col, big_val, big_work;  // large-capacity pass
     DevBuf nb_cnt, nb_lab, cell_box;               // stage 1 -> stage 2
     bool prev_valid = false;                       // nb_cnt/nb_lab match the current site index
+    DevBuf abortf;                                 // empty-cell flag of a line-search trial
+    bool aborted = false;                          // the last evaluation stopped at an empty cell
     DevBuf counters;                               // stage-1 search counters (profiling)
     DevBuf info;  // status, nredo, nnz
     int64_t nnz = 0;
@@ -119,6 +121,10 @@ struct EvalFlags {
     bool hessian = true;
     int moments = 0;  // 0 none, 1 first, 2 second
     const double* nu = nullptr;  // when given, stat_out[0] = value - <nu, w>
+    // Newton line-search trial: an empty cell already rejects the trial (its mass 0
+    // is below eps0 > 0), so the evaluation stops at the first one and sets
+    // Ctx::aborted instead of computing the rest
+    bool abort_on_empty = false;
 };
 ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlags& f);
 // Newton linear solve H[:n-1,:n-1] x = b with the multigrid-preconditioned CG (ma_amg.cu)

@@ -449,15 +449,24 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    auto timed_eval = [&](const double* wv) -> ma_status {
+    auto timed_eval = [&](const double* wv, bool trial) -> ma_status {
         cudaEventRecord(e0, s);
         EvalFlags f;
         f.hessian = true;
         f.nu = dnu;
+        f.abort_on_empty = trial;
         ma_status r = run_eval(c, m, n, wv, f);
         if (r != MA_OK) return r;
         cudaEventRecord(e1, s);
-        MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->stat_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (c->aborted) {
+            // value, -, min mass, |g|, max rel: the trial is rejected on its min mass
+            c->hstat[0] = NAN;
+            c->hstat[2] = 0.0;
+            c->hstat[3] = INFINITY;
+            c->hstat[4] = INFINITY;
+        } else {
+            MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->stat_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
         MA_CUDA(c, cudaStreamSynchronize(s));
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
@@ -474,7 +483,7 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     k_min_nu<<<1, 256, 0, s>>>(dnu, n, c->cg_scal.as<double>() + 7);
     c->launches += 1;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat + 15, c->cg_scal.as<double>() + 7, sizeof(double), cudaMemcpyDeviceToHost, s));
-    if ((st = timed_eval(w)) != MA_OK) {
+    if ((st = timed_eval(w, false)) != MA_OK) {
         result = st;
         goto done;
     }
@@ -523,7 +532,7 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
                 // w = w0 - alpha * solution
                 k_axpy_to<<<(n + 255) / 256, 256, 0, s>>>(c->w0.as<double>(), c->dirn.as<double>(), -alpha, n, w);
                 c->launches += 1;
-                if ((st = timed_eval(w)) != MA_OK) {
+                if ((st = timed_eval(w, true)) != MA_OK) {
                     result = st;
                     break;
                 }
