@@ -270,36 +270,56 @@ def main():
         t_dev = float(tt.item())
     value = args.steps * world / t_dev
     ms_per_step = 1e3 * t_dev / args.steps
-    neval = sum(s.neval for s in stats)
-    t_eval = sum(s.t_eval_ms for s in stats) / 1e3
-    evals_per_s = neval / t_eval if t_eval > 0 else None
     for s in stats:
         assert s.max_rel_err <= p.tol_rel, "solve did not converge"
 
-    # ---- dominant kernel: live per-launch duration (profiled run, untimed) ----
+    # ---- full Laguerre evaluations and the dominant kernel ----------------------
+    # evaluations/s: complete evaluations (masses, value, Hessian in CSR) at the
+    # solution weights through the public call (which also rebuilds the site index);
+    # the solve's own count includes line-search trials that stop at an empty cell
+    wsol, _ = solve_device()
+    X = torch.stack([x, y], 1)
+    api.kantorovich(dmesh, X, wsol, ctx=ctx)
+    n_full = 10
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(n_full):
+        _, _, h = api.kantorovich(dmesh, X, wsol, ctx=ctx)
+    e1.record()
+    torch.cuda.synchronize()
+    evals_per_s = n_full / (e0.elapsed_time(e1) * 1e-3)
+    nnz = int(h.col.shape[0])
+    # live per-launch durations of the evaluation kernels (CUDA events on the
+    # context's stream, profiled run, untimed)
     ctx.profile(True)
-    _, stp = solve_device()
+    for _ in range(n_full):
+        api.kantorovich(dmesh, X, wsol, ctx=ctx)
     torch.cuda.synchronize()
     prof = ctx.profile_read()
     ctx.profile(False)
-    _, _, h = api.kantorovich(dmesh, torch.stack([x, y], 1), torch.zeros(p.n, dtype=torch.float64, device=dev),
-                              ctx=ctx)
-    nnz = int(h.col.shape[0])
-    cells_ms = prof["cells_ms"] / max(prof["cells_launches"], 1)
+    pieces_ms = prof["pieces_ms"] / max(prof["pieces_launches"], 1)
+    stage1_ms = prof["cells_ms"] / max(prof["cells_launches"], 1)
+    bounds_ms = prof["bounds_ms"] / max(prof["bounds_launches"], 1)
     bytes_eval = eval_bytes(p.n, nnz, p.mesh.nv)
     peak, peak_kind = measured_peaks()
-    achieved = bytes_eval / (cells_ms * 1e-3) / 1e9
+    achieved = bytes_eval / (pieces_ms * 1e-3) / 1e9
+    # DRAM bytes (read + write) of one k_pieces launch from the ncu capture summarised
+    # in profiles/k_pieces_c2_full.md, for this workload
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    tfile = os.path.join(ROOT, "profiles", "traffic.txt")
     if os.path.exists(tfile):
         with open(tfile) as fh:
-            tj = json.load(fh)
-        if "cells_bytes_per_site" in tj:
-            traffic = tj["cells_bytes_per_site"] * p.n
+            for ln in fh:
+                f = ln.split()
+                if len(f) == 2 and f[0] == "k_pieces_c2_dram_bytes_per_launch":
+                    traffic = float(f[1])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "k_cells_small (Laguerre cell + triangle clip + integrals)",
+                "traffic": traffic,
+                "kernel": "k_pieces (triangle clipping + FP64 integrals + Hessian rows of one evaluation)",
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_eval,
-                "avg_launch_ms": cells_ms}
+                "avg_launch_ms": pieces_ms,
+                "other_eval_kernels_ms": {"k_cells_stage1": stage1_ms, "k_tree_bounds": bounds_ms}}
 
     # ---- e2e through the C ABI with host buffers ----
     xh = torch.tensor(p.x).pin_memory().numpy()
