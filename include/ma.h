@@ -13,6 +13,8 @@
  *   ma_lloyd           MA::lloyd                      include/MA/lloyd.hpp:126-144
  *   ma_pieces          MA::voronoi_triangulation_intersection
  *                                                     include/MA/voronoi_triangulation_intersection.hpp:315-343
+ *   ma_kantorovich_vjp no counterpart in the reference: the adjoint of ma_kantorovich
+ *                      and ma_moments (vector-Jacobian product)
  *   ma_mesh_create_*   the density: a triangulation plus one linear function per
  *                      face (include/MA/functions.hpp:55-120,
  *                      include/CGAL/Triangulation_incremental_builder_2.h:27-80)
@@ -109,6 +111,11 @@ ma_status ma_mesh_create_grid(ma_ctx* ctx, int nx, int ny, const double* gx, con
 /* Explicit triangulation (nv vertices, nt counter-clockwise triangles).  Host arrays. */
 ma_status ma_mesh_create_triangles(ma_ctx* ctx, int nv, const double* vx, const double* vy,
                                    const double* values, int nt, const int32_t* tri, ma_mesh** out);
+/* New vertex values for an existing mesh (same geometry): values[nx*ny] for a grid,
+ * values[nv] for a triangle mesh, in host or device memory.  The density is a
+ * differentiable input of ma_kantorovich_vjp; this updates it without rebuilding the
+ * mesh's bins. */
+ma_status ma_mesh_set_values(ma_ctx* ctx, ma_mesh* mesh, const double* values, ma_mem mem);
 void ma_mesh_destroy(ma_mesh* mesh);
 /* Integral of the density (the value image_to_pl_function returns, functions.hpp:116-119). */
 ma_status ma_mesh_total_mass(const ma_mesh* mesh, double* out);
@@ -185,6 +192,28 @@ ma_status ma_laplacian_solve(ma_ctx* ctx, const double* g, double* d, ma_mem mem
 ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
                                     const double* g, double* d, double rtol, int64_t maxiter, int64_t* iters,
                                     void* stream);
+
+/* ----------------------------------------------------------------- adjoint */
+/* Vector-Jacobian product of (value, mass[n], first[2n]) -- the Kantorovich value
+ * sum_i (w_i m_i - int_{cell i} rho |x - x_i|^2), the cell masses and the first
+ * moments int_{cell i} rho x of ma_moments -- with respect to the site positions,
+ * the weights and the density's vertex values.  No counterpart in the reference (it
+ * has no derivatives beyond the Hessian in w); this is for gradient-based callers
+ * (W2 gradient flows, Lloyd-type descent, learning pipelines) that differentiate
+ * through the transport.
+ *   cot_value           cotangent of the value
+ *   cot_mass[n]         cotangents of the masses (NULL: zero)
+ *   cot_first[2n]       cotangents of the first moments, (x, y) per site (NULL: zero)
+ *   grad_x, grad_y, grad_w [n]  receive the gradients with respect to the sites and weights
+ *   grad_rho            receives the gradient with respect to the mesh's vertex values
+ *                       (grid: nx * ny, row-major like the values; triangles: nv), or NULL
+ * Cells with more than 48 neighbours, or whose pieces need exact predicates, are not
+ * handled (MA_ERR_CAPACITY).  grad_rho is accumulated with atomics: its last bits may
+ * differ from run to run; the other gradients are reproducible. */
+ma_status ma_kantorovich_vjp(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
+                             const double* w, ma_mem mem, double cot_value, const double* cot_mass,
+                             const double* cot_first, double* grad_x, double* grad_y, double* grad_w,
+                             double* grad_rho);
 
 /* --------------------------------------------------------- moments / Lloyd */
 /* mass[n]; first[2n] = (int rho x, int rho y) per site; second[3n] (nullable) =

@@ -10,7 +10,9 @@ Names and argument meaning follow MongeAmpere++:
 * :func:`first_moment`, :func:`second_moment`, :func:`lloyd` --
   include/MA/lloyd.hpp:30-144;
 * :func:`solve_laplacian_matrix` -- include/MA/optimal_transport.hpp:41-87, for the
-  Hessian of the last evaluation on the context.
+  Hessian of the last evaluation on the context;
+* :func:`kantorovich_vjp` -- the adjoint (no counterpart in the reference), wrapped for
+  torch by :mod:`mongeampere_gb300.autograd`.
 
 ``X`` is an ``(N, 2)`` array (or a pair ``(x, y)``).  Arrays may be numpy arrays
 (host memory) or CUDA torch tensors (device memory, used in place).
@@ -114,6 +116,12 @@ class DeviceMesh:
             raise TypeError("mesh must be a GridMesh or a TriMesh")
         _check(lib, ctx.h, st, "ma_mesh_create")
         self.h = h
+
+    def set_values(self, values):
+        """New vertex values for the same geometry (``ma_mesh_set_values``)."""
+        a = _Args(values.reshape(-1) if hasattr(values, "reshape") else values)
+        _check(self.ctx.lib, self.ctx.h, self.ctx.lib.ma_mesh_set_values(self.ctx.h, self.h, a.ptrs[0], a.mem),
+               "ma_mesh_set_values")
 
     def close(self):
         if getattr(self, "h", None):
@@ -228,6 +236,37 @@ def kantorovich(mesh, X, weights, y=None, *, precision: str = "fp64", hessian: b
     if hessian:
         h = hessian_copy(ctx, n, int(nnz.value))
     return val.value, g, h
+
+
+def kantorovich_vjp(mesh, X, weights, cot_value: float = 0.0, cot_mass=None, cot_first=None, y=None, *,
+                    grad_rho: bool = True, ctx: Context | None = None):
+    """Adjoint of ``(value, masses, first moments)`` (``ma_kantorovich_vjp``; no
+    counterpart in the reference).  ``cot_first`` is ``(N, 2)``.  Returns
+    ``(grad_X (N, 2), grad_w (N,), grad_rho (V,) or None)`` where ``grad_rho`` is per
+    mesh vertex (row-major ``ny x nx`` for a grid)."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    x, yy = _split_xy(X, y)
+    cf = None
+    if cot_first is not None:
+        cf = cot_first.reshape(-1) if hasattr(cot_first, "reshape") else np.asarray(cot_first).reshape(-1)
+    a = _Args(x, yy, weights, cot_mass, cf)
+    n = int(a.keep[0].shape[0])
+    gx, gxp = a.out(n)
+    gy, gyp = a.out(n)
+    gw, gwp = a.out(n)
+    src = dm.src
+    nv = src.nx * src.ny if isinstance(src, GridMesh) else src.nv
+    gr, grp = a.out(nv) if grad_rho else (None, None)
+    st = ctx.lib.ma_kantorovich_vjp(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.mem, float(cot_value),
+                                    a.ptrs[3], a.ptrs[4], gxp, gyp, gwp, grp)
+    _check(ctx.lib, ctx.h, st, "ma_kantorovich_vjp")
+    if a.device:
+        import torch
+        gX = torch.stack([gx, gy], 1)
+    else:
+        gX = np.stack([gx, gy], 1)
+    return gX, gw, gr
 
 
 def hessian_copy(ctx: Context, n: int, nnz: int) -> Hessian:

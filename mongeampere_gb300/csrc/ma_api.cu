@@ -154,9 +154,11 @@ static ma_status ensure_eval_buffers(Ctx* c, int n, bool mom)
     return MA_OK;
 }
 
-// main pass: stage 1 (cells) then stage 2 (pieces); cap_kind 1: large-capacity pass
-static void launch_cells(Ctx* c, const Mesh* m, const CellArgs& a, int cap_kind, bool mom)
+// main pass: stage 1 (cells) then stage 2 (pieces); cap_kind 1: large-capacity pass.
+// mode: 0 evaluation, 1 with moments, 2 adjoint
+static void launch_cells(Ctx* c, const Mesh* m, const CellArgs& a, int cap_kind, int mode)
 {
+    const bool mom = mode == 1;
     if (cap_kind == 0) {
         {
             ProfScope ps(c, &c->profile.cells_ms, &c->profile.cells_launches);
@@ -165,9 +167,9 @@ static void launch_cells(Ctx* c, const Mesh* m, const CellArgs& a, int cap_kind,
         {
             ProfScope ps(c, &c->profile.pieces_ms, &c->profile.pieces_launches);
             if (m->kind == 0)
-                launch_pieces_grid(a, m->grid_dev(), mom, c->stream);
+                launch_pieces_grid(a, m->grid_dev(), mode, c->stream);
             else
-                launch_pieces_tri(a, m->tri_dev(), mom, c->stream);
+                launch_pieces_tri(a, m->tri_dev(), mode, c->stream);
         }
         c->launches += 2;
     } else {
@@ -248,7 +250,21 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     a.big_col = nullptr;
     a.big_val = nullptr;
     a.big_cap = large_row_cap();
-    launch_cells(c, m, a, 0, f.moments > 0);
+    a.cot_value = 0.0;
+    a.cot_mass = nullptr;
+    a.cot_mom = nullptr;
+    a.grad_x = a.grad_y = a.grad_w = a.grad_rho = nullptr;
+    if (f.vjp) {
+        a.cot_value = f.vjp->cot_value;
+        a.cot_mass = f.vjp->cot_mass;
+        a.cot_mom = f.vjp->cot_first;
+        a.grad_x = f.vjp->grad_x;
+        a.grad_y = f.vjp->grad_y;
+        a.grad_w = f.vjp->grad_w;
+        a.grad_rho = f.vjp->grad_rho;
+    }
+    const int mode = f.vjp ? 2 : (f.moments > 0 ? 1 : 0);
+    launch_cells(c, m, a, 0, mode);
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     c->hinfo[3] = 0;
@@ -262,6 +278,15 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         return MA_OK;
     }
     int nredo = c->hinfo[0];
+    if (f.vjp) {
+        c->have_h = false;
+        if (nredo > 0)
+            return fail(c, MA_ERR_CAPACITY,
+                        "the adjoint handles cells of at most 48 neighbours whose pieces need no exact predicate");
+        uint32_t vb = (uint32_t)c->hinfo[1];
+        if (vb & ST_BAD_INPUT) return fail(c, MA_ERR_INVALID_ARGUMENT, "non-finite site or weight");
+        return MA_OK;
+    }
     if (nredo > 0) {
         // sites whose cell outgrew the small capacity: redo them with the large one
         CellArgs b = a;
@@ -279,7 +304,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         b.nredo = c->nredo.as<int>() + 1;
         {
             ProfScope ps(c, &c->profile.cells_large_ms, &c->profile.cells_large_launches);
-            launch_cells(c, m, b, 1, f.moments > 0);
+            launch_cells(c, m, b, 1, mode);
         }
         c->profile.large_sites += nredo;
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -383,7 +408,8 @@ void ma_ctx_destroy(ma_ctx* c)
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->abortf, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
+    DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->abortf, &c->vjp_cm, &c->vjp_cf,
+                      &c->vjp_gx, &c->vjp_gy, &c->vjp_gw, &c->vjp_gr, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
                       &c->perm, &c->sites, &c->posf, &c->scan_scratch, &c->fill, &c->t_child, &c->t_range,
                       &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab,
                       &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,
@@ -442,6 +468,64 @@ ma_status ma_ctx_profile_read(const ma_ctx* c, ma_profile* out)
     return MA_OK;
 }
 
+// the linear interpolant of grid values integrates to area * mean of the three
+// vertex values on each of the two triangles of a square
+static double grid_total_mass(const std::vector<double>& gx, const std::vector<double>& gy, const double* values)
+{
+    const int nx = (int)gx.size(), ny = (int)gy.size();
+    double tot = 0;
+    for (int j = 0; j + 1 < ny; j++) {
+        for (int i = 0; i + 1 < nx; i++) {
+            double a = (gx[i + 1] - gx[i]) * (gy[j + 1] - gy[j]) / 2.0;
+            double v00 = values[j * nx + i], v10 = values[j * nx + i + 1];
+            double v01 = values[(j + 1) * nx + i], v11 = values[(j + 1) * nx + i + 1];
+            tot += a * (v00 + v10 + v11) / 3.0 + a * (v00 + v11 + v01) / 3.0;
+        }
+    }
+    return tot;
+}
+
+// per-triangle linear function (value at the first corner, gradient) of the
+// vertex values, Linear_function of functions.hpp:55-80; returns the total mass
+static double tri_linear(const std::vector<double>& vx, const std::vector<double>& vy, const std::vector<int>& t,
+                         const double* values, std::vector<double>& lin)
+{
+    const size_t nt = t.size() / 3;
+    lin.assign(3 * nt, 0.0);
+    double tot = 0;
+    for (size_t f = 0; f < nt; f++) {
+        const int a = t[3 * f], b = t[3 * f + 1], d = t[3 * f + 2];
+        const double e1x = vx[b] - vx[a], e1y = vy[b] - vy[a], e2x = vx[d] - vx[a], e2y = vy[d] - vy[a];
+        const double det = e1x * e2y - e1y * e2x;
+        const double f1 = values[b] - values[a], f2 = values[d] - values[a];
+        lin[3 * f] = values[a];
+        lin[3 * f + 1] = (f1 * e2y - f2 * e1y) / det;
+        lin[3 * f + 2] = (e1x * f2 - e2x * f1) / det;
+        tot += det / 2.0 * (values[a] + values[b] + values[d]) / 3.0;
+    }
+    return tot;
+}
+
+ma_status ma_mesh_set_values(ma_ctx* c, ma_mesh* m, const double* values, ma_mem mem)
+{
+    if (!c || !m || !values || m->ctx != c) return MA_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    const size_t nv = m->kind == 0 ? (size_t)m->nx * m->ny : (size_t)m->nv;
+    std::vector<double> v(nv);
+    MA_CUDA(c, cudaStreamSynchronize(c->stream));
+    MA_CUDA(c, cudaMemcpy(v.data(), values, sizeof(double) * nv,
+                          mem == MA_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+    if (m->kind == 0) {
+        m->total_mass = grid_total_mass(m->hgx, m->hgy, v.data());
+        MA_CUDA(c, cudaMemcpy(m->val.p, v.data(), sizeof(double) * nv, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<double> lin;
+        m->total_mass = tri_linear(m->hvx, m->hvy, m->htri, v.data(), lin);
+        MA_CUDA(c, cudaMemcpy(m->lin.p, lin.data(), sizeof(double) * lin.size(), cudaMemcpyHostToDevice));
+    }
+    return MA_OK;
+}
+
 ma_status ma_mesh_create_grid(ma_ctx* c, int nx, int ny, const double* gx, const double* gy, const double* values,
                               ma_mesh** out)
 {
@@ -465,18 +549,9 @@ ma_status ma_mesh_create_grid(ma_ctx* c, int nx, int ny, const double* gx, const
     for (int j = 0; j + 1 < ny; j++) ihy[j] = 1.0 / (gy[j + 1] - gy[j]);
     ihx[nx - 1] = 0;
     ihy[ny - 1] = 0;
-    // total mass: every square holds two triangles of area A/2; the linear
-    // interpolant integrates to area * mean of the three vertex values
-    double tot = 0;
-    for (int j = 0; j + 1 < ny; j++) {
-        for (int i = 0; i + 1 < nx; i++) {
-            double a = (gx[i + 1] - gx[i]) * (gy[j + 1] - gy[j]) / 2.0;
-            double v00 = values[j * nx + i], v10 = values[j * nx + i + 1];
-            double v01 = values[(j + 1) * nx + i], v11 = values[(j + 1) * nx + i + 1];
-            tot += a * (v00 + v10 + v11) / 3.0 + a * (v00 + v11 + v01) / 3.0;
-        }
-    }
-    m->total_mass = tot;
+    m->hgx.assign(gx, gx + nx);
+    m->hgy.assign(gy, gy + ny);
+    m->total_mass = grid_total_mass(m->hgx, m->hgy, values);
     cudaError_t e = cudaSuccess;
     if ((e = m->gx.ensure(sizeof(double) * nx)) != cudaSuccess ||
         (e = m->gy.ensure(sizeof(double) * ny)) != cudaSuccess ||
@@ -545,6 +620,9 @@ ma_status ma_mesh_create_triangles(ma_ctx* c, int nv, const double* vx, const do
     m->Y0 = Y0;
     m->Y1 = Y1;
     m->total_mass = tot;
+    m->hvx.assign(vx, vx + nv);
+    m->hvy.assign(vy, vy + nv);
+    m->htri = t;
     // bins: about two triangles per bin
     double W = std::max(X1 - X0, 1e-300), H = std::max(Y1 - Y0, 1e-300);
     double target = std::max(1.0, nt / 2.0);
@@ -666,6 +744,59 @@ ma_status ma_kantorovich(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x
     MA_CUDA(c, cudaStreamSynchronize(c->stream));
     if (value) *value = c->hstat[0];
     if (nnz) *nnz = c->nnz;
+    return MA_OK;
+}
+
+ma_status ma_kantorovich_vjp(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x, const double* y,
+                             const double* w, ma_mem mem, double cot_value, const double* cot_mass,
+                             const double* cot_first, double* grad_x, double* grad_y, double* grad_w,
+                             double* grad_rho)
+{
+    if (!c || !m || !x || !y || !w || !grad_x || !grad_y || !grad_w || n < 1 || n > (int64_t)1 << 30)
+        return MA_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    const double *dx, *dy, *dw, *dcm = nullptr, *dcf = nullptr;
+    ma_status st;
+    if ((st = stage_in(c, c->hx, x, n, mem, &dx)) != MA_OK) return st;
+    if ((st = stage_in(c, c->hy, y, n, mem, &dy)) != MA_OK) return st;
+    if ((st = stage_in(c, c->hw, w, n, mem, &dw)) != MA_OK) return st;
+    if (cot_mass && (st = stage_in(c, c->vjp_cm, cot_mass, n, mem, &dcm)) != MA_OK) return st;
+    if (cot_first && (st = stage_in(c, c->vjp_cf, cot_first, 2 * n, mem, &dcf)) != MA_OK) return st;
+    const int64_t nv = m->kind == 0 ? (int64_t)m->nx * m->ny : (int64_t)m->nv;
+    VjpArgs v;
+    v.cot_value = cot_value;
+    v.cot_mass = dcm;
+    v.cot_first = dcf;
+    if (mem == MA_MEM_DEVICE) {
+        v.grad_x = grad_x;
+        v.grad_y = grad_y;
+        v.grad_w = grad_w;
+        v.grad_rho = grad_rho;
+    } else {
+        MA_CUDA(c, c->vjp_gx.ensure(sizeof(double) * (size_t)n));
+        MA_CUDA(c, c->vjp_gy.ensure(sizeof(double) * (size_t)n));
+        MA_CUDA(c, c->vjp_gw.ensure(sizeof(double) * (size_t)n));
+        v.grad_x = c->vjp_gx.as<double>();
+        v.grad_y = c->vjp_gy.as<double>();
+        v.grad_w = c->vjp_gw.as<double>();
+        if (grad_rho) {
+            MA_CUDA(c, c->vjp_gr.ensure(sizeof(double) * (size_t)nv));
+            v.grad_rho = c->vjp_gr.as<double>();
+        }
+    }
+    if (v.grad_rho) MA_CUDA(c, cudaMemsetAsync(v.grad_rho, 0, sizeof(double) * (size_t)nv, c->stream));
+    if ((st = build_site_index(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
+    EvalFlags f;
+    f.hessian = false;
+    f.vjp = &v;
+    if ((st = run_eval(c, m, (int)n, dw, f)) != MA_OK) return st;
+    if (mem == MA_MEM_HOST) {
+        if ((st = copy_out(c, grad_x, v.grad_x, (size_t)n, mem)) != MA_OK) return st;
+        if ((st = copy_out(c, grad_y, v.grad_y, (size_t)n, mem)) != MA_OK) return st;
+        if ((st = copy_out(c, grad_w, v.grad_w, (size_t)n, mem)) != MA_OK) return st;
+        if (grad_rho && (st = copy_out(c, grad_rho, v.grad_rho, (size_t)nv, mem)) != MA_OK) return st;
+    }
+    MA_CUDA(c, cudaStreamSynchronize(c->stream));
     return MA_OK;
 }
 

@@ -598,6 +598,94 @@ MA_HD void integrate_labels(int n, const Lab& lab_of, const Nb64* nb, const Fixe
     }
 }
 
+// ---------------------------------------------------------------------------
+// adjoint of one piece
+// ---------------------------------------------------------------------------
+// Moments of the piece in owner-relative coordinates u = x - x_i (fan from the
+// owner, as above): I1 = int 1, Iu = int u, S = int u u^T (xx, yy, xy),
+// Iq = int |u|^2, Ic = int u |u|^2.
+struct PieceMoments {
+    double I1, Iux, Iuy, Sxx, Syy, Sxy, Iq, Icx, Icy;
+};
+
+// The cotangent-weighted boundary terms of the piece's radical-axis edges.  An edge
+// on the radical axis of neighbour j moves when x_i, x_j, w_i or w_j move; with
+// d = x_j - x_i and the line integrals over the edge
+//     E0 = int rho / |d|,  Eu = int rho u / |d|,  Euu = int rho u u^T / |d|
+// (rho and u are linear along the edge, so Simpson's rule is exact for all three),
+// the terms that land on site i are
+//     g_w += (b_i - b_j) E0 / 2 + (e_i - e_j) . (x_i E0 + Eu) / 2
+//     g_x += (b_i - b_j) Eu + ((e_i - e_j) . x_i) Eu + Euu (e_i - e_j)
+// for the cotangents b of the masses and e of the first moments int rho x.  (The
+// reference has no adjoint; these are the shape derivatives of its cells, whose
+// w-part is the Hessian of kantorovich.hpp:110-121.)  cot(slot) returns the
+// neighbour's (b_j, e_jx, e_jy).
+template <class Lab, class Cot>
+MA_HD void integrate_vjp(int n, const Lab& lab_of, const Nb64* nb, const Fixed& fx, double c0, double gx, double gy,
+                         double xi, double yi, double bi, double exi, double eyi, const Cot& cot, PieceMoments& M,
+                         double& gw, double& gpx, double& gpy)
+{
+    double x0, y0;
+    vtx64(lab_of(n - 1), lab_of(0), nb, fx, x0, y0);
+    double ax = x0, ay = y0;
+    double m0 = 0, m1x = 0, m1y = 0, q2 = 0, c3x = 0, c3y = 0, sxx = 0, syy = 0, sxy = 0;
+    for (int k = 0; k < n; k++) {
+        const int lab = lab_of(k);
+        double bx, by;
+        if (k + 1 < n)
+            vtx64(lab, lab_of(k + 1), nb, fx, bx, by);
+        else {
+            bx = x0;
+            by = y0;
+        }
+        const double cr = ax * by - ay * bx;
+        const double aa = ax * ax + ay * ay, ab = ax * bx + ay * by, bb = bx * bx + by * by;
+        m0 += cr;
+        m1x += cr * (ax + bx);
+        m1y += cr * (ay + by);
+        q2 += cr * (aa + ab + bb);
+        const double ka = 3.0 * aa + 2.0 * ab + bb, kb = aa + 2.0 * ab + 3.0 * bb;
+        c3x += cr * (ax * ka + bx * kb);
+        c3y += cr * (ay * ka + by * kb);
+        sxx += cr * (2.0 * (ax * ax + bx * bx) + 2.0 * ax * bx);
+        syy += cr * (2.0 * (ay * ay + by * by) + 2.0 * ay * by);
+        sxy += cr * (2.0 * (ax * ay + bx * by) + ax * by + bx * ay);
+        if (lab >= 0) {
+            const Nb64 d = nb[lab];
+            const double ex = bx - ax, ey = by - ay;
+            // |edge| / |d| = |edge x d| / |d|^2 (the edge is perpendicular to d)
+            const double ratio = fabs(ex * d.dy - ey * d.dx) / (d.dx * d.dx + d.dy * d.dy);
+            const double mx = 0.5 * (ax + bx), my = 0.5 * (ay + by);
+            const double ra = c0 + gx * ax + gy * ay, rb = c0 + gx * bx + gy * by, rm = c0 + gx * mx + gy * my;
+            const double E0 = ratio * rm;
+            const double w6 = ratio * (1.0 / 6.0);
+            const double Eux = w6 * (ra * ax + 4.0 * rm * mx + rb * bx);
+            const double Euy = w6 * (ra * ay + 4.0 * rm * my + rb * by);
+            const double Exx = w6 * (ra * ax * ax + 4.0 * rm * mx * mx + rb * bx * bx);
+            const double Eyy = w6 * (ra * ay * ay + 4.0 * rm * my * my + rb * by * by);
+            const double Exy = w6 * (ra * ax * ay + 4.0 * rm * mx * my + rb * bx * by);
+            double bj, ejx, ejy;
+            cot(lab, bj, ejx, ejy);
+            const double db = bi - bj, dex = exi - ejx, dey = eyi - ejy;
+            gw += 0.5 * db * E0 + 0.5 * (dex * (xi * E0 + Eux) + dey * (yi * E0 + Euy));
+            const double dx = dex * xi + dey * yi;
+            gpx += (db + dx) * Eux + Exx * dex + Exy * dey;
+            gpy += (db + dx) * Euy + Exy * dex + Eyy * dey;
+        }
+        ax = bx;
+        ay = by;
+    }
+    M.I1 = m0 * 0.5;
+    M.Iux = m1x * (1.0 / 6.0);
+    M.Iuy = m1y * (1.0 / 6.0);
+    M.Sxx = sxx * (1.0 / 24.0);
+    M.Syy = syy * (1.0 / 24.0);
+    M.Sxy = sxy * (1.0 / 24.0);
+    M.Iq = q2 * (1.0 / 12.0);
+    M.Icx = c3x * (1.0 / 60.0);
+    M.Icy = c3y * (1.0 / 60.0);
+}
+
 template <int CAP, bool MOM>
 MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, double c0, double gx,
                            double gy, Acc& acc, double* hv, Bits<CAP>& touched)

@@ -661,9 +661,12 @@ struct CellInfo {
     int4 box;  // mesh-specific range of triangles under the cell's box
 };
 
-template <bool MOM>
+// modes of k_pieces: the evaluation, the evaluation with moments, the adjoint
+constexpr int kModeEval = 0, kModeMoments = 1, kModeVjp = 2;
+
+template <int MODE>
 struct PieceWarp {
-    static constexpr int kAcc = MOM ? 7 : 2;
+    static constexpr int kAcc = MODE == kModeVjp ? 3 : (MODE == kModeMoments ? 7 : 2);
     Slot slot[kSlotPool];
     Nb64 nb[kSlotPool];
     PieceRec rec[kList];
@@ -700,6 +703,15 @@ struct GridPieces {
     {
         int sq = id >> 1;
         grid_triangle(m, sq % (m.nx - 1), sq / (m.nx - 1), id & 1, o, T, c0, gx, gy);
+    }
+    // vertex indices (j nx + i) of the triangle's corners, in the order of grid_fixed
+    __device__ __forceinline__ void vertices(int id, int* v) const
+    {
+        const int sq = id >> 1, i = sq % (m.nx - 1), j = sq / (m.nx - 1);
+        const int v00 = j * m.nx + i;
+        v[0] = v00;
+        v[1] = (id & 1) ? v00 + m.nx + 1 : v00 + 1;
+        v[2] = (id & 1) ? v00 + m.nx : v00 + m.nx + 1;
     }
 };
 
@@ -740,6 +752,12 @@ struct TriPieces {
                                              double& gy) const
     {
         tri_triangle(m, id, o, T, c0, gx, gy);
+    }
+    __device__ __forceinline__ void vertices(int id, int* v) const
+    {
+        v[0] = m.tri[3 * id];
+        v[1] = m.tri[3 * id + 1];
+        v[2] = m.tri[3 * id + 2];
     }
 };
 
@@ -807,14 +825,63 @@ __device__ __forceinline__ void finish_cell(const CellArgs& A, const CellInfo& C
     }
 }
 
-template <bool MOM, class E>
+// the adjoint of one listed piece: its share of g_w and g_x of the owner (the
+// radical-axis edge terms of integrate_vjp plus the value's interior terms
+// a int rho and 2 a int rho u), and its share of g_rho on the triangle's corners,
+//     int_piece (a (w_i - |u|^2) + b_i + e_i . x) lambda_k(x)
+// for the barycentric coordinate lambda_k (linear; the integrand is cubic in u)
+template <class E>
+__device__ __forceinline__ void vjp_piece(const CellArgs& A, const E& mesh, const PieceRec& R, int k, int gi,
+                                          const SiteD& S, const Slot* sl, const Nb64* nb, const Fixed& T, double c0,
+                                          double gx, double gy, double& ow, double& ox, double& oy)
+{
+    const double a = A.cot_value;
+    const double bi = A.cot_mass ? A.cot_mass[gi] : 0.0;
+    const double exi = A.cot_mom ? A.cot_mom[2 * (size_t)gi] : 0.0;
+    const double eyi = A.cot_mom ? A.cot_mom[2 * (size_t)gi + 1] : 0.0;
+    PieceMoments M;
+    double gw = 0.0, gpx = 0.0, gpy = 0.0;
+    integrate_vjp(
+        (int)R.n, [&](int e) { return (int)R.lab[e]; }, nb, T, c0, gx, gy, S.x, S.y, bi, exi, eyi,
+        [&](int slot, double& bj, double& ejx, double& ejy) {
+            const int gj = A.perm[sl[slot].site];
+            bj = A.cot_mass ? A.cot_mass[gj] : 0.0;
+            ejx = A.cot_mom ? A.cot_mom[2 * (size_t)gj] : 0.0;
+            ejy = A.cot_mom ? A.cot_mom[2 * (size_t)gj + 1] : 0.0;
+        },
+        M, gw, gpx, gpy);
+    const double rho_m = c0 * M.I1 + gx * M.Iux + gy * M.Iuy;
+    const double rux = c0 * M.Iux + gx * M.Sxx + gy * M.Sxy, ruy = c0 * M.Iuy + gx * M.Sxy + gy * M.Syy;
+    ow = gw + a * rho_m;
+    ox = gpx + 2.0 * a * rux;
+    oy = gpy + 2.0 * a * ruy;
+    if (!A.grad_rho) return;
+    int v[3];
+    mesh.vertices(R.tri, v);
+    const double cp = a * S.w + bi + exi * S.x + eyi * S.y;
+    const double s0 = cp * M.I1 + exi * M.Iux + eyi * M.Iuy - a * M.Iq;
+    const double sx = cp * M.Iux + M.Sxx * exi + M.Sxy * eyi - a * M.Icx;
+    const double sy = cp * M.Iuy + M.Sxy * exi + M.Syy * eyi - a * M.Icy;
+    const double A2 = (T.rx[1] - T.rx[0]) * (T.ry[2] - T.ry[0]) - (T.ry[1] - T.ry[0]) * (T.rx[2] - T.rx[0]);
+    for (int q = 0; q < 3; q++) {
+        const int q1 = q == 2 ? 0 : q + 1, q2 = q == 0 ? 2 : q - 1;
+        const double ex = T.rx[q2] - T.rx[q1], ey = T.ry[q2] - T.ry[q1];
+        // lambda_q(u) = (e x (u - r_q1)) / A2 = alpha + beta . u
+        const double alpha = (ey * T.rx[q1] - ex * T.ry[q1]) / A2;
+        const double bx = -ey / A2, by = ex / A2;
+        atomicAdd(&A.grad_rho[v[q]], alpha * s0 + bx * sx + by * sy);
+    }
+}
+
+template <int MODE, class E>
 __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
 {
-    constexpr int kAcc = PieceWarp<MOM>::kAcc;
+    constexpr bool MOM = MODE == kModeMoments, VJP = MODE == kModeVjp;
+    constexpr int kAcc = PieceWarp<MODE>::kAcc;
     constexpr unsigned kFull = 0xffffffffu;
-    __shared__ PieceWarp<MOM> shw[kPieceWarps];
+    __shared__ PieceWarp<MODE> shw[kPieceWarps];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    PieceWarp<MOM>& W = shw[wib];
+    PieceWarp<MODE>& W = shw[wib];
     const int kbase = (blockIdx.x * kPieceWarps + wib) * kWarpCells;
     if (kbase >= A.n) return;
     if (A.abort_flag && *(volatile const int*)A.abort_flag) return;
@@ -825,7 +892,16 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
     if (lane < ncell) {
         const int k = kbase + lane;
         my_m = A.nb_cnt[k];
-        if (my_m == -1) write_empty(A, A.perm[k], MOM);
+        if (my_m == -1) {
+            const int gi = A.perm[k];
+            if (VJP) {
+                A.grad_w[gi] = 0.0;
+                A.grad_x[gi] = 0.0;
+                A.grad_y[gi] = 0.0;
+            } else {
+                write_empty(A, gi, MOM);
+            }
+        }
         if (my_m >= 0) my_cnt = mesh.setup(A.cell_box[k], my_box);
     }
     uint32_t st = 0;
@@ -927,6 +1003,15 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                 Fixed T;
                 double c0, gx, gy;
                 mesh.triangle(R.tri, o, T, c0, gx, gy);
+                if (VJP) {
+                    double ow, ox, oy;
+                    vjp_piece(A, mesh, R, C.k, A.perm[C.k], S, W.slot + C.soff, W.nb + C.soff, T, c0, gx, gy, ow, ox,
+                              oy);
+                    W.out[0][p] = ow;
+                    W.out[1 % kAcc][p] = ox;
+                    W.out[2 % kAcc][p] = oy;
+                    continue;
+                }
                 Acc acc{0, 0, 0, 0, 0, 0, 0};
                 integrate_labels<MOM>(
                     (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.nb + C.soff, T, c0, gx, gy, acc,
@@ -961,7 +1046,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                     for (int p = p0 + lane; p < p1; p += 32) v += W.out[q][p];
                     run[q] += warp_sum(v);
                 }
-                for (int p = p0; p < p1; p++) {
+                for (int p = p0; p < p1 && !VJP; p++) {
                     const int n = W.rec[p].n;
                     for (int e = 0; e < n; e++) {
                         const int l = W.rec[p].lab[e];
@@ -981,6 +1066,13 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                         if (lane == 0) {
                             A.redo[atomicAdd(A.nredo, 1)] = C.k;
                             atomicOr(A.status, ST_POLY_OVERFLOW);
+                        }
+                    } else if (VJP) {
+                        if (lane == 0) {
+                            const int gi = A.perm[C.k];
+                            A.grad_w[gi] = run[0];
+                            A.grad_x[gi] = run[1 % kAcc];
+                            A.grad_y[gi] = run[2 % kAcc];
                         }
                     } else {
                         finish_cell<MOM>(A, C, run, h0, h1, t0, t1, W.slot + C.soff, W.nb + C.soff, lane);
@@ -1029,24 +1121,28 @@ static unsigned pieces_blocks(int n)
     return (unsigned)((warps + kPieceWarps - 1) / kPieceWarps);
 }
 
-void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s)
+void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, int mode, cudaStream_t s)
 {
     if (a.n <= 0) return;
     GridPieces e{m};
-    if (mom)
-        k_pieces<true><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    if (mode == kModeVjp)
+        k_pieces<kModeVjp><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeMoments)
+        k_pieces<kModeMoments><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else
-        k_pieces<false><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeEval><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
 }
 
-void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s)
+void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, int mode, cudaStream_t s)
 {
     if (a.n <= 0) return;
     TriPieces e{m};
-    if (mom)
-        k_pieces<true><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    if (mode == kModeVjp)
+        k_pieces<kModeVjp><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeMoments)
+        k_pieces<kModeMoments><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else
-        k_pieces<false><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeEval><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
 }
 
 void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s)

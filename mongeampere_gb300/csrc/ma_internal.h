@@ -71,6 +71,16 @@ struct CellArgs {
     double4* cell_box;       // stage 1 -> 2: absolute bounding box of the cell
     unsigned long long* counters;  // optional stage-1 search counters (6)
     int* abort_flag;         // optional: set at the first empty cell, and every cell then stops
+    // adjoint (k_pieces in its VJP mode): cotangents of the value, the masses and
+    // the first moments int rho x (2 per site), and the gradients (original order;
+    // grad_rho per mesh vertex, accumulated with atomics)
+    double cot_value;
+    const double* cot_mass;
+    const double* cot_mom;
+    double* grad_x;
+    double* grad_y;
+    double* grad_w;
+    double* grad_rho;
     void* scratch;           // large-capacity pass: one workspace per work item
     int* big_index;          // per site: row slot in the side buffer, -1 otherwise
     int* big_col;
@@ -102,8 +112,9 @@ void launch_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s); 
 size_t scan_scratch_ints(int n);
 // cell kernels (ma_cells.cu)
 void launch_cells_stage1(const CellArgs& a, cudaStream_t s);
-void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s);
-void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s);
+// mode: 0 evaluation, 1 evaluation with moments, 2 adjoint (vector-Jacobian product)
+void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, int mode, cudaStream_t s);
+void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, int mode, cudaStream_t s);
 void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s);
 void launch_cells_large_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s);
 int stage1_cap();

@@ -55,6 +55,9 @@ struct Mesh {
     DevBuf vx, vy, tri, lin, tbin, bin_start, bin_tri;
     int bnx = 0, bny = 0;
     double bx0 = 0, by0 = 0, bcw = 0, bch = 0;
+    // host copies of the geometry (new vertex values keep it)
+    std::vector<double> hgx, hgy, hvx, hvy;
+    std::vector<int> htri;  // counter-clockwise
     MeshGridDev grid_dev() const;
     MeshTriDev tri_dev() const;
 };
@@ -88,6 +91,7 @@ struct Ctx {
     DevBuf nb_cnt, nb_lab, cell_box;               // stage 1 -> stage 2
     bool prev_valid = false;                       // nb_cnt/nb_lab match the current site index
     DevBuf abortf;                                 // empty-cell flag of a line-search trial
+    DevBuf vjp_cm, vjp_cf, vjp_gx, vjp_gy, vjp_gw, vjp_gr;  // adjoint staging (host callers)
     bool aborted = false;                          // the last evaluation stopped at an empty cell
     DevBuf counters;                               // stage-1 search counters (profiling)
     DevBuf info;  // status, nredo, nnz
@@ -117,8 +121,20 @@ ma_status cuda_fail(Ctx* c, cudaError_t e, const char* what);
 
 // evaluation pipeline (device pointers)
 ma_status build_site_index(Ctx* c, const Mesh* m, int n, const double* x, const double* y, const double* w);
+// adjoint of one evaluation: cotangents in, gradients out (device, original order)
+struct VjpArgs {
+    double cot_value = 0.0;
+    const double* cot_mass = nullptr;  // n or null
+    const double* cot_first = nullptr; // 2n (x, y per site) or null
+    double* grad_x = nullptr;
+    double* grad_y = nullptr;
+    double* grad_w = nullptr;
+    double* grad_rho = nullptr;  // mesh vertices (zeroed by the caller) or null
+};
+
 struct EvalFlags {
     bool hessian = true;
+    const VjpArgs* vjp = nullptr;  // when set: the adjoint instead of the outputs
     int moments = 0;  // 0 none, 1 first, 2 second
     const double* nu = nullptr;  // when given, stat_out[0] = value - <nu, w>
     // Newton line-search trial: an empty cell already rejects the trial (its mass 0
