@@ -193,6 +193,28 @@ ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int3
                                     const double* g, double* d, double rtol, int64_t maxiter, int64_t* iters,
                                     void* stream);
 
+/* ------------------------------------------------------------------ pieces */
+/* MA::voronoi_triangulation_intersection (voronoi_triangulation_intersection.hpp:
+ * 315-343): every non-empty intersection of a Laguerre cell with a mesh triangle, as
+ * a convex polygon.  The reference hands each piece to a callback out(polygon, face,
+ * vertex); here ma_pieces computes them all on the device and returns their number
+ * and their total vertex count, and ma_pieces_copy fills (each pointer nullable):
+ *   site[np]    the cell's site (original index)     -- the reference's Vertex_handle
+ *   tri[np]     the mesh triangle (grid: 2 (j (nx-1) + i) + t, the explicit
+ *               triangulation's order; triangle mesh: its index) -- the Face_handle
+ *   off[np+1]   first vertex of each piece; off[np] = nverts
+ *   xy[2 nv]    polygon vertices, counter-clockwise, absolute (x, y)
+ *   edge[nv]    the edge from vertex k to vertex k+1: the neighbouring site whose
+ *               radical axis it lies on (original index; the reference's EDGE_DT), or
+ *               -1-e for edge e (v_e -> v_e+1) of the triangle (EDGE_T)
+ * Pieces are ordered by cell (in the site index's Morton order), then by triangle.
+ * Cells of more than 48 neighbours, or whose pieces need exact predicates, are not
+ * listed (MA_ERR_CAPACITY). */
+ma_status ma_pieces(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
+                    const double* w, ma_mem mem, int64_t* npieces, int64_t* nverts);
+ma_status ma_pieces_copy(ma_ctx* ctx, int32_t* site, int32_t* tri, int64_t* off, double* xy, int32_t* edge,
+                         ma_mem mem);
+
 /* ----------------------------------------------------------------- adjoint */
 /* Vector-Jacobian product of (value, mass[n], first[2n]) -- the Kantorovich value
  * sum_i (w_i m_i - int_{cell i} rho |x - x_i|^2), the cell masses and the first

@@ -64,6 +64,8 @@ SIGNATURES = {
     "ma_laplacian_solve_static": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, ctypes.c_double,
                                                  ctypes.c_int64, _i64p, _vp]),
     "ma_moments": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp]),
+    "ma_pieces": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
+    "ma_pieces_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
     "ma_mesh_set_values": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
     "ma_kantorovich_vjp": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, ctypes.c_double,
                                           _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -238,6 +238,45 @@ def kantorovich(mesh, X, weights, y=None, *, precision: str = "fp64", hessian: b
     return val.value, g, h
 
 
+@dataclass
+class Pieces:
+    """Every non-empty cell-triangle intersection (``MA::voronoi_triangulation_intersection``):
+    piece ``k`` is cell ``site[k]`` on triangle ``tri[k]`` with vertices
+    ``xy[off[k]:off[k+1]]`` (counter-clockwise); ``edge[v]`` labels the edge from vertex
+    ``v`` to the next: the neighbouring site, or ``-1-e`` for triangle edge ``e``."""
+    site: np.ndarray
+    tri: np.ndarray
+    off: np.ndarray
+    xy: np.ndarray
+    edge: np.ndarray
+
+    def polygon(self, k):
+        return self.xy[self.off[k]:self.off[k + 1]], self.edge[self.off[k]:self.off[k + 1]]
+
+
+def pieces(mesh, X, weights, y=None, ctx: Context | None = None) -> Pieces:
+    """``MA::voronoi_triangulation_intersection`` (``ma_pieces`` + ``ma_pieces_copy``)."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    x, yy = _split_xy(X, y)
+    a = _Args(x, yy, weights)
+    n = int(a.keep[0].shape[0])
+    npc, nvt = ctypes.c_int64(), ctypes.c_int64()
+    st = ctx.lib.ma_pieces(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.mem, ctypes.byref(npc),
+                           ctypes.byref(nvt))
+    _check(ctx.lib, ctx.h, st, "ma_pieces")
+    np_, nv = int(npc.value), int(nvt.value)
+    site = np.empty(np_, np.int32)
+    tri = np.empty(np_, np.int32)
+    off = np.empty(np_ + 1, np.int64)
+    xy = np.empty((nv, 2), np.float64)
+    edge = np.empty(nv, np.int32)
+    vp = lambda arr: ctypes.c_void_p(arr.ctypes.data)
+    st = ctx.lib.ma_pieces_copy(ctx.h, vp(site), vp(tri), vp(off), vp(xy), vp(edge), L.MA_MEM_HOST)
+    _check(ctx.lib, ctx.h, st, "ma_pieces_copy")
+    return Pieces(site, tri, off, xy, edge)
+
+
 def kantorovich_vjp(mesh, X, weights, cot_value: float = 0.0, cot_mass=None, cot_first=None, y=None, *,
                     grad_rho: bool = True, ctx: Context | None = None):
     """Adjoint of ``(value, masses, first moments)`` (``ma_kantorovich_vjp``; no

@@ -263,7 +263,22 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         a.grad_w = f.vjp->grad_w;
         a.grad_rho = f.vjp->grad_rho;
     }
-    const int mode = f.vjp ? 2 : (f.moments > 0 ? 1 : 0);
+    a.pc_cnt = a.pv_cnt = nullptr;
+    a.pc_base = a.pv_base = nullptr;
+    a.out_site = a.out_tri = a.out_edge = nullptr;
+    a.out_off = nullptr;
+    a.out_xy = nullptr;
+    if (f.pieces) {
+        MA_CUDA(c, c->pc_cnt.ensure(sizeof(int) * ((size_t)n + 1)));
+        MA_CUDA(c, c->pv_cnt.ensure(sizeof(int) * ((size_t)n + 1)));
+        MA_CUDA(c, c->pc_base.ensure(sizeof(int) * ((size_t)n + 1)));
+        MA_CUDA(c, c->pv_base.ensure(sizeof(int) * ((size_t)n + 1)));
+        MA_CUDA(c, cudaMemsetAsync(c->pc_cnt.p, 0, sizeof(int) * ((size_t)n + 1), s));
+        MA_CUDA(c, cudaMemsetAsync(c->pv_cnt.p, 0, sizeof(int) * ((size_t)n + 1), s));
+        a.pc_cnt = c->pc_cnt.as<int>();
+        a.pv_cnt = c->pv_cnt.as<int>();
+    }
+    const int mode = f.pieces ? 3 : (f.vjp ? 2 : (f.moments > 0 ? 1 : 0));
     launch_cells(c, m, a, 0, mode);
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -278,6 +293,45 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         return MA_OK;
     }
     int nredo = c->hinfo[0];
+    if (f.pieces) {
+        // the count pass is done: offsets, then the emit pass over the same cells
+        c->have_h = false;
+        c->have_pieces = false;
+        if (nredo > 0)
+            return fail(c, MA_ERR_CAPACITY,
+                        "the pieces are listed for cells of at most 48 neighbours whose pieces need no exact "
+                        "predicate");
+        if ((uint32_t)c->hinfo[1] & ST_BAD_INPUT) return fail(c, MA_ERR_INVALID_ARGUMENT, "non-finite site or weight");
+        launch_scan(c->pc_cnt.as<int>(), c->pc_base.as<int>(), n, c->scan_scratch.as<int>(), s);
+        launch_scan(c->pv_cnt.as<int>(), c->pv_base.as<int>(), n, c->scan_scratch.as<int>(), s);
+        MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 4, c->pc_base.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 5, c->pv_base.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MA_CUDA(c, cudaStreamSynchronize(s));
+        const int64_t np = c->hinfo[4], nv = c->hinfo[5];
+        MA_CUDA(c, c->pc_site.ensure(sizeof(int) * (size_t)(np + 1)));
+        MA_CUDA(c, c->pc_tri.ensure(sizeof(int) * (size_t)(np + 1)));
+        MA_CUDA(c, c->pc_off.ensure(sizeof(int64_t) * (size_t)(np + 1)));
+        MA_CUDA(c, c->pc_xy.ensure(sizeof(double) * 2 * (size_t)(nv + 1)));
+        MA_CUDA(c, c->pc_edge.ensure(sizeof(int) * (size_t)(nv + 1)));
+        a.pc_base = c->pc_base.as<int>();
+        a.pv_base = c->pv_base.as<int>();
+        a.out_site = c->pc_site.as<int>();
+        a.out_tri = c->pc_tri.as<int>();
+        a.out_off = c->pc_off.as<int64_t>();
+        a.out_xy = c->pc_xy.as<double>();
+        a.out_edge = c->pc_edge.as<int>();
+        if (m->kind == 0)
+            launch_pieces_grid(a, m->grid_dev(), 4, s);
+        else
+            launch_pieces_tri(a, m->tri_dev(), 4, s);
+        c->launches += 5;
+        MA_CUDA(c, cudaMemcpyAsync(c->pc_off.as<int64_t>() + np, &nv, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        MA_CUDA(c, cudaStreamSynchronize(s));
+        c->npieces = np;
+        c->npverts = nv;
+        c->have_pieces = true;
+        return MA_OK;
+    }
     if (f.vjp) {
         c->have_h = false;
         if (nredo > 0)
@@ -409,7 +463,8 @@ void ma_ctx_destroy(ma_ctx* c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->abortf, &c->vjp_cm, &c->vjp_cf,
-                      &c->vjp_gx, &c->vjp_gy, &c->vjp_gw, &c->vjp_gr, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
+                      &c->vjp_gx, &c->vjp_gy, &c->vjp_gw, &c->vjp_gr, &c->pc_cnt, &c->pv_cnt,
+                      &c->pc_base, &c->pv_base, &c->pc_site, &c->pc_tri, &c->pc_off, &c->pc_xy, &c->pc_edge, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
                       &c->perm, &c->sites, &c->posf, &c->scan_scratch, &c->fill, &c->t_child, &c->t_range,
                       &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab,
                       &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,
@@ -796,6 +851,42 @@ ma_status ma_kantorovich_vjp(ma_ctx* c, const ma_mesh* m, int64_t n, const doubl
         if ((st = copy_out(c, grad_w, v.grad_w, (size_t)n, mem)) != MA_OK) return st;
         if (grad_rho && (st = copy_out(c, grad_rho, v.grad_rho, (size_t)nv, mem)) != MA_OK) return st;
     }
+    MA_CUDA(c, cudaStreamSynchronize(c->stream));
+    return MA_OK;
+}
+
+ma_status ma_pieces(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x, const double* y, const double* w,
+                    ma_mem mem, int64_t* npieces, int64_t* nverts)
+{
+    if (!c || !m || !x || !y || !w || n < 1 || n > (int64_t)1 << 30) return MA_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    const double *dx, *dy, *dw;
+    ma_status st;
+    if ((st = stage_in(c, c->hx, x, n, mem, &dx)) != MA_OK) return st;
+    if ((st = stage_in(c, c->hy, y, n, mem, &dy)) != MA_OK) return st;
+    if ((st = stage_in(c, c->hw, w, n, mem, &dw)) != MA_OK) return st;
+    if ((st = build_site_index(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
+    EvalFlags f;
+    f.hessian = false;
+    f.pieces = true;
+    if ((st = run_eval(c, m, (int)n, dw, f)) != MA_OK) return st;
+    if (npieces) *npieces = c->npieces;
+    if (nverts) *nverts = c->npverts;
+    return MA_OK;
+}
+
+ma_status ma_pieces_copy(ma_ctx* c, int32_t* site, int32_t* tri, int64_t* off, double* xy, int32_t* edge, ma_mem mem)
+{
+    if (!c) return MA_ERR_INVALID_ARGUMENT;
+    if (!c->have_pieces) return fail(c, MA_ERR_INVALID_ARGUMENT, "no pieces have been computed");
+    cudaSetDevice(c->device);
+    cudaMemcpyKind k = mem == MA_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const size_t np = (size_t)c->npieces, nv = (size_t)c->npverts;
+    if (site && np) MA_CUDA(c, cudaMemcpyAsync(site, c->pc_site.p, sizeof(int) * np, k, c->stream));
+    if (tri && np) MA_CUDA(c, cudaMemcpyAsync(tri, c->pc_tri.p, sizeof(int) * np, k, c->stream));
+    if (off) MA_CUDA(c, cudaMemcpyAsync(off, c->pc_off.p, sizeof(int64_t) * (np + 1), k, c->stream));
+    if (xy && nv) MA_CUDA(c, cudaMemcpyAsync(xy, c->pc_xy.p, sizeof(double) * 2 * nv, k, c->stream));
+    if (edge && nv) MA_CUDA(c, cudaMemcpyAsync(edge, c->pc_edge.p, sizeof(int) * nv, k, c->stream));
     MA_CUDA(c, cudaStreamSynchronize(c->stream));
     return MA_OK;
 }

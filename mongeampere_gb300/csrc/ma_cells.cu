@@ -651,6 +651,7 @@ struct PieceRec {
     int tri;
     int8_t cell, n;
     int8_t lab[kPV];
+    int rank, vrank;  // count / emit modes: index of the piece and of its first vertex within the cell
 };
 
 struct CellInfo {
@@ -659,10 +660,12 @@ struct CellInfo {
     int soff;  // first slot in the pool
     int pre;   // first flat triangle entry
     int4 box;  // mesh-specific range of triangles under the cell's box
+    int np, nv;  // count / emit modes: pieces and vertices listed so far
 };
 
-// modes of k_pieces: the evaluation, the evaluation with moments, the adjoint
-constexpr int kModeEval = 0, kModeMoments = 1, kModeVjp = 2;
+// modes of k_pieces: the evaluation, the evaluation with moments, the adjoint, and
+// the two passes that materialise the pieces (count per cell, then emit)
+constexpr int kModeEval = 0, kModeMoments = 1, kModeVjp = 2, kModeCount = 3, kModeEmit = 4;
 
 template <int MODE>
 struct PieceWarp {
@@ -877,6 +880,7 @@ template <int MODE, class E>
 __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
 {
     constexpr bool MOM = MODE == kModeMoments, VJP = MODE == kModeVjp;
+    constexpr bool LISTING = MODE == kModeCount || MODE == kModeEmit;
     constexpr int kAcc = PieceWarp<MODE>::kAcc;
     constexpr unsigned kFull = 0xffffffffu;
     __shared__ PieceWarp<MODE> shw[kPieceWarps];
@@ -894,7 +898,12 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
         my_m = A.nb_cnt[k];
         if (my_m == -1) {
             const int gi = A.perm[k];
-            if (VJP) {
+            if (LISTING) {
+                if (MODE == kModeCount) {
+                    A.pc_cnt[k] = 0;
+                    A.pv_cnt[k] = 0;
+                }
+            } else if (VJP) {
                 A.grad_w[gi] = 0.0;
                 A.grad_x[gi] = 0.0;
                 A.grad_y[gi] = 0.0;
@@ -915,7 +924,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                                       __shfl_sync(kFull, my_box.z, g1), __shfl_sync(kFull, my_box.w, g1));
             const int used = max(mc, 0);
             if (soff + used > kSlotPool) break;
-            if (lane == 0) W.ci[g1 - g0] = CellInfo{kbase + g1, mc, soff, pre, bx};
+            if (lane == 0) W.ci[g1 - g0] = CellInfo{kbase + g1, mc, soff, pre, bx, 0, 0};
             soff += used;
             pre += nc;
             g1++;
@@ -989,14 +998,59 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                     R.n = (int8_t)P->n;
                     for (int e = 0; e < P->n; e++) R.lab[e] = (int8_t)P->lab[e];
                 }
+                if (LISTING) {
+                    // rank of each kept piece within its cell, and the vertices of the
+                    // cell's earlier pieces (the lanes of one cell are adjacent)
+                    const unsigned same = __match_any_sync(kFull, keep ? cc : -1 - lane);
+                    const unsigned before = same & bal & ((1u << lane) - 1u);
+                    const int nk = keep ? P->n : 0;
+                    int vpre = 0;
+                    for (int j = 0; j < 32; j++) {
+                        const int nj = __shfl_sync(kFull, nk, j);
+                        if ((before >> j) & 1u) vpre += nj;
+                    }
+                    if (keep) {
+                        PieceRec& R = W.rec[L + __popc(bal & ((1u << lane) - 1u))];
+                        R.rank = W.ci[cc].np + __popc(before);
+                        R.vrank = W.ci[cc].nv + vpre;
+                    }
+                    __syncwarp();
+                    if (keep && !(same & bal & ~((2u << lane) - 1u))) {
+                        W.ci[cc].np += __popc(before) + 1;
+                        W.ci[cc].nv += vpre + nk;
+                    }
+                    __syncwarp();
+                }
                 L += __popc(bal);
                 f += 32;
             }
             f = min(f, total);
             __syncwarp();
             // B: one piece per lane
-            for (int p = lane; p < L; p += 32) {
+            for (int p = lane; p < L && MODE != kModeCount; p += 32) {
                 const PieceRec R = W.rec[p];
+                if (MODE == kModeEmit) {
+                    const CellInfo& C = W.ci[R.cell];
+                    const SiteD S = A.sites[C.k];
+                    const Owner o{S.x, S.y, S.w, C.k};
+                    Fixed T;
+                    mesh.fixed(R.tri, o, T);
+                    const int64_t gp = A.pc_base[C.k] + R.rank, gv = A.pv_base[C.k] + R.vrank;
+                    A.out_site[gp] = A.perm[C.k];
+                    A.out_tri[gp] = R.tri;
+                    A.out_off[gp] = gv;
+                    const Slot* sl = W.slot + C.soff;
+                    const int n = R.n;
+                    for (int e = 0; e < n; e++) {
+                        double X, Y;
+                        vtx64(R.lab[e == 0 ? n - 1 : e - 1], R.lab[e], W.nb + C.soff, T, X, Y);
+                        A.out_xy[2 * (gv + e)] = S.x + X;
+                        A.out_xy[2 * (gv + e) + 1] = S.y + Y;
+                        const int l = R.lab[e];
+                        A.out_edge[gv + e] = l >= 0 ? A.perm[sl[l].site] : l;
+                    }
+                    continue;
+                }
                 const CellInfo& C = W.ci[R.cell];
                 const SiteD S = A.sites[C.k];
                 const Owner o{S.x, S.y, S.w, C.k};
@@ -1041,12 +1095,12 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                     p1 += __popc(b);
                     if (b != kFull) break;
                 }
-                for (int q = 0; q < kAcc; q++) {
+                for (int q = 0; q < kAcc && !LISTING; q++) {
                     double v = 0.0;
                     for (int p = p0 + lane; p < p1; p += 32) v += W.out[q][p];
                     run[q] += warp_sum(v);
                 }
-                for (int p = p0; p < p1 && !VJP; p++) {
+                for (int p = p0; p < p1 && !VJP && !LISTING; p++) {
                     const int n = W.rec[p].n;
                     for (int e = 0; e < n; e++) {
                         const int l = W.rec[p].lab[e];
@@ -1066,6 +1120,11 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                         if (lane == 0) {
                             A.redo[atomicAdd(A.nredo, 1)] = C.k;
                             atomicOr(A.status, ST_POLY_OVERFLOW);
+                        }
+                    } else if (LISTING) {
+                        if (MODE == kModeCount && lane == 0) {
+                            A.pc_cnt[C.k] = C.np;
+                            A.pv_cnt[C.k] = C.nv;
                         }
                     } else if (VJP) {
                         if (lane == 0) {
@@ -1127,6 +1186,10 @@ void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, int mode, cudaS
     GridPieces e{m};
     if (mode == kModeVjp)
         k_pieces<kModeVjp><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeCount)
+        k_pieces<kModeCount><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeEmit)
+        k_pieces<kModeEmit><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeMoments)
         k_pieces<kModeMoments><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else
@@ -1139,6 +1202,10 @@ void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, int mode, cudaStr
     TriPieces e{m};
     if (mode == kModeVjp)
         k_pieces<kModeVjp><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeCount)
+        k_pieces<kModeCount><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeEmit)
+        k_pieces<kModeEmit><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeMoments)
         k_pieces<kModeMoments><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else

@@ -81,6 +81,16 @@ struct CellArgs {
     double* grad_y;
     double* grad_w;
     double* grad_rho;
+    // materialised pieces (k_pieces in its count and emit modes), cells in sorted order
+    int* pc_cnt;         // count: pieces per cell
+    int* pv_cnt;         // count: polygon vertices per cell
+    const int* pc_base;  // emit: first piece of each cell
+    const int* pv_base;  // emit: first vertex of each cell
+    int* out_site;       // emit, per piece: site (original index)
+    int* out_tri;        //                  mesh triangle
+    int64_t* out_off;    //                  first vertex
+    double* out_xy;      // emit, per vertex: absolute position (x, y)
+    int* out_edge;       //                  the edge starting there: neighbour site, or -1-e for triangle edge e
     void* scratch;           // large-capacity pass: one workspace per work item
     int* big_index;          // per site: row slot in the side buffer, -1 otherwise
     int* big_col;
@@ -112,7 +122,8 @@ void launch_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s); 
 size_t scan_scratch_ints(int n);
 // cell kernels (ma_cells.cu)
 void launch_cells_stage1(const CellArgs& a, cudaStream_t s);
-// mode: 0 evaluation, 1 evaluation with moments, 2 adjoint (vector-Jacobian product)
+// mode: 0 evaluation, 1 evaluation with moments, 2 adjoint (vector-Jacobian product),
+// 3 count the pieces per cell, 4 emit them
 void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, int mode, cudaStream_t s);
 void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, int mode, cudaStream_t s);
 void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s);

@@ -92,6 +92,10 @@ struct Ctx {
     bool prev_valid = false;                       // nb_cnt/nb_lab match the current site index
     DevBuf abortf;                                 // empty-cell flag of a line-search trial
     DevBuf vjp_cm, vjp_cf, vjp_gx, vjp_gy, vjp_gw, vjp_gr;  // adjoint staging (host callers)
+    // materialised pieces of the last ma_pieces call
+    DevBuf pc_cnt, pv_cnt, pc_base, pv_base, pc_site, pc_tri, pc_off, pc_xy, pc_edge;
+    int64_t npieces = 0, npverts = 0;
+    bool have_pieces = false;
     bool aborted = false;                          // the last evaluation stopped at an empty cell
     DevBuf counters;                               // stage-1 search counters (profiling)
     DevBuf info;  // status, nredo, nnz
@@ -135,6 +139,7 @@ struct VjpArgs {
 struct EvalFlags {
     bool hessian = true;
     const VjpArgs* vjp = nullptr;  // when set: the adjoint instead of the outputs
+    bool pieces = false;           // materialise the pieces instead of the outputs
     int moments = 0;  // 0 none, 1 first, 2 second
     const double* nu = nullptr;  // when given, stat_out[0] = value - <nu, w>
     // Newton line-search trial: an empty cell already rejects the trial (its mass 0
