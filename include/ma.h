@@ -59,8 +59,10 @@ typedef enum ma_mem { MA_MEM_HOST = 0, MA_MEM_DEVICE = 1 } ma_mem;
 
 typedef enum ma_precision {
     MA_FP64 = 0,   /* the reference's arithmetic: FP64 integrals, exact combinatorics */
-    MA_MIXED = 1   /* FP32 geometry and integrals with compensated sums, exact combinatorics,
-                      FP64 Newton residual and refined linear solves */
+    MA_MIXED = 1   /* FP32 piece integrals (from FP32 vertex positions), summed per cell in FP64;
+                      combinatorics still certified / exact.  ma_ot_solve iterates on these
+                      evaluations, then finishes on FP64 evaluations: its stopping test and
+                      result are those of the FP64 masses; the linear solves stay FP64 */
 } ma_precision;
 
 typedef enum ma_stop_rule {
@@ -98,6 +100,8 @@ typedef struct ma_profile {
     int64_t search[6];        /* stage-1 totals: tree nodes popped, node bounds tested, nodes
                                  pruned, candidate sites clipped against, clips that cut,
                                  final neighbours */
+    int64_t amg_fallbacks;    /* Newton solves whose multigrid setup met a coarse row beyond its
+                                 capacity and ran with the diagonal preconditioner */
 } ma_profile;
 /* enable != 0: reset the profile and start recording; 0: stop. */
 ma_status ma_ctx_profile(ma_ctx* ctx, int enable);
@@ -160,6 +164,8 @@ typedef struct ma_stats {
     double value;                /* Kantorovich value minus <nu, w> at exit */
     double t_eval_ms;            /* device time spent in Laguerre evaluations */
     double t_linsolve_ms;        /* device time spent in linear solves */
+    size_t neval_fp64;           /* evaluations with FP64 integrals (all of them unless precision
+                                    is MA_MIXED) */
 } ma_stats;
 
 void ma_solve_opts_default(ma_solve_opts* o);

@@ -27,7 +27,7 @@ class MaStats(ctypes.Structure):
     _fields_ = [("niter", ctypes.c_size_t), ("neval", ctypes.c_size_t), ("cg_iters", ctypes.c_size_t),
                 ("linesearch_halvings", ctypes.c_size_t), ("grad_norm", ctypes.c_double),
                 ("max_rel_err", ctypes.c_double), ("value", ctypes.c_double), ("t_eval_ms", ctypes.c_double),
-                ("t_linsolve_ms", ctypes.c_double)]
+                ("t_linsolve_ms", ctypes.c_double), ("neval_fp64", ctypes.c_size_t)]
 
 
 class MaProfile(ctypes.Structure):
@@ -36,7 +36,8 @@ class MaProfile(ctypes.Structure):
                 ("cells_large_ms", ctypes.c_double), ("cells_large_launches", ctypes.c_int64),
                 ("bounds_ms", ctypes.c_double), ("bounds_launches", ctypes.c_int64),
                 ("pcg_ms", ctypes.c_double), ("pcg_launches", ctypes.c_int64), ("pcg_iters", ctypes.c_int64),
-                ("large_sites", ctypes.c_int64), ("search", ctypes.c_int64 * 6)]
+                ("large_sites", ctypes.c_int64), ("search", ctypes.c_int64 * 6),
+                ("amg_fallbacks", ctypes.c_int64)]
 
 
 # every symbol include/ma.h declares, with its ctypes signature

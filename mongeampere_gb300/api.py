@@ -331,6 +331,7 @@ class Statistics:
     value: float = 0.0
     t_eval_ms: float = 0.0
     t_linsolve_ms: float = 0.0
+    neval_fp64: int = 0
     status: int = 0
 
 

@@ -362,7 +362,7 @@ __device__ __forceinline__ void restrict_level(const AmgPcgArgs& a, int l)
         double s = 0.0;
         if (J >= 0) {
             const int I0 = J * kAggSize, I1 = min(I0 + kAggSize, A.n);
-            if (t < I1 - I0) s = A.b[I0 + t];
+            for (int q = t; q < I1 - I0; q += T) s += A.b[I0 + q];
             for (int k = A.rp[I0] + t; k < A.rp[I1]; k += T) {
                 const int K = A.ci[k];
                 s -= A.va[k] * (kOmega * A.dinv[K] * A.b[K]);
@@ -725,9 +725,11 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     }
     c->launches += 1;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat + 8, c->cg_scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 6, G.flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaStreamSynchronize(s));
     if (iters) *iters = (int)c->hstat[8];
     c->profile.pcg_iters += (int64_t)c->hstat[8];
+    if (c->hinfo[6]) c->profile.amg_fallbacks++;
     if (relres) *relres = c->hstat[10] > 0 ? c->hstat[9] / c->hstat[10] : 0.0;
     return MA_OK;
 }

@@ -278,7 +278,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         a.pc_cnt = c->pc_cnt.as<int>();
         a.pv_cnt = c->pv_cnt.as<int>();
     }
-    const int mode = f.pieces ? 3 : (f.vjp ? 2 : (f.moments > 0 ? 1 : 0));
+    const int mode = f.pieces ? 3 : (f.vjp ? 2 : (f.moments > 0 ? 1 : (f.mixed ? 5 : 0)));
     launch_cells(c, m, a, 0, mode);
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -793,6 +793,7 @@ ma_status ma_kantorovich(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x
     if ((st = build_site_index(c, m, (int)n, dx, dy, dw)) != MA_OK) return st;
     EvalFlags f;
     f.hessian = true;
+    f.mixed = prec == MA_MIXED;
     if ((st = run_eval(c, m, (int)n, dw, f)) != MA_OK) return st;
     if ((st = copy_out(c, g, c->mass.as<double>(), (size_t)n, mem)) != MA_OK) return st;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->stat_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -599,6 +599,77 @@ MA_HD void integrate_labels(int n, const Lab& lab_of, const Nb64* nb, const Fixe
 }
 
 // ---------------------------------------------------------------------------
+// the mixed-precision integrals (FP32)
+// ---------------------------------------------------------------------------
+// FP32 vertex between edges prev and cur from the FP32 slot data (the values of
+// vtx_fixed_bis / vtx_bis_bis without their error radii)
+MA_HD void vtx32(int prev, int cur, const Slot* slots, const Fixed& fx, float& X, float& Y)
+{
+    if (prev < 0 && cur < 0) {
+        const int e = -1 - cur;
+        X = fx.ux[e];
+        Y = fx.uy[e];
+        return;
+    }
+    if (prev >= 0 && cur >= 0) {
+        const Slot a = slots[prev], b = slots[cur];
+        const float inv = 1.0f / (2.0f * (a.dx * b.dy - a.dy * b.dx));
+        X = (a.z * b.dy - b.z * a.dy) * inv;
+        Y = (a.dx * b.z - b.dx * a.z) * inv;
+        return;
+    }
+    const int e = (prev < 0) ? -1 - prev : -1 - cur;
+    const Slot a = slots[(prev < 0) ? cur : prev];
+    const int e1 = (e + 1 == fx.n) ? 0 : e + 1;
+    const float px = fx.ux[e], py = fx.uy[e];
+    const float ex = fx.ux[e1] - px, ey = fx.uy[e1] - py;
+    const float t = -(2.0f * (px * a.dx + py * a.dy) - a.z) / (2.0f * (ex * a.dx + ey * a.dy));
+    X = px + t * ex;
+    Y = py + t * ey;
+}
+
+// integrate_labels (mass, value part, Hessian edges; no moments) in FP32 from the
+// FP32 vertices; the caller sums the pieces of a cell in FP64.  Relative error of a
+// piece's integrals: a few FP32 roundings of the cell-relative coordinates.
+template <class Lab, class Edge>
+MA_HD void integrate_labels32(int n, const Lab& lab_of, const Slot* slots, const Fixed& fx, float c0, float gx,
+                              float gy, float& mass, float& second, const Edge& edge)
+{
+    float x0, y0;
+    vtx32(lab_of(n - 1), lab_of(0), slots, fx, x0, y0);
+    float ax = x0, ay = y0;
+    float m0 = 0, m1x = 0, m1y = 0, q2 = 0, c3x = 0, c3y = 0;
+    for (int k = 0; k < n; k++) {
+        const int lab = lab_of(k);
+        float bx, by;
+        if (k + 1 < n)
+            vtx32(lab, lab_of(k + 1), slots, fx, bx, by);
+        else {
+            bx = x0;
+            by = y0;
+        }
+        const float cr = ax * by - ay * bx;
+        const float aa = ax * ax + ay * ay, ab = ax * bx + ay * by, bb = bx * bx + by * by;
+        m0 += cr;
+        m1x += cr * (ax + bx);
+        m1y += cr * (ay + by);
+        q2 += cr * (aa + ab + bb);
+        const float ka = 3.0f * aa + 2.0f * ab + bb, kb = aa + 2.0f * ab + 3.0f * bb;
+        c3x += cr * (ax * ka + bx * kb);
+        c3y += cr * (ay * ka + by * kb);
+        if (lab >= 0) {
+            const Slot d = slots[lab];
+            const float crs = fabsf((bx - ax) * d.dy - (by - ay) * d.dx);
+            edge(k, lab, crs * (c0 + gx * 0.5f * (ax + bx) + gy * 0.5f * (ay + by)));
+        }
+        ax = bx;
+        ay = by;
+    }
+    mass = c0 * (m0 * 0.5f) + gx * (m1x * (1.0f / 6.0f)) + gy * (m1y * (1.0f / 6.0f));
+    second = c0 * (q2 * (1.0f / 12.0f)) + gx * (c3x * (1.0f / 60.0f)) + gy * (c3y * (1.0f / 60.0f));
+}
+
+// ---------------------------------------------------------------------------
 // adjoint of one piece
 // ---------------------------------------------------------------------------
 // Moments of the piece in owner-relative coordinates u = x - x_i (fan from the

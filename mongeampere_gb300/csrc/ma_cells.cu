@@ -665,7 +665,7 @@ struct CellInfo {
 
 // modes of k_pieces: the evaluation, the evaluation with moments, the adjoint, and
 // the two passes that materialise the pieces (count per cell, then emit)
-constexpr int kModeEval = 0, kModeMoments = 1, kModeVjp = 2, kModeCount = 3, kModeEmit = 4;
+constexpr int kModeEval = 0, kModeMoments = 1, kModeVjp = 2, kModeCount = 3, kModeEmit = 4, kModeMixed = 5;
 
 template <int MODE>
 struct PieceWarp {
@@ -881,6 +881,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
 {
     constexpr bool MOM = MODE == kModeMoments, VJP = MODE == kModeVjp;
     constexpr bool LISTING = MODE == kModeCount || MODE == kModeEmit;
+    constexpr bool MIXED = MODE == kModeMixed;
     constexpr int kAcc = PieceWarp<MODE>::kAcc;
     constexpr unsigned kFull = 0xffffffffu;
     __shared__ PieceWarp<MODE> shw[kPieceWarps];
@@ -1066,6 +1067,16 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                     W.out[2 % kAcc][p] = oy;
                     continue;
                 }
+                if (MIXED) {
+                    // FP32 integrals of the piece; the cell sums below are FP64
+                    float pm, ps;
+                    integrate_labels32(
+                        (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.slot + C.soff, T, (float)c0, (float)gx,
+                        (float)gy, pm, ps, [&](int e, int, float v) { W.hvc[e][p] = (double)v; });
+                    W.out[0][p] = (double)pm;
+                    W.out[1][p] = (double)ps;
+                    continue;
+                }
                 Acc acc{0, 0, 0, 0, 0, 0, 0};
                 integrate_labels<MOM>(
                     (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.nb + C.soff, T, c0, gx, gy, acc,
@@ -1190,6 +1201,10 @@ void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, int mode, cudaS
         k_pieces<kModeCount><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeEmit)
         k_pieces<kModeEmit><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeMixed)
+        k_pieces<kModeMixed><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeMixed)
+        k_pieces<kModeMixed><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeMoments)
         k_pieces<kModeMoments><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else

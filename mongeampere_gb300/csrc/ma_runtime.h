@@ -140,6 +140,8 @@ struct EvalFlags {
     bool hessian = true;
     const VjpArgs* vjp = nullptr;  // when set: the adjoint instead of the outputs
     bool pieces = false;           // materialise the pieces instead of the outputs
+    bool mixed = false;            // FP32 piece integrals (cell sums, predicates and vertices of
+                                   // the clip stay certified / FP64)
     int moments = 0;  // 0 none, 1 first, 2 second
     const double* nu = nullptr;  // when given, stat_out[0] = value - <nu, w>
     // Newton line-search trial: an empty cell already rejects the trial (its mass 0

@@ -449,12 +449,22 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    // mixed precision: evaluations with FP32 piece integrals until their residual
+    // meets the stopping rule, then FP64 evaluations (and FP64 Newton steps if the
+    // FP64 residual is not yet below it): the stopping test is always made on FP64
+    // masses
+    bool mixed_phase = o.precision == MA_MIXED;
+    // the FP32 integrals are good to about 1e-5 of a cell's mass: below this relative
+    // residual the mixed evaluations stop helping the Newton iteration
+    constexpr double kMixedFloor = 1e-4;
     auto timed_eval = [&](const double* wv, bool trial) -> ma_status {
         cudaEventRecord(e0, s);
         EvalFlags f;
         f.hessian = true;
         f.nu = dnu;
         f.abort_on_empty = trial;
+        f.mixed = mixed_phase;
+        if (!mixed_phase) S.neval_fp64++;
         ma_status r = run_eval(c, m, n, wv, f);
         if (r != MA_OK) return r;
         cudaEventRecord(e1, s);
@@ -500,7 +510,21 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
         }
         int64_t niter = 0;
         const double g0 = gn > 0 ? gn : 1.0;
-        while (!converged(gn, mr)) {
+        for (;;) {
+            if (converged(gn, mr) || (mixed_phase && mr <= kMixedFloor)) {
+                if (!mixed_phase) break;
+                // the mixed residual has converged: check (and finish) in FP64
+                mixed_phase = false;
+                if ((st = timed_eval(w, false)) != MA_OK) {
+                    result = st;
+                    break;
+                }
+                fx = c->hstat[0];
+                minm = c->hstat[2];
+                gn = c->hstat[3];
+                mr = c->hstat[4];
+                continue;
+            }
             if (niter > o.maxiter) {
                 result = MA_MAXITER;
                 break;
@@ -551,6 +575,20 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
                 if (alpha < 0x1p-40) break;
             }
             if (result != MA_OK) break;
+            if (!ok && mixed_phase) {
+                // the mixed residual is at its noise level: redo this step in FP64
+                mixed_phase = false;
+                MA_CUDA(c, cudaMemcpyAsync(w, c->w0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+                if ((st = timed_eval(w, false)) != MA_OK) {
+                    result = st;
+                    break;
+                }
+                fx = c->hstat[0];
+                minm = c->hstat[2];
+                gn = c->hstat[3];
+                mr = c->hstat[4];
+                continue;
+            }
             if (!ok) {
                 result = fail(c, MA_LINESEARCH_FAIL, "line search failed");
                 break;

@@ -117,3 +117,54 @@ def test_multigrid_laplacian_solve_with_empty_cells(ctx, oracle):
     d_ref[act] = spla.spsolve(H[act][:, act].tocsc(), rhs[act])
     assert np.all(d[empty] == 0.0) and d[-1] == 0.0
     np.testing.assert_allclose(d, d_ref, rtol=0, atol=1e-9 * np.abs(d_ref).max())
+
+
+def test_mixed_precision_evaluation_error(ctx):
+    # FP32 piece integrals, FP64 cell sums: the error against the FP64 evaluation
+    from mongeampere_gb300 import api
+    p = W.make_problem(128, 20000, "gauss", "uniform", "random", seed=9)
+    X = np.c_[p.x, p.y]
+    w = np.zeros(p.n)
+    v64, g64, h64 = api.kantorovich(p.mesh, X, w, ctx=ctx)
+    v32, g32, h32 = api.kantorovich(p.mesh, X, w, precision="mixed", ctx=ctx)
+    rel = np.abs(np.asarray(g32) - np.asarray(g64)) / np.asarray(g64)
+    assert rel.max() < 2e-5 and np.median(rel) < 1e-6
+    assert abs(v32 - v64) <= 1e-6 * abs(v64)
+    np.testing.assert_array_equal(h32.col, h64.col)  # same combinatorics
+    np.testing.assert_allclose(h32.val, h64.val, rtol=1e-4, atol=1e-6 * np.abs(h64.val).max())
+
+
+def test_mixed_precision_solve_meets_fp64_tolerance(ctx, oracle):
+    # the mixed solve stops on FP64 masses: same tolerance, few FP64 evaluations
+    from mongeampere_gb300 import api
+    p = W.make_problem(96, 8000, "gauss", "uniform", "random", seed=10)
+    X = np.c_[p.x, p.y]
+    st_m, st_d = api.Statistics(), api.Statistics()
+    w_m = api.ot_solve(p.mesh, X, p.nu, eps_g=1e-6, stop="rel", precision="mixed", stats=st_m, ctx=ctx)
+    w_d = api.ot_solve(p.mesh, X, p.nu, eps_g=1e-6, stop="rel", stats=st_d, ctx=ctx)
+    assert st_m.max_rel_err <= 1e-6 and st_d.max_rel_err <= 1e-6
+    assert 1 <= st_m.neval_fp64 <= 6 and st_m.neval_fp64 < st_m.neval
+    assert st_d.neval_fp64 == st_d.neval
+    # the oracle's masses at the mixed solution
+    r = oracle.kantorovich(p.mesh, p.x, p.y, np.asarray(w_m), arith="fp64", ring=1)
+    assert np.max(np.abs(r.g - p.nu) / p.nu) <= 1.5e-6
+    del w_d
+
+
+def test_multigrid_at_one_million_sites(ctx):
+    # levels wider than the launched grid: coarse rows get teams of fewer than four
+    # lanes (every member of an aggregate must still be restricted)
+    import torch
+    from mongeampere_gb300 import api
+    p = W.make_problem(1024, 1_000_000, "uniform", "uniform", "equal", seed=0)
+    dev = torch.device("cuda", 0)
+    X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
+    _, g, h = api.kantorovich(p.mesh, X, torch.zeros(p.n, dtype=torch.float64, device=dev), ctx=ctx)
+    rhs = g - torch.tensor(p.nu, device=dev)
+    d, it = api.solve_laplacian_matrix(rhs, rtol=1e-8, maxiter=1000, ctx=ctx)
+    H = h.to_scipy().tocsr()
+    r = rhs.cpu().numpy().copy()
+    r[-1] = 0
+    res = (H @ d.cpu().numpy() - r)[:-1]
+    assert np.linalg.norm(res) <= 1e-7 * np.linalg.norm(r)
+    assert it < 400
