@@ -162,6 +162,75 @@ def run_reference(args, rank):
     print(json.dumps(line))
 
 
+def run_c3(args, ctx, dev, rank):
+    """Mixed precision against FP64 at 1M sites: (a) complete Laguerre evaluations of the
+    clustered 1M-site / 2048^2 workload (workloads.c3) at w = 0 -- evaluations/s and the
+    mixed form's mass and Hessian errors against the FP64 form; (b) one OT solve to max
+    relative mass error 1e-6 of 1M uniform sites on the same density (the clustered
+    sites stall the reference's damped Newton from w = 0: every step is cut to 2^-11 to
+    keep all cells non-empty), wall clock of each form and the FP64-evaluated error."""
+    import numpy as np
+    import torch
+
+    from mongeampere_gb300 import api
+    from mongeampere_gb300 import workloads as W
+    out = {"metric": METRIC, "workload": "c3", "n_gpus": 1}
+    p = W.c3(0)
+    dm = ctx.mesh(p.mesh)
+    X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
+    w = torch.zeros(p.n, dtype=torch.float64, device=dev)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        for _ in range(args.warmup):
+            api.kantorovich(dm, X, w, precision=prec, ctx=ctx)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            v, g, h = api.kantorovich(dm, X, w, precision=prec, ctx=ctx)
+        e1.record()
+        torch.cuda.synchronize()
+        res[prec] = (args.steps / (e0.elapsed_time(e1) * 1e-3), v, g.cpu().numpy(), h)
+    g64, g32 = res["fp64"][2], res["mixed"][2]
+    rel = np.abs(g32 - g64) / np.maximum(g64, 1e-300)
+    h64, h32 = res["fp64"][3], res["mixed"][3]
+    hrel = np.abs(h32.val - h64.val) / np.maximum(np.abs(h64.val), 1e-300)
+    out["evaluations"] = {
+        "config": "1,000,000 sites (70% in 20 Gaussian blobs), 2048^2 grid U[0.5,1.5], w = 0, masses + value + CSR Hessian",
+        "fp64_evals_per_s": res["fp64"][0], "mixed_evals_per_s": res["mixed"][0],
+        "mixed_mass_rel_err_max": float(rel.max()), "mixed_mass_rel_err_median": float(np.median(rel)),
+        "mixed_value_rel_err": float(abs(res["mixed"][1] - res["fp64"][1]) / abs(res["fp64"][1])),
+        "mixed_hessian_rel_err_max": float(hrel.max()), "same_sparsity": bool(np.array_equal(h32.col, h64.col))}
+    q = W.make_problem(2048, 1_000_000, "uniform", "uniform", "equal", seed=0)
+    dq = ctx.mesh(q.mesh)
+    xq = torch.tensor(q.x, device=dev)
+    yq = torch.tensor(q.y, device=dev)
+    nq = torch.tensor(q.nu, device=dev)
+    solves = {}
+    for prec in ("fp64", "mixed"):
+        times = []
+        for k in range(max(1, args.steps // 2) + 1):
+            wq = torch.zeros(q.n, dtype=torch.float64, device=dev)
+            st = api.Statistics()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            api.ot_solve(dq, xq, nq, x=wq, y=yq, eps_g=1e-6, stop="rel", precision=prec, stats=st, ctx=ctx)
+            e1.record()
+            torch.cuda.synchronize()
+            if k > 0:
+                times.append(e0.elapsed_time(e1) * 1e-3)
+        v, g, _ = api.kantorovich(dq, torch.stack([xq, yq], 1), wq, ctx=ctx)
+        err = float(np.max(np.abs(g.cpu().numpy() - q.nu) / q.nu))
+        solves[prec] = {"s_per_solve": float(np.median(times)), "newton_iters": st.niter, "evals": st.neval,
+                        "fp64_evals": st.neval_fp64, "cg_iters": st.cg_iters, "max_rel_err_fp64": err}
+    out["solve_1M_uniform"] = {
+        "config": "1,000,000 uniform sites, 2048^2 grid U[0.5,1.5], equal masses, from w = 0 to max rel mass err 1e-6",
+        **solves, "mixed_speedup": solves["fp64"]["s_per_solve"] / solves["mixed"]["s_per_solve"]}
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -175,6 +244,9 @@ def main():
                          "solution weights and print per-kernel device times (no benchmark line)")
     ap.add_argument("--profile-solve", action="store_true",
                     help="profiling driver: one solve with per-kernel device times (no benchmark line)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
+                    help="c3: the 1M-site mixed-precision comparison (evaluations of the clustered "
+                         "1M-site / 2048^2 workload, and a 1M-uniform-site solve), one JSON line")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -201,6 +273,9 @@ def main():
     dev = torch.device("cuda", local)
     ctx = api.Context(local)
     ctx.use_torch_stream()
+    if args.workload == "c3":
+        run_c3(args, ctx, dev, rank)
+        return
     # weak scaling: every rank solves its own problem (replicas; the solve has no
     # data-path exchange)
     p = W.c2(rank)

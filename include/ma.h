@@ -142,6 +142,14 @@ typedef enum ma_precond {
     MA_PRECOND_JACOBI = 1     /* diagonal scaling */
 } ma_precond;
 
+typedef enum ma_init {
+    MA_INIT_GIVEN = 0,      /* start from w_inout (the reference's behaviour; zeros = its empty start) */
+    MA_INIT_MULTISCALE = 1  /* coarse-to-fine initial guess: sites aggregated by 8 in Morton order
+                               down to ~4,000, each level solved to 1e-2 relative from its parent's
+                               weights (no counterpart in the reference, whose ot_solve takes the
+                               initial guess as an argument); for clustered sites far from equilibrium */
+} ma_init;
+
 typedef struct ma_solve_opts {
     double eps_g;          /* stop threshold (reference default 1e-7) */
     int64_t maxiter;       /* Newton iterations (reference default 100) */
@@ -152,6 +160,7 @@ typedef struct ma_solve_opts {
                               min(1e-3, max(1e-12, 0.1 |g| / |g0|)) at each step */
     int64_t cg_maxiter;    /* CG iteration cap (0: default 20000) */
     int precond;           /* ma_precond: CG preconditioner of the Newton step */
+    int init;              /* ma_init: initial guess */
 } ma_solve_opts;
 
 typedef struct ma_stats {

@@ -20,7 +20,7 @@ _vp = ctypes.c_void_p
 class MaSolveOpts(ctypes.Structure):
     _fields_ = [("eps_g", ctypes.c_double), ("maxiter", ctypes.c_int64), ("stop_rule", ctypes.c_int),
                 ("precision", ctypes.c_int), ("verbose", ctypes.c_int), ("cg_rtol", ctypes.c_double),
-                ("cg_maxiter", ctypes.c_int64), ("precond", ctypes.c_int)]
+                ("cg_maxiter", ctypes.c_int64), ("precond", ctypes.c_int), ("init", ctypes.c_int)]
 
 
 class MaStats(ctypes.Structure):
@@ -125,3 +125,5 @@ MA_STOP_GRAD_NORM = 0
 MA_STOP_MAX_REL = 1
 MA_PRECOND_MULTIGRID = 0
 MA_PRECOND_JACOBI = 1
+MA_INIT_GIVEN = 0
+MA_INIT_MULTISCALE = 1

@@ -337,12 +337,13 @@ class Statistics:
 
 def ot_solve(mesh, X, masses, x=None, eps_g: float = 1e-7, maxiter: int = 100, verbose: bool = False,
              stats: Statistics | None = None, *, y=None, stop: str = "grad", precision: str = "fp64",
-             cg_rtol: float = 0.0, cg_maxiter: int = 0, precond: str = "multigrid", ctx: Context | None = None,
-             raise_on_error: bool = True):
+             cg_rtol: float = 0.0, cg_maxiter: int = 0, precond: str = "multigrid", init: str = "given",
+             ctx: Context | None = None, raise_on_error: bool = True):
     """``MA::ot_solve``.  Returns the weights (``x`` is the initial guess; ``None``
     or a wrong-sized array starts from zero like the reference).  ``stop="rel"``
     uses ``max_i |m_i - nu_i| / nu_i <= eps_g`` instead of ``|m - nu|_2 < eps_g``.
-    ``precond`` is the CG preconditioner of the Newton step: "multigrid" or "jacobi"."""
+    ``precond`` is the CG preconditioner of the Newton step: "multigrid" or "jacobi".
+    ``init="multiscale"`` replaces the initial guess by a coarse-to-fine one."""
     ctx = ctx or default_context()
     dm = _dmesh(ctx, mesh)
     xs, ys = _split_xy(X, y)
@@ -370,6 +371,9 @@ def ot_solve(mesh, X, masses, x=None, eps_g: float = 1e-7, maxiter: int = 100, v
     if precond not in ("multigrid", "jacobi"):
         raise ValueError("precond must be 'multigrid' or 'jacobi'")
     o.precond = L.MA_PRECOND_JACOBI if precond == "jacobi" else L.MA_PRECOND_MULTIGRID
+    if init not in ("given", "multiscale"):
+        raise ValueError("init must be 'given' or 'multiscale'")
+    o.init = L.MA_INIT_MULTISCALE if init == "multiscale" else L.MA_INIT_GIVEN
     s = L.MaStats()
     st = ctx.lib.ma_ot_solve(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], wp, a.mem, ctypes.byref(o),
                              ctypes.byref(s))

@@ -470,7 +470,8 @@ void ma_ctx_destroy(ma_ctx* c)
                       &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,
                       &c->st_col, &c->st_val, &c->rowptr, &c->col, &c->val, &c->status, &c->redo, &c->nredo,
                       &c->stat_partial, &c->stat_out, &c->info, &c->big_index, &c->big_col, &c->big_val, &c->big_work, &c->wcur, &c->w0, &c->dirn, &c->g, &c->cg_r,
-                      &c->cg_z, &c->cg_p, &c->cg_q, &c->cg_dinv, &c->cg_scal, &c->cg_part};
+                      &c->cg_z, &c->cg_p, &c->cg_q, &c->cg_dinv, &c->cg_scal, &c->cg_part,
+                      &c->ms_x, &c->ms_y, &c->ms_nu, &c->ms_w};
     for (DevBuf* b : bufs) b->release();
     for (AmgBuf& l : c->amg.lev) {
         DevBuf* lb[] = {&l.rp, &l.ci, &l.va, &l.dinv, &l.b, &l.xp};

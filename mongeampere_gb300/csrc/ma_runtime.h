@@ -103,6 +103,7 @@ struct Ctx {
     bool have_h = false;
     // solver work vectors
     DevBuf wcur, w0, dirn, g, cg_r, cg_z, cg_p, cg_q, cg_dinv, cg_scal, cg_part;
+    DevBuf ms_x, ms_y, ms_nu, ms_w;  // a coarse level of the multiscale initial guess
     Amg amg;
     // profiling (CUDA events around the main kernels)
     bool prof = false;

@@ -12,9 +12,12 @@
 //   * stop when |g|_2 < eps_g (:150), or max_i |g_i| / nu_i <= eps_g.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "ma_runtime.h"
 
@@ -305,6 +308,365 @@ static ma_status static_setup(int dev, StaticSetup* out)
 
 using namespace ma;
 
+// The Newton iteration of MA::ot_solve on one set of sites (device arrays; w in/out).
+static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, const double* dy, const double* dnu,
+                             double* w, const ma_solve_opts& o, ma_stats& S)
+{
+    cudaStream_t s = c->stream;
+    const bool adaptive = !(o.cg_rtol > 0);
+    MA_CUDA(c, c->w0.ensure(sizeof(double) * n));
+    MA_CUDA(c, c->dirn.ensure(sizeof(double) * n));
+    MA_CUDA(c, c->g.ensure(sizeof(double) * n));
+    ma_status st = build_site_index(c, m, n, dx, dy, w);
+    if (st != MA_OK) return st;
+
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    // mixed precision: evaluations with FP32 piece integrals until their residual
+    // meets the stopping rule, then FP64 evaluations (and FP64 Newton steps if the
+    // FP64 residual is not yet below it): the stopping test is always made on FP64
+    // masses
+    bool mixed_phase = o.precision == MA_MIXED;
+    // The FP32 integrals leave a noise of 1e-5 to 1e-4 of a cell's mass in the masses
+    // (measured up to 3e-4 max-relative at 1M sites): from this relative residual on,
+    // where only the quadratically convergent last steps remain, the evaluations are
+    // FP64; a mixed line search that has to cut the step below kMixedMinStep is also
+    // taken as the noise floor and redone in FP64.
+    constexpr double kMixedFloor = 1e-2;
+    constexpr double kMixedMinStep = 1.0 / 64.0;
+    auto timed_eval = [&](const double* wv, bool trial) -> ma_status {
+        cudaEventRecord(e0, s);
+        EvalFlags f;
+        f.hessian = true;
+        f.nu = dnu;
+        f.abort_on_empty = trial;
+        f.mixed = mixed_phase;
+        if (!mixed_phase) S.neval_fp64++;
+        ma_status r = run_eval(c, m, n, wv, f);
+        if (r != MA_OK) return r;
+        cudaEventRecord(e1, s);
+        if (c->aborted) {
+            // value, -, min mass, |g|, max rel: the trial is rejected on its min mass
+            c->hstat[0] = NAN;
+            c->hstat[2] = 0.0;
+            c->hstat[3] = INFINITY;
+            c->hstat[4] = INFINITY;
+        } else {
+            MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->stat_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        MA_CUDA(c, cudaStreamSynchronize(s));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        S.t_eval_ms += ms;
+        S.neval++;
+        return MA_OK;
+    };
+    auto converged = [&](double gn, double mr) {
+        return o.stop_rule == MA_STOP_MAX_REL ? (mr <= o.eps_g) : (gn < o.eps_g);
+    };
+
+    ma_status result = MA_OK;
+    MA_CUDA(c, c->cg_scal.ensure(sizeof(double) * 8));
+    k_min_nu<<<1, 256, 0, s>>>(dnu, n, c->cg_scal.as<double>() + 7);
+    c->launches += 1;
+    MA_CUDA(c, cudaMemcpyAsync(c->hstat + 15, c->cg_scal.as<double>() + 7, sizeof(double), cudaMemcpyDeviceToHost, s));
+    if ((st = timed_eval(w, false)) != MA_OK) {
+        result = st;
+        goto core_done;
+    }
+    {
+        double fx = c->hstat[0], minm = c->hstat[2], gn = c->hstat[3], mr = c->hstat[4];
+        double minnu = c->hstat[15];
+        double eps0 = std::fmin(minm, minnu) / 2.0;
+        if (!(eps0 > 0)) {
+            result = fail(c, MA_EMPTY_CELL, "computed minimum mass is non-positive: a Laguerre cell is empty");
+            S.grad_norm = gn;
+            S.max_rel_err = mr;
+            S.value = fx;
+            goto core_done;
+        }
+        int64_t niter = 0;
+        const double g0 = gn > 0 ? gn : 1.0;
+        for (;;) {
+            if (converged(gn, mr) || (mixed_phase && mr <= kMixedFloor)) {
+                if (!mixed_phase) break;
+                // the mixed residual has converged: check (and finish) in FP64
+                mixed_phase = false;
+                if ((st = timed_eval(w, false)) != MA_OK) {
+                    result = st;
+                    break;
+                }
+                fx = c->hstat[0];
+                minm = c->hstat[2];
+                gn = c->hstat[3];
+                mr = c->hstat[4];
+                continue;
+            }
+            if (niter > o.maxiter) {
+                result = MA_MAXITER;
+                break;
+            }
+            niter++;
+            // Newton direction: d = -H_s^{-1} g_s
+            k_grad<<<(n + 255) / 256, 256, 0, s>>>(c->mass.as<double>(), dnu, n, c->g.as<double>());
+            c->launches += 1;
+            cudaEventRecord(e0, s);
+            int it = 0;
+            double rr = 0;
+            // inexact Newton: the linear solve only needs to beat the current residual
+            double rtol = adaptive ? std::fmin(1e-3, std::fmax(1e-12, 0.1 * gn / g0)) : o.cg_rtol;
+            if ((st = pcg_solve(c, n, c->g.as<double>(), c->dirn.as<double>(), rtol, (int)o.cg_maxiter, &it,
+                                &rr, o.precond)) != MA_OK) {
+                result = st;
+                break;
+            }
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            S.t_linsolve_ms += ms;
+            S.cg_iters += it;
+            MA_CUDA(c, cudaMemcpyAsync(c->w0.p, w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            double alpha = 1.0, n0 = gn;
+            bool ok = false;
+            while (true) {
+                // w = w0 - alpha * solution
+                k_axpy_to<<<(n + 255) / 256, 256, 0, s>>>(c->w0.as<double>(), c->dirn.as<double>(), -alpha, n, w);
+                c->launches += 1;
+                if ((st = timed_eval(w, true)) != MA_OK) {
+                    result = st;
+                    break;
+                }
+                fx = c->hstat[0];
+                minm = c->hstat[2];
+                gn = c->hstat[3];
+                mr = c->hstat[4];
+                if (minm >= eps0 && gn <= (1.0 - alpha / 2.0) * n0) {
+                    ok = true;
+                    break;
+                }
+                alpha *= 0.5;
+                S.linesearch_halvings++;
+                if (mixed_phase && alpha < kMixedMinStep) break;
+                if (o.verbose)
+                    fprintf(stderr, "subit %lld: min(masses)=%.17g\n", (long long)niter, minm);
+                if (alpha < 0x1p-40) break;
+            }
+            if (result != MA_OK) break;
+            if (!ok && mixed_phase) {
+                // the mixed residual is at its noise level: redo this step in FP64
+                mixed_phase = false;
+                MA_CUDA(c, cudaMemcpyAsync(w, c->w0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+                if ((st = timed_eval(w, false)) != MA_OK) {
+                    result = st;
+                    break;
+                }
+                fx = c->hstat[0];
+                minm = c->hstat[2];
+                gn = c->hstat[3];
+                mr = c->hstat[4];
+                continue;
+            }
+            if (!ok) {
+                result = fail(c, MA_LINESEARCH_FAIL, "line search failed");
+                break;
+            }
+            if (o.verbose)
+                fprintf(stderr, "it %lld: f=%.17g |df|=%.17g max_rel=%.3g tau=%g eval=%zu cg=%d\n", (long long)niter, fx,
+                        gn, mr, alpha, S.neval, it);
+        }
+        S.niter = (size_t)niter;
+        S.grad_norm = gn;
+        S.max_rel_err = mr;
+        S.value = fx;
+    }
+core_done:
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return result;
+}
+
+// ---------------------------------------------------------------------------
+// multiscale initial guess (Merigot, "A multiscale approach to optimal transport",
+// 2011): the sites are coarsened by groups of kMsGroup consecutive sites in Morton
+// order (nu-weighted centroid, summed target mass) down to about kMsCoarse sites;
+// the coarsest problem is solved from w = 0, and each finer level starts from
+//     w_i = w_c + 2 (x_i - x_c) . (x_c - z_c)
+// (c the parent of i, z_c the rho-centroid of c's Laguerre cell at the coarse
+// solution): within a group the power diagram is the group's Voronoi diagram moved
+// by z_c - x_c, i.e. placed where the parent's cell is (for clustered sites the
+// cells lie far from their sites).  The guess is scaled back towards 0 while a cell
+// would be empty; each level is solved to kMsLevelTol before the finest is solved to
+// the caller's tolerance.  The Newton iteration on every level is the reference's;
+// only the initial guess of the finest one changes, which MA::ot_solve takes as an
+// argument.
+// ---------------------------------------------------------------------------
+constexpr int kMsGroup = 8;
+constexpr int kMsCoarse = 4000;
+constexpr double kMsLevelTol = 1e-2;
+
+static uint64_t morton2(double x, double y, double x0, double y0, double sx, double sy)
+{
+    auto spread = [](uint64_t v) {
+        v &= 0xFFFFFull;
+        v = (v | (v << 16)) & 0x0000FFFF0000FFFFull;
+        v = (v | (v << 8)) & 0x00FF00FF00FF00FFull;
+        v = (v | (v << 4)) & 0x0F0F0F0F0F0F0F0Full;
+        v = (v | (v << 2)) & 0x3333333333333333ull;
+        v = (v | (v << 1)) & 0x5555555555555555ull;
+        return v;
+    };
+    const double fx = std::min(std::max((x - x0) * sx, 0.0), 1048575.0);
+    const double fy = std::min(std::max((y - y0) * sy, 0.0), 1048575.0);
+    return spread((uint64_t)fx) | (spread((uint64_t)fy) << 1);
+}
+
+struct MsLevel {
+    std::vector<double> x, y, nu;
+    std::vector<int> parent;  // aggregate (site of the next coarser level) of each site
+};
+
+// has the evaluation at w an empty cell?  (a cheap evaluation that stops at the first)
+static ma_status has_empty_cell(Ctx* c, const Mesh* m, int n, const double* w, bool* empty)
+{
+    EvalFlags f;
+    f.hessian = true;
+    f.abort_on_empty = true;
+    ma_status st = run_eval(c, m, n, w, f);
+    if (st != MA_OK) return st;
+    *empty = c->aborted;
+    return MA_OK;
+}
+
+static ma_status multiscale_solve(Ctx* c, const Mesh* m, int n, const double* dx, const double* dy,
+                                  const double* dnu, double* w, const ma_solve_opts& o, ma_stats& S)
+{
+    cudaStream_t s = c->stream;
+    std::vector<MsLevel> L(1);
+    L[0].x.resize(n);
+    L[0].y.resize(n);
+    L[0].nu.resize(n);
+    MA_CUDA(c, cudaMemcpyAsync(L[0].x.data(), dx, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaMemcpyAsync(L[0].y.data(), dy, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaMemcpyAsync(L[0].nu.data(), dnu, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaStreamSynchronize(s));
+    while ((int)L.back().x.size() > kMsCoarse) {
+        MsLevel& f = L.back();
+        const size_t nf = f.x.size();
+        double x0 = f.x[0], x1 = f.x[0], y0 = f.y[0], y1 = f.y[0];
+        for (size_t i = 0; i < nf; i++) {
+            x0 = std::min(x0, f.x[i]);
+            x1 = std::max(x1, f.x[i]);
+            y0 = std::min(y0, f.y[i]);
+            y1 = std::max(y1, f.y[i]);
+        }
+        const double sx = x1 > x0 ? 1048576.0 / (x1 - x0) : 0.0, sy = y1 > y0 ? 1048576.0 / (y1 - y0) : 0.0;
+        std::vector<std::pair<uint64_t, int>> key(nf);
+        for (size_t i = 0; i < nf; i++) key[i] = {morton2(f.x[i], f.y[i], x0, y0, sx, sy), (int)i};
+        std::sort(key.begin(), key.end());
+        const size_t nc = (nf + kMsGroup - 1) / kMsGroup;
+        MsLevel cl;
+        cl.x.assign(nc, 0.0);
+        cl.y.assign(nc, 0.0);
+        cl.nu.assign(nc, 0.0);
+        f.parent.assign(nf, 0);
+        for (size_t r = 0; r < nf; r++) {
+            const int i = key[r].second, J = (int)(r / kMsGroup);
+            f.parent[i] = J;
+            cl.x[J] += f.nu[i] * f.x[i];
+            cl.y[J] += f.nu[i] * f.y[i];
+            cl.nu[J] += f.nu[i];
+        }
+        for (size_t J = 0; J < nc; J++) {
+            cl.x[J] /= cl.nu[J];
+            cl.y[J] /= cl.nu[J];
+        }
+        L.push_back(std::move(cl));
+    }
+    std::vector<double> wl(L.back().x.size(), 0.0);
+    for (int l = (int)L.size() - 1; l >= 0; l--) {
+        const int nl = (int)L[l].x.size();
+        const double *lx = dx, *ly = dy, *lnu = dnu;
+        double* lw = w;
+        if (l > 0) {
+            MA_CUDA(c, c->ms_x.ensure(sizeof(double) * nl));
+            MA_CUDA(c, c->ms_y.ensure(sizeof(double) * nl));
+            MA_CUDA(c, c->ms_nu.ensure(sizeof(double) * nl));
+            MA_CUDA(c, c->ms_w.ensure(sizeof(double) * nl));
+            MA_CUDA(c, cudaMemcpyAsync(c->ms_x.p, L[l].x.data(), sizeof(double) * nl, cudaMemcpyHostToDevice, s));
+            MA_CUDA(c, cudaMemcpyAsync(c->ms_y.p, L[l].y.data(), sizeof(double) * nl, cudaMemcpyHostToDevice, s));
+            MA_CUDA(c, cudaMemcpyAsync(c->ms_nu.p, L[l].nu.data(), sizeof(double) * nl, cudaMemcpyHostToDevice, s));
+            lx = c->ms_x.as<double>();
+            ly = c->ms_y.as<double>();
+            lnu = c->ms_nu.as<double>();
+            lw = c->ms_w.as<double>();
+        }
+        // the initial guess: the prolonged weights, scaled towards 0 while a cell is empty
+        std::vector<double> wt(nl);
+        double t = 1.0;
+        for (int tries = 0;; tries++) {
+            for (int i = 0; i < nl; i++) wt[i] = t * wl[i];
+            MA_CUDA(c, cudaMemcpyAsync(lw, wt.data(), sizeof(double) * nl, cudaMemcpyHostToDevice, s));
+            MA_CUDA(c, cudaStreamSynchronize(s));
+            if (t == 0.0) break;
+            ma_status st = build_site_index(c, m, nl, lx, ly, lw);
+            if (st != MA_OK) return st;
+            bool empty = false;
+            if ((st = has_empty_cell(c, m, nl, lw, &empty)) != MA_OK) return st;
+            if (!empty) break;
+            t = tries < 12 ? 0.5 * t : 0.0;
+        }
+        ma_solve_opts ol = o;
+        if (l > 0) {
+            ol.stop_rule = MA_STOP_MAX_REL;
+            ol.eps_g = kMsLevelTol;
+            ol.verbose = 0;
+        }
+        ma_stats Sl{};
+        ma_status st = newton_core(c, m, nl, lx, ly, lnu, lw, ol, Sl);
+        if (o.verbose)
+            fprintf(stderr, "multiscale level %d: %d sites, guess scale %g, status %d, %zu Newton steps, max_rel %.3g\n",
+                    l, nl, t, (int)st, Sl.niter, Sl.max_rel_err);
+        S.niter += Sl.niter;
+        S.neval += Sl.neval;
+        S.neval_fp64 += Sl.neval_fp64;
+        S.cg_iters += Sl.cg_iters;
+        S.linesearch_halvings += Sl.linesearch_halvings;
+        S.t_eval_ms += Sl.t_eval_ms;
+        S.t_linsolve_ms += Sl.t_linsolve_ms;
+        S.grad_norm = Sl.grad_norm;
+        S.max_rel_err = Sl.max_rel_err;
+        S.value = Sl.value;
+        if (l == 0) return st;
+        if (st != MA_OK && st != MA_MAXITER) return st;
+        // the coarse solution and the centroids of its cells
+        std::vector<double> wc(nl), mo(6 * (size_t)nl);
+        {
+            EvalFlags f;
+            f.hessian = false;
+            f.moments = 1;
+            if ((st = build_site_index(c, m, nl, lx, ly, lw)) != MA_OK) return st;
+            if ((st = run_eval(c, m, nl, lw, f)) != MA_OK) return st;
+        }
+        MA_CUDA(c, cudaMemcpyAsync(wc.data(), lw, sizeof(double) * nl, cudaMemcpyDeviceToHost, s));
+        MA_CUDA(c, cudaMemcpyAsync(mo.data(), c->mom.p, sizeof(double) * 6 * nl, cudaMemcpyDeviceToHost, s));
+        MA_CUDA(c, cudaStreamSynchronize(s));
+        const MsLevel& F = L[l - 1];
+        const MsLevel& Cl = L[l];
+        const std::vector<int>& par = F.parent;
+        wl.assign(par.size(), 0.0);
+        for (size_t i = 0; i < par.size(); i++) {
+            const int J = par[i];
+            const double mJ = mo[6 * (size_t)J];
+            const double zx = mJ > 0 ? mo[6 * (size_t)J + 1] / mJ : Cl.x[J];
+            const double zy = mJ > 0 ? mo[6 * (size_t)J + 2] / mJ : Cl.y[J];
+            wl[i] = wc[J] + 2.0 * ((F.x[i] - Cl.x[J]) * (Cl.x[J] - zx) + (F.y[i] - Cl.y[J]) * (Cl.y[J] - zy));
+        }
+    }
+    return MA_OK;
+}
+
 extern "C" {
 
 ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
@@ -377,6 +739,7 @@ void ma_solve_opts_default(ma_solve_opts* o)
     o->cg_rtol = 0.0;  // adaptive forcing
     o->cg_maxiter = 20000;
     o->precond = MA_PRECOND_MULTIGRID;
+    o->init = MA_INIT_GIVEN;
 }
 
 ma_status ma_laplacian_solve(ma_ctx* cp, const double* g, double* d, ma_mem mem, double rtol, int64_t maxiter,
@@ -417,7 +780,6 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     ma_solve_opts o;
     ma_solve_opts_default(&o);
     if (opts) o = *opts;
-    const bool adaptive = !(o.cg_rtol > 0);
     if (o.cg_maxiter <= 0) o.cg_maxiter = 20000;
     const int n = (int)n64;
     cudaSetDevice(c->device);
@@ -437,174 +799,11 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
         dnu = c->hnu.as<double>();
     }
     MA_CUDA(c, c->wcur.ensure(sizeof(double) * n));
-    MA_CUDA(c, c->w0.ensure(sizeof(double) * n));
-    MA_CUDA(c, c->dirn.ensure(sizeof(double) * n));
-    MA_CUDA(c, c->g.ensure(sizeof(double) * n));
     double* w = c->wcur.as<double>();
     MA_CUDA(c, cudaMemcpyAsync(w, w_inout, sizeof(double) * n,
                                mem == MA_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
-    ma_status st = build_site_index(c, m, n, dx, dy, w);
-    if (st != MA_OK) return st;
-
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    // mixed precision: evaluations with FP32 piece integrals until their residual
-    // meets the stopping rule, then FP64 evaluations (and FP64 Newton steps if the
-    // FP64 residual is not yet below it): the stopping test is always made on FP64
-    // masses
-    bool mixed_phase = o.precision == MA_MIXED;
-    // the FP32 integrals are good to about 1e-5 of a cell's mass: below this relative
-    // residual the mixed evaluations stop helping the Newton iteration
-    constexpr double kMixedFloor = 1e-4;
-    auto timed_eval = [&](const double* wv, bool trial) -> ma_status {
-        cudaEventRecord(e0, s);
-        EvalFlags f;
-        f.hessian = true;
-        f.nu = dnu;
-        f.abort_on_empty = trial;
-        f.mixed = mixed_phase;
-        if (!mixed_phase) S.neval_fp64++;
-        ma_status r = run_eval(c, m, n, wv, f);
-        if (r != MA_OK) return r;
-        cudaEventRecord(e1, s);
-        if (c->aborted) {
-            // value, -, min mass, |g|, max rel: the trial is rejected on its min mass
-            c->hstat[0] = NAN;
-            c->hstat[2] = 0.0;
-            c->hstat[3] = INFINITY;
-            c->hstat[4] = INFINITY;
-        } else {
-            MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->stat_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
-        }
-        MA_CUDA(c, cudaStreamSynchronize(s));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        S.t_eval_ms += ms;
-        S.neval++;
-        return MA_OK;
-    };
-    auto converged = [&](double gn, double mr) {
-        return o.stop_rule == MA_STOP_MAX_REL ? (mr <= o.eps_g) : (gn < o.eps_g);
-    };
-
-    ma_status result = MA_OK;
-    MA_CUDA(c, c->cg_scal.ensure(sizeof(double) * 8));
-    k_min_nu<<<1, 256, 0, s>>>(dnu, n, c->cg_scal.as<double>() + 7);
-    c->launches += 1;
-    MA_CUDA(c, cudaMemcpyAsync(c->hstat + 15, c->cg_scal.as<double>() + 7, sizeof(double), cudaMemcpyDeviceToHost, s));
-    if ((st = timed_eval(w, false)) != MA_OK) {
-        result = st;
-        goto done;
-    }
-    {
-        double fx = c->hstat[0], minm = c->hstat[2], gn = c->hstat[3], mr = c->hstat[4];
-        double minnu = c->hstat[15];
-        double eps0 = std::fmin(minm, minnu) / 2.0;
-        if (!(eps0 > 0)) {
-            result = fail(c, MA_EMPTY_CELL, "computed minimum mass is non-positive: a Laguerre cell is empty");
-            S.grad_norm = gn;
-            S.max_rel_err = mr;
-            S.value = fx;
-            goto done;
-        }
-        int64_t niter = 0;
-        const double g0 = gn > 0 ? gn : 1.0;
-        for (;;) {
-            if (converged(gn, mr) || (mixed_phase && mr <= kMixedFloor)) {
-                if (!mixed_phase) break;
-                // the mixed residual has converged: check (and finish) in FP64
-                mixed_phase = false;
-                if ((st = timed_eval(w, false)) != MA_OK) {
-                    result = st;
-                    break;
-                }
-                fx = c->hstat[0];
-                minm = c->hstat[2];
-                gn = c->hstat[3];
-                mr = c->hstat[4];
-                continue;
-            }
-            if (niter > o.maxiter) {
-                result = MA_MAXITER;
-                break;
-            }
-            niter++;
-            // Newton direction: d = -H_s^{-1} g_s
-            k_grad<<<(n + 255) / 256, 256, 0, s>>>(c->mass.as<double>(), dnu, n, c->g.as<double>());
-            c->launches += 1;
-            cudaEventRecord(e0, s);
-            int it = 0;
-            double rr = 0;
-            // inexact Newton: the linear solve only needs to beat the current residual
-            double rtol = adaptive ? std::fmin(1e-3, std::fmax(1e-12, 0.1 * gn / g0)) : o.cg_rtol;
-            if ((st = pcg_solve(c, n, c->g.as<double>(), c->dirn.as<double>(), rtol, (int)o.cg_maxiter, &it,
-                                &rr, o.precond)) != MA_OK) {
-                result = st;
-                break;
-            }
-            cudaEventRecord(e1, s);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            S.t_linsolve_ms += ms;
-            S.cg_iters += it;
-            MA_CUDA(c, cudaMemcpyAsync(c->w0.p, w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-            double alpha = 1.0, n0 = gn;
-            bool ok = false;
-            while (true) {
-                // w = w0 - alpha * solution
-                k_axpy_to<<<(n + 255) / 256, 256, 0, s>>>(c->w0.as<double>(), c->dirn.as<double>(), -alpha, n, w);
-                c->launches += 1;
-                if ((st = timed_eval(w, true)) != MA_OK) {
-                    result = st;
-                    break;
-                }
-                fx = c->hstat[0];
-                minm = c->hstat[2];
-                gn = c->hstat[3];
-                mr = c->hstat[4];
-                if (minm >= eps0 && gn <= (1.0 - alpha / 2.0) * n0) {
-                    ok = true;
-                    break;
-                }
-                alpha *= 0.5;
-                S.linesearch_halvings++;
-                if (o.verbose)
-                    fprintf(stderr, "subit %lld: min(masses)=%.17g\n", (long long)niter, minm);
-                if (alpha < 0x1p-40) break;
-            }
-            if (result != MA_OK) break;
-            if (!ok && mixed_phase) {
-                // the mixed residual is at its noise level: redo this step in FP64
-                mixed_phase = false;
-                MA_CUDA(c, cudaMemcpyAsync(w, c->w0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-                if ((st = timed_eval(w, false)) != MA_OK) {
-                    result = st;
-                    break;
-                }
-                fx = c->hstat[0];
-                minm = c->hstat[2];
-                gn = c->hstat[3];
-                mr = c->hstat[4];
-                continue;
-            }
-            if (!ok) {
-                result = fail(c, MA_LINESEARCH_FAIL, "line search failed");
-                break;
-            }
-            if (o.verbose)
-                fprintf(stderr, "it %lld: f=%.17g |df|=%.17g max_rel=%.3g tau=%g eval=%zu cg=%d\n", (long long)niter, fx,
-                        gn, mr, alpha, S.neval, it);
-        }
-        S.niter = (size_t)niter;
-        S.grad_norm = gn;
-        S.max_rel_err = mr;
-        S.value = fx;
-    }
-done:
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    ma_status result = o.init == MA_INIT_MULTISCALE ? multiscale_solve(c, m, n, dx, dy, dnu, w, o, S)
+                                                    : newton_core(c, m, n, dx, dy, dnu, w, o, S);
     if (result == MA_OK || result == MA_MAXITER || result == MA_LINESEARCH_FAIL) {
         cudaMemcpyAsync(w_inout, w, sizeof(double) * n,
                         mem == MA_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s);

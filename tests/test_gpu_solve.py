@@ -168,3 +168,18 @@ def test_multigrid_at_one_million_sites(ctx):
     res = (H @ d.cpu().numpy() - r)[:-1]
     assert np.linalg.norm(res) <= 1e-7 * np.linalg.norm(r)
     assert it < 400
+
+
+def test_multiscale_initial_guess(ctx):
+    # clustered sites on a uniform density: the coarse-to-fine start reaches the same
+    # solution (unique up to the additive constant of the gauge) as the plain start
+    from mongeampere_gb300 import api
+    p = W.make_problem(128, 20000, "uniform", "blobs", "equal", seed=6)
+    X = np.c_[p.x, p.y]
+    st_m, st_p = api.Statistics(), api.Statistics()
+    w_m = api.ot_solve(p.mesh, X, p.nu, eps_g=1e-8, stop="rel", init="multiscale", stats=st_m, ctx=ctx,
+                       maxiter=400)
+    w_p = api.ot_solve(p.mesh, X, p.nu, eps_g=1e-8, stop="rel", stats=st_p, ctx=ctx, maxiter=400)
+    assert st_m.max_rel_err <= 1e-8 and st_p.max_rel_err <= 1e-8
+    a, b = np.asarray(w_m) - w_m[-1], np.asarray(w_p) - w_p[-1]
+    np.testing.assert_allclose(a, b, rtol=0, atol=1e-7 * np.abs(b).max())
