@@ -13,6 +13,7 @@
  *   ma_lloyd           MA::lloyd                      include/MA/lloyd.hpp:126-144
  *   ma_pieces          MA::voronoi_triangulation_intersection
  *                                                     include/MA/voronoi_triangulation_intersection.hpp:315-343
+ *   ma_ot_solve_batch  no counterpart in the reference: many problems, solved concurrently
  *   ma_kantorovich_vjp no counterpart in the reference: the adjoint of ma_kantorovich
  *                      and ma_moments (vector-Jacobian product)
  *   ma_mesh_create_*   the density: a triangulation plus one linear function per
@@ -184,6 +185,30 @@ void ma_solve_opts_default(ma_solve_opts* o);
 ma_status ma_ot_solve(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
                       const double* nu, double* w_inout, ma_mem mem, const ma_solve_opts* opts,
                       ma_stats* stats);
+/* ------------------------------------------------------------------- batch */
+/* Many independent problems (no counterpart in the reference, which solves one per
+ * MA::ot_solve call).  Each problem has its own mesh (created on any context of the
+ * same device), sites, target masses and weights (initial guess in, solution out);
+ * every array of the batch is in `mem`.  The problems are solved by `workers`
+ * contexts (one CUDA stream and one host thread each) taking them in order; kernels of
+ * different problems run concurrently.  workers = 0 autotunes the count (4 to 32) on the
+ * first chunks of the batch (kept in the context for later calls); *workers_used (nullable)
+ * receives the count used.  Each problem's status and statistics are those of
+ * ma_ot_solve on it, which is exactly what the batch computes for it.  The call
+ * returns MA_OK unless a CUDA or argument error stopped a worker. */
+typedef struct ma_problem {
+    const ma_mesh* mesh;
+    int64_t n;
+    const double* x;
+    const double* y;
+    const double* nu;
+    double* w;
+    ma_status status; /* out */
+    ma_stats stats;   /* out */
+} ma_problem;
+ma_status ma_ot_solve_batch(ma_ctx* ctx, ma_problem* problems, int64_t count, ma_mem mem,
+                            const ma_solve_opts* opts, int workers, int* workers_used);
+
 /* Newton direction of solve_laplacian_matrix: solve H[:n-1,:n-1] d = g[:n-1], d[n-1] = 0,
  * for the Hessian of the last ma_kantorovich call.  Returns the CG iteration count in *iters. */
 ma_status ma_laplacian_solve(ma_ctx* ctx, const double* g, double* d, ma_mem mem, double rtol,

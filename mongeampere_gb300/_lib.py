@@ -30,6 +30,11 @@ class MaStats(ctypes.Structure):
                 ("t_linsolve_ms", ctypes.c_double), ("neval_fp64", ctypes.c_size_t)]
 
 
+class MaProblem(ctypes.Structure):
+    _fields_ = [("mesh", ctypes.c_void_p), ("n", ctypes.c_int64), ("x", ctypes.c_void_p), ("y", ctypes.c_void_p),
+                ("nu", ctypes.c_void_p), ("w", ctypes.c_void_p), ("status", ctypes.c_int), ("stats", MaStats)]
+
+
 class MaProfile(ctypes.Structure):
     _fields_ = [("cells_ms", ctypes.c_double), ("cells_launches", ctypes.c_int64),
                 ("pieces_ms", ctypes.c_double), ("pieces_launches", ctypes.c_int64),
@@ -67,6 +72,7 @@ SIGNATURES = {
     "ma_moments": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp]),
     "ma_pieces": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
     "ma_pieces_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
+    "ma_ot_solve_batch": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int, _vp, ctypes.c_int, _vp]),
     "ma_mesh_set_values": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
     "ma_kantorovich_vjp": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, ctypes.c_double,
                                           _vp, _vp, _vp, _vp, _vp, _vp]),

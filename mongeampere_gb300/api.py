@@ -386,6 +386,61 @@ def ot_solve(mesh, X, masses, x=None, eps_g: float = 1e-7, maxiter: int = 100, v
     return w
 
 
+def ot_solve_batch(problems, eps_g: float = 1e-6, stop: str = "rel", precision: str = "fp64",
+                   init: str = "given", workers: int = 0, maxiter: int = 100, ctx: Context | None = None):
+    """Many independent problems (``ma_ot_solve_batch``): ``problems`` is a list of
+    ``(mesh, X, nu)`` or ``(mesh, X, nu, w0)``.  Returns ``(weights, stats, workers)``:
+    the solved weights and a :class:`Statistics` per problem (``status`` set), and
+    the number of concurrent workers used (``workers=0``: autotuned)."""
+    ctx = ctx or default_context()
+    n = len(problems)
+    arr = (L.MaProblem * n)()
+    keep = []
+    device = None
+    for k, pr in enumerate(problems):
+        mesh, X, nu = pr[0], pr[1], pr[2]
+        dm = _dmesh(ctx, mesh)
+        x, y = _split_xy(X)
+        w0 = pr[3] if len(pr) > 3 and pr[3] is not None else None
+        if w0 is None:
+            w0 = np.zeros(int(np.asarray(nu).shape[0])) if not _is_device(nu) else None
+            if w0 is None:
+                import torch
+                w0 = torch.zeros(nu.shape[0], dtype=torch.float64, device=nu.device)
+        a = _Args(x, y, nu, w0)
+        if device is None:
+            device = a.device
+        elif device != a.device:
+            raise ValueError("all arrays of a batch must be host arrays or all CUDA tensors")
+        w = a.keep[3] if a.device else a.keep[3].copy()
+        wp = ctypes.c_void_p(w.data_ptr()) if a.device else ctypes.c_void_p(w.ctypes.data)
+        keep.append((dm, a, w))
+        arr[k].mesh = dm.h
+        arr[k].n = int(a.keep[0].shape[0])
+        arr[k].x, arr[k].y, arr[k].nu = a.ptrs[0], a.ptrs[1], a.ptrs[2]
+        arr[k].w = wp
+    o = L.MaSolveOpts()
+    ctx.lib.ma_solve_opts_default(ctypes.byref(o))
+    o.eps_g = eps_g
+    o.maxiter = maxiter
+    o.stop_rule = L.MA_STOP_MAX_REL if stop == "rel" else L.MA_STOP_GRAD_NORM
+    o.precision = L.MA_MIXED if precision == "mixed" else L.MA_FP64
+    o.init = L.MA_INIT_MULTISCALE if init == "multiscale" else L.MA_INIT_GIVEN
+    used = ctypes.c_int()
+    mem = L.MA_MEM_DEVICE if device else L.MA_MEM_HOST
+    st = ctx.lib.ma_ot_solve_batch(ctx.h, arr, n, mem, ctypes.byref(o), int(workers), ctypes.byref(used))
+    _check(ctx.lib, ctx.h, st, "ma_ot_solve_batch")
+    ws, stats = [], []
+    for k in range(n):
+        s_ = Statistics()
+        for f, _ in L.MaStats._fields_:
+            setattr(s_, f, getattr(arr[k].stats, f))
+        s_.status = arr[k].status
+        stats.append(s_)
+        ws.append(keep[k][2])
+    return ws, stats, int(used.value)
+
+
 def solve_laplacian_matrix(g, rtol: float = 1e-10, maxiter: int = 0, ctx: Context | None = None):
     """Newton direction for the Hessian of the context's last evaluation
     (optimal_transport.hpp:41-87): ``H[:n-1,:n-1] d = g[:n-1]``, ``d[n-1] = 0``."""

@@ -25,6 +25,8 @@
 // held at zero on every level.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "ma_runtime.h"
 
 namespace cg = cooperative_groups;
@@ -681,12 +683,14 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     // the co-resident grid, at most kBlocksPerSm blocks per SM: every grid barrier
     // waits for all blocks, and the coarse levels' teams want the lanes
     constexpr int kBlocksPerSm = 4;
-    static int max_blocks = 0;
-    if (max_blocks == 0) {
+    int max_blocks = 0;
+    {
         int per_sm = 0, sms = 0;
         MA_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_amg, kAmgThreads, 0));
         MA_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
         max_blocks = (per_sm < kBlocksPerSm ? per_sm : kBlocksPerSm) * sms;
+        // a batch worker leaves the rest of the GPU to the other workers' problems
+        if (c->grid_share > 1) max_blocks = std::max(1, max_blocks / c->grid_share);
     }
     int want = (n + kAmgThreads / 4 - 1) / (kAmgThreads / 4);
     int nb = want < max_blocks ? want : max_blocks;

@@ -460,6 +460,8 @@ ma_status ma_ctx_create(int device, ma_ctx** out)
 void ma_ctx_destroy(ma_ctx* c)
 {
     if (!c) return;
+    for (ma_ctx* w : c->workers) ma_ctx_destroy(w);
+    c->workers.clear();
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->abortf, &c->vjp_cm, &c->vjp_cf,
@@ -471,7 +473,7 @@ void ma_ctx_destroy(ma_ctx* c)
                       &c->st_col, &c->st_val, &c->rowptr, &c->col, &c->val, &c->status, &c->redo, &c->nredo,
                       &c->stat_partial, &c->stat_out, &c->info, &c->big_index, &c->big_col, &c->big_val, &c->big_work, &c->wcur, &c->w0, &c->dirn, &c->g, &c->cg_r,
                       &c->cg_z, &c->cg_p, &c->cg_q, &c->cg_dinv, &c->cg_scal, &c->cg_part,
-                      &c->ms_x, &c->ms_y, &c->ms_nu, &c->ms_w};
+                      &c->ms_x, &c->ms_y, &c->ms_nu, &c->ms_w, &c->tune_w};
     for (DevBuf* b : bufs) b->release();
     for (AmgBuf& l : c->amg.lev) {
         DevBuf* lb[] = {&l.rp, &l.ci, &l.va, &l.dinv, &l.b, &l.xp};

@@ -104,6 +104,12 @@ struct Ctx {
     // solver work vectors
     DevBuf wcur, w0, dirn, g, cg_r, cg_z, cg_p, cg_q, cg_dinv, cg_scal, cg_part;
     DevBuf ms_x, ms_y, ms_nu, ms_w;  // a coarse level of the multiscale initial guess
+    // batches: worker contexts (one stream each) and the autotuned worker count
+    std::vector<ma_ctx*> workers;
+    int batch_workers = 0;
+    int grid_share = 1;  // a batch worker's cooperative grids use 1 / grid_share of the GPU
+    DevBuf tune_w;                // weight copies of the batch autotuner (device callers)
+    std::vector<double> tune_wh;  //                                       (host callers)
     Amg amg;
     // profiling (CUDA events around the main kernels)
     bool prof = false;

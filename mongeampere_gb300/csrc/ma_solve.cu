@@ -212,12 +212,13 @@ static ma_status pcg_solve(Ctx* c, int n, const double* b, double* x, double rto
     MA_CUDA(c, c->cg_q.ensure(sizeof(double) * n));
     MA_CUDA(c, c->cg_dinv.ensure(sizeof(double) * n));
     MA_CUDA(c, c->cg_scal.ensure(sizeof(double) * 8));
-    static int max_blocks = 0;
-    if (max_blocks == 0) {
+    int max_blocks = 0;
+    {
         int per_sm = 0, sms = 0;
         MA_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, kPcgThreads, 0));
         MA_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
         max_blocks = per_sm * sms;
+        if (c->grid_share > 1) max_blocks = std::max(1, max_blocks / c->grid_share);
     }
     int want = (n + kPcgThreads - 1) / kPcgThreads;
     int nb = want < max_blocks ? want : max_blocks;

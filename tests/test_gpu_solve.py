@@ -183,3 +183,24 @@ def test_multiscale_initial_guess(ctx):
     assert st_m.max_rel_err <= 1e-8 and st_p.max_rel_err <= 1e-8
     a, b = np.asarray(w_m) - w_m[-1], np.asarray(w_p) - w_p[-1]
     np.testing.assert_allclose(a, b, rtol=0, atol=1e-7 * np.abs(b).max())
+
+
+def test_batch_matches_sequential_solves(ctx):
+    # the batch solves every problem with the same ma_ot_solve, on concurrent
+    # worker contexts: the results are those of a sequential loop
+    from mongeampere_gb300 import api
+    probs = [p for p in W.c5(seed=3, count=40) if p.n <= 8000][:16]
+    assert len(probs) >= 8
+    items = [(p.mesh, np.c_[p.x, p.y], p.nu) for p in probs]
+    ws, stats, used = api.ot_solve_batch(items, eps_g=1e-6, stop="rel", workers=4, ctx=ctx)
+    assert used == 4
+    for p, w, st in zip(probs, ws, stats):
+        assert st.status == 0 and st.max_rel_err <= 1e-6
+        s1 = api.Statistics()
+        w1 = api.ot_solve(p.mesh, np.c_[p.x, p.y], p.nu, eps_g=1e-6, stop="rel", stats=s1, ctx=ctx)
+        np.testing.assert_allclose(w, w1, rtol=0, atol=1e-13 * max(1e-30, np.abs(w1).max()))
+        assert st.niter == s1.niter and st.neval == s1.neval
+    # autotuned worker count
+    ws2, stats2, used2 = api.ot_solve_batch(items, eps_g=1e-6, stop="rel", workers=0, ctx=ctx)
+    assert used2 in (4, 8, 16, 32)
+    assert all(s.status == 0 for s in stats2)
