@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../ma.h"
@@ -265,6 +266,47 @@ void lloyd(const Density& density, const Matrix& X, const Vector& weights, Vecto
     for (int64_t i = 0; i < n; i++) {
         centroids(i, 0) = c[2 * i];
         centroids(i, 1) = c[2 * i + 1];
+    }
+}
+
+// MA::voronoi_triangulation_intersection (voronoi_triangulation_intersection.hpp:
+// 315-343): calls out(polygon, triangle, site) for every non-empty intersection of a
+// Laguerre cell with a mesh triangle.  polygon is a std::vector of (x, y) pairs,
+// counter-clockwise; triangle is the mesh triangle's index (the Face_handle), site
+// the site's index (the Vertex_handle); edge[k] labels polygon edge k -> k+1: the
+// neighbouring site, or -1-e for edge e of the triangle.
+struct Piece {
+    int32_t site = 0, triangle = 0;
+    std::vector<std::pair<double, double>> polygon;
+    std::vector<int32_t> edge;
+};
+
+template <class Matrix, class Vector, class Out>
+void voronoi_triangulation_intersection(const Density& density, const Matrix& X, const Vector& weights, Out&& out)
+{
+    std::vector<double> x, y;
+    detail::split_sites(X, x, y);
+    const int64_t n = (int64_t)x.size();
+    std::vector<double> w = detail::to_vec(weights, n);
+    int64_t np = 0, nv = 0;
+    check(ma_pieces(density.ctx(), density.get(), n, x.data(), y.data(), w.data(), MA_MEM_HOST, &np, &nv),
+          density.ctx(), "ma_pieces");
+    std::vector<int32_t> site(np), tri(np), edge(nv);
+    std::vector<int64_t> off(np + 1);
+    std::vector<double> xy(2 * nv);
+    check(ma_pieces_copy(density.ctx(), site.data(), tri.data(), off.data(), xy.data(), edge.data(), MA_MEM_HOST),
+          density.ctx(), "ma_pieces_copy");
+    Piece p;
+    for (int64_t k = 0; k < np; k++) {
+        p.site = site[k];
+        p.triangle = tri[k];
+        p.polygon.clear();
+        p.edge.clear();
+        for (int64_t v = off[k]; v < off[k + 1]; v++) {
+            p.polygon.emplace_back(xy[2 * v], xy[2 * v + 1]);
+            p.edge.push_back(edge[v]);
+        }
+        out(p);
     }
 }
 

@@ -42,3 +42,39 @@ def test_python_api_fails_loudly_without_device():
     from mongeampere_gb300 import _lib, api
     with pytest.raises(_lib.MaError):
         api.Context(0)
+
+
+def _build_wrapper_example(tmp_path):
+    import shutil
+    import subprocess
+    from mongeampere_gb300 import build as B
+    lib = B.build()
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no g++")
+    exe = str(tmp_path / "wrapper_example")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.check_call([gxx, "-std=c++17", "-O1", "-I", os.path.join(root, "include"),
+                           os.path.join(root, "tests", "cpp", "wrapper_example.cpp"), "-o", exe,
+                           "-L", os.path.dirname(lib), "-lma_gb300", "-Wl,-rpath," + os.path.dirname(lib)])
+    return exe
+
+
+def test_cpp_wrapper_builds_and_reports_missing_device(tmp_path):
+    # the reference-shaped C++ API links against the library; without a GPU the
+    # error surfaces as MA::Error (exit status 3)
+    import subprocess
+    exe = _build_wrapper_example(tmp_path)
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: covered by the GPU test")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 3 and "no usable CUDA device" in r.stdout
+
+
+@pytest.mark.gpu
+def test_cpp_wrapper_runs(tmp_path):
+    import subprocess
+    exe = _build_wrapper_example(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
