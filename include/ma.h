@@ -157,8 +157,8 @@ typedef struct ma_solve_opts {
     int stop_rule;         /* ma_stop_rule */
     int precision;         /* ma_precision */
     int verbose;           /* print the reference's per-iteration line to stderr */
-    double cg_rtol;        /* relative residual of the preconditioned CG; 0 (default): inexact Newton,
-                              min(1e-3, max(1e-12, 0.1 |g| / |g0|)) at each step */
+    double cg_rtol;        /* relative residual of the preconditioned CG; 0 (default): inexact Newton
+                              with the forcing term 1e-2 */
     int64_t cg_maxiter;    /* CG iteration cap (0: default 20000) */
     int precond;           /* ma_precond: CG preconditioner of the Newton step */
     int init;              /* ma_init: initial guess */

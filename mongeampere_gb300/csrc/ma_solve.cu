@@ -310,11 +310,13 @@ static ma_status static_setup(int dev, StaticSetup* out)
 using namespace ma;
 
 // The Newton iteration of MA::ot_solve on one set of sites (device arrays; w in/out).
+constexpr double kForcing = 1e-2;  // relative CG residual of a Newton direction (cg_rtol = 0)
+
 static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, const double* dy, const double* dnu,
                              double* w, const ma_solve_opts& o, ma_stats& S)
 {
     cudaStream_t s = c->stream;
-    const bool adaptive = !(o.cg_rtol > 0);
+    const bool default_forcing = !(o.cg_rtol > 0);
     MA_CUDA(c, c->w0.ensure(sizeof(double) * n));
     MA_CUDA(c, c->dirn.ensure(sizeof(double) * n));
     MA_CUDA(c, c->g.ensure(sizeof(double) * n));
@@ -388,7 +390,6 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
             goto core_done;
         }
         int64_t niter = 0;
-        const double g0 = gn > 0 ? gn : 1.0;
         for (;;) {
             if (converged(gn, mr) || (mixed_phase && mr <= kMixedFloor)) {
                 if (!mixed_phase) break;
@@ -415,8 +416,11 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
             cudaEventRecord(e0, s);
             int it = 0;
             double rr = 0;
-            // inexact Newton: the linear solve only needs to beat the current residual
-            double rtol = adaptive ? std::fmin(1e-3, std::fmax(1e-12, 0.1 * gn / g0)) : o.cg_rtol;
+            // inexact Newton with a constant forcing term: directions to 1e-2 relative
+            // residual keep the reference's Newton and evaluation counts (measured on the
+            // 64^2 / 1,000-site, 512^2 / 100,000-site and 2048^2 / 1M-site workloads)
+            // while tighter solves only cost CG iterations
+            double rtol = default_forcing ? kForcing : o.cg_rtol;
             if ((st = pcg_solve(c, n, c->g.as<double>(), c->dirn.as<double>(), rtol, (int)o.cg_maxiter, &it,
                                 &rr, o.precond)) != MA_OK) {
                 result = st;
@@ -737,7 +741,7 @@ void ma_solve_opts_default(ma_solve_opts* o)
     o->stop_rule = MA_STOP_GRAD_NORM;
     o->precision = MA_FP64;
     o->verbose = 0;
-    o->cg_rtol = 0.0;  // adaptive forcing
+    o->cg_rtol = 0.0;  // the default forcing term
     o->cg_maxiter = 20000;
     o->precond = MA_PRECOND_MULTIGRID;
     o->init = MA_INIT_GIVEN;
