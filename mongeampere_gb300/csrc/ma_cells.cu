@@ -978,7 +978,24 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                         }
                         Poly<kClipCap>* Q = &PB;
                         const Slot* sl = W.slot + C.soff;
-                        for (int s = 0; s < C.m && P->n > 0; s++) {
+                        // certified corner tests first, in registers: a slot with all three
+                        // corners outside rejects the triangle, a slot with all three inside
+                        // contains every sub-polygon of it and needs no clip
+                        uint64_t cut = 0;
+                        for (int s = 0; s < C.m; s++) {
+                            const Slot cs = sl[s];
+                            const int t0 = test32(T.ux[0], T.uy[0], T.ur[0], cs);
+                            const int t1 = test32(T.ux[1], T.uy[1], T.ur[1], cs);
+                            const int t2 = test32(T.ux[2], T.uy[2], T.ur[2], cs);
+                            if (t0 > 0 && t1 > 0 && t2 > 0) {
+                                P->n = 0;
+                                break;
+                            }
+                            if (!(t0 < 0 && t1 < 0 && t2 < 0)) cut |= 1ull << s;
+                        }
+                        while (cut && P->n > 0) {
+                            const int s = __ffsll((long long)cut) - 1;
+                            cut &= cut - 1;
                             if (clip_poly<kClipCap, false>(*P, *Q, s, sl, T, o, A.sites, st, bad)) {
                                 if (bad) break;
                                 Poly<kClipCap>* t = P;
