@@ -193,9 +193,10 @@ ma_status ma_ot_solve(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double*
  * contexts (one CUDA stream and one host thread each) taking them in order; kernels of
  * different problems run concurrently.  workers = 0 autotunes the count (4 to 32) on the
  * first chunks of the batch (kept in the context for later calls); *workers_used (nullable)
- * receives the count used.  Each problem's status and statistics are those of
- * ma_ot_solve on it, which is exactly what the batch computes for it.  The call
- * returns MA_OK unless a CUDA or argument error stopped a worker. */
+ * receives the count used.  Each problem is solved by ma_ot_solve (status and
+ * statistics are its); a worker's CG uses a share of the GPU, so results agree with
+ * separate calls to the solver's tolerance, not to the last bit.  The call returns
+ * MA_OK unless a CUDA or argument error stopped a worker. */
 typedef struct ma_problem {
     const ma_mesh* mesh;
     int64_t n;

@@ -8,8 +8,8 @@
 //
 //   * the fine level is H copied into Morton order (the order of the site index),
 //     so that neighbouring rows are close in memory; every level is then
-//     aggregated the same way, kAggSize consecutive rows per aggregate, which are
-//     spatially compact without any graph search;
+//     aggregated the same way, consecutive rows per aggregate (kAggFine on the fine
+//     level, kAggCoarse below), spatially compact without any graph search;
 //   * the coarse matrices are Galerkin products P^T A P with the piecewise-constant
 //     prolongation P: a coarse entry (I, J) is the sum of the fine entries (i, j)
 //     with i in I and j in J.  Each coarse row is assembled by one warp, its
@@ -33,18 +33,22 @@ namespace cg = cooperative_groups;
 
 namespace ma {
 
-constexpr int kAggSize = 4;         // nodes per aggregate, every level (four lanes in the kernels)
+constexpr int kAggFine = 4;    // fine rows per aggregate (four lanes of the fused fine restriction)
+constexpr int kAggCoarse = 4;  // coarse rows per aggregate on the levels below (8 gives fewer
+                               // levels but more iterations: slower on the 100k-site workload)
+__host__ __device__ constexpr int agg_size(int l) { return l == 0 ? kAggFine : kAggCoarse; }
 constexpr int kCoarsest = 64;       // dense solve at or below this many nodes
 constexpr int kRowCap = 512;        // gathered entries of one coarse row
 constexpr int kRowWarps = 4;        // coarse rows per block in the setup
 constexpr double kOmega = 2.0 / 3.0;
 constexpr double kCoarseScale = 1.5;
-static_assert(kAggSize == 4, "aggregate sums use two shuffle steps");
+static_assert(kAggFine == 4, "the fine aggregate sums use two shuffle steps");
 
 // ---------------------------------------------------------------------------
 // setup: coarse rows
 // ---------------------------------------------------------------------------
 struct CoarseSrc {
+    int agg;           // rows per aggregate
     int n;             // fine nodes
     const int* rp;     // fine CSR
     const int* ci;
@@ -71,8 +75,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_coarse_rows(CoarseSrc s, int
     unsigned char* lead = slead[wib];
     int E = 0;
     bool over = false;
-    for (int q = 0; q < kAggSize && !over; q++) {
-        const int i = I * kAggSize + q;
+    for (int q = 0; q < s.agg && !over; q++) {
+        const int i = I * s.agg + q;
         if (i >= s.n) break;
         if (s.dinv[i] == 0.0) continue;
         const int k0 = s.rp[i], k1 = s.rp[i + 1];
@@ -83,7 +87,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_coarse_rows(CoarseSrc s, int
             if (k < k1) {
                 const int j = s.ci[k];
                 if (s.dinv[j] != 0.0) {
-                    c = j / kAggSize;
+                    c = j / s.agg;
                     v = s.va[k];
                 }
             }
@@ -363,7 +367,8 @@ __device__ __forceinline__ void restrict_level(const AmgPcgArgs& a, int l)
     team_rows(C.n, T, [&](int J, int t) {
         double s = 0.0;
         if (J >= 0) {
-            const int I0 = J * kAggSize, I1 = min(I0 + kAggSize, A.n);
+            const int S = agg_size(l);
+            const int I0 = J * S, I1 = min(I0 + S, A.n);
             for (int q = t; q < I1 - I0; q += T) s += A.b[I0 + q];
             for (int k = A.rp[I0] + t; k < A.rp[I1]; k += T) {
                 const int K = A.ci[k];
@@ -411,10 +416,10 @@ __device__ __forceinline__ void prolong_level(const AmgPcgArgs& a, int l, double
                 for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) {
                     const int K = A.ci[k];
                     const double dK = A.dinv[K];
-                    const double yK = dK != 0.0 ? kOmega * dK * A.b[K] + kCoarseScale * coarse_corr(a, l, K / kAggSize, xc) : 0.0;
+                    const double yK = dK != 0.0 ? kOmega * dK * A.b[K] + kCoarseScale * coarse_corr(a, l, K / agg_size(l), xc) : 0.0;
                     s -= A.va[k] * yK;
                 }
-                if (t == 0) yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, I / kAggSize, xc);
+                if (t == 0) yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, I / agg_size(l), xc);
             }
         }
         s = team_sum(s, T);
@@ -477,9 +482,9 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                     }
                 }
                 if (!jacobi) {
-                    s = team_sum(s, kAggSize);
-                    const int J = k / kAggSize;
-                    if ((k & (kAggSize - 1)) == 0 && J < C.n) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
+                    s = team_sum(s, kAggFine);
+                    const int J = k / kAggFine;
+                    if ((k & (kAggFine - 1)) == 0 && J < C.n) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
                 }
             }
             const double t = amg_block_sum(l_rr, sh);
@@ -519,7 +524,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                 const double dk = F.dinv[k];
                 double zk = 0.0;
                 if (dk != 0.0) {
-                    const double yk = kOmega * dk * rc[k] + kCoarseScale * coarse_corr(a, 0, k / kAggSize, xc);
+                    const double yk = kOmega * dk * rc[k] + kCoarseScale * coarse_corr(a, 0, k / kAggFine, xc);
                     double s = rc[k];
                     const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
 #pragma unroll 4
@@ -527,7 +532,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                         const int j = F.eci[b0 + 32 * e];
                         const double dj = F.dinv[j];
                         const double yj =
-                            dj != 0.0 ? kOmega * dj * rc[j] + kCoarseScale * coarse_corr(a, 0, j / kAggSize, xc)
+                            dj != 0.0 ? kOmega * dj * rc[j] + kCoarseScale * coarse_corr(a, 0, j / kAggFine, xc)
                                       : 0.0;
                         s -= F.eva[b0 + 32 * e] * yj;
                     }
@@ -588,7 +593,7 @@ int amg_levels(int n)
     int L = 1;
     int m = n;
     while (m > kCoarsest && L < kAmgMaxLevels) {
-        m = (m + kAggSize - 1) / kAggSize;
+        m = (m + agg_size(L - 1) - 1) / agg_size(L - 1);
         L++;
     }
     return L;
@@ -652,7 +657,7 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
                          G.eci.as<int>(), G.eva.as<double>()};
     int nl = n;
     for (int l = 1; l < nlev; l++) {
-        const int nc = (nl + kAggSize - 1) / kAggSize;
+        const int nc = (nl + agg_size(l - 1) - 1) / agg_size(l - 1);
         AmgBuf& B = G.lev[l];
         MA_CUDA(c, B.rp.ensure(sizeof(int) * (nc + 1)));
         MA_CUDA(c, B.ci.ensure(sizeof(int) * nnz));
@@ -661,7 +666,7 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         MA_CUDA(c, B.b.ensure(sizeof(double) * nc));
         MA_CUDA(c, B.xp.ensure(sizeof(double) * nc));
         const AmgLevelDev& A = a.L[l - 1];
-        CoarseSrc src{nl, A.rp, A.ci, A.va, A.dinv};
+        CoarseSrc src{agg_size(l - 1), nl, A.rp, A.ci, A.va, A.dinv};
         const unsigned g = (unsigned)((nc + kRowWarps - 1) / kRowWarps);
         k_coarse_rows<false><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), nullptr, nullptr, nullptr,
                                                            G.flag.as<int>());

@@ -6,8 +6,10 @@
 // latency, so a batch of them is solved by K workers, each a context of its own (one
 // CUDA stream, its own scratch) driven by one host thread: the workers take the
 // problems in order from a shared counter, and the kernels of K problems run side by
-// side on the GPU.  Every problem goes through the same ma_ot_solve as a single call,
-// so its result is the one a sequential loop gives.
+// side on the GPU.  Every problem goes through the same ma_ot_solve as a single call;
+// a worker's cooperative CG grid is its share of the GPU, so the CG sums run in
+// another order and the result agrees with a sequential loop's to the solver's
+// tolerance (not to the last bit).
 //
 // K is autotuned when the caller passes 0 and the context has no earlier choice: the
 // batch's median-sized problem is solved once on every candidate worker (their
