@@ -14,6 +14,7 @@
  *   ma_pieces          MA::voronoi_triangulation_intersection
  *                                                     include/MA/voronoi_triangulation_intersection.hpp:315-343
  *   ma_ot_solve_batch  no counterpart in the reference: many problems, solved concurrently
+ *   ma_draw_laguerre   MA::draw_laguerre_diagram        include/MA/rasterization.hpp:516-547
  *   ma_kantorovich_vjp no counterpart in the reference: the adjoint of ma_kantorovich
  *                      and ma_moments (vector-Jacobian product)
  *   ma_mesh_create_*   the density: a triangulation plus one linear function per
@@ -255,6 +256,17 @@ ma_status ma_pieces(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x
                     const double* w, ma_mem mem, int64_t* npieces, int64_t* nverts);
 ma_status ma_pieces_copy(ma_ctx* ctx, int32_t* site, int32_t* tri, int64_t* off, double* xy, int32_t* edge,
                          ma_mem mem);
+
+/* MA::draw_laguerre_diagram (rasterization.hpp:516-547): every piece rasterised with
+ * exact pixel coverage into image[height][width][channels] (row y = 0 first; pixel
+ * (i, j) covers [x0 + i dx, x0 + (i+1) dx] x [y0 + j dy, y0 + (j+1) dy] with
+ * dx = (x1 - x0) / width), adding cover * (mean of the density at the piece's
+ * vertices) * colors[site][channel] -- the reference's put_pixel(x, y, cover * ff *
+ * color); the image is added to (zero it for a plain drawing).  colors[n][channels],
+ * channels 1..16; image and colors in `mem`. */
+ma_status ma_draw_laguerre(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
+                           const double* w, const double* colors, int channels, double x0, double y0,
+                           double x1, double y1, int width, int height, double* image, ma_mem mem);
 
 /* ----------------------------------------------------------------- adjoint */
 /* Vector-Jacobian product of (value, mass[n], first[2n]) -- the Kantorovich value

@@ -277,6 +277,36 @@ def pieces(mesh, X, weights, y=None, ctx: Context | None = None) -> Pieces:
     return Pieces(site, tri, off, xy, edge)
 
 
+def draw_laguerre_diagram(mesh, X, weights, colors, bbox, width: int, height: int, image=None, y=None,
+                          ctx: Context | None = None):
+    """``MA::draw_laguerre_diagram`` (``ma_draw_laguerre``): every cell-triangle piece
+    rasterised with exact pixel coverage, ``cover * (mean density at the piece's
+    vertices) * colors[site]`` added to ``image`` (``(height, width, channels)``, zeros
+    when not given); ``colors`` is ``(N,)`` or ``(N, channels)``; ``bbox`` =
+    ``(x0, y0, x1, y1)``.  Returns the image."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    x, yy = _split_xy(X, y)
+    col = colors
+    nc = 1 if len(col.shape) == 1 else int(col.shape[1])
+    col = col.reshape(-1)
+    a = _Args(x, yy, weights, col)
+    n = int(a.keep[0].shape[0])
+    if image is None:
+        if a.device:
+            import torch
+            image = torch.zeros((height, width, nc), dtype=torch.float64, device=a.keep[0].device)
+        else:
+            image = np.zeros((height, width, nc))
+    img = image if a.device else np.ascontiguousarray(image, dtype=np.float64)
+    ip = ctypes.c_void_p(img.data_ptr()) if a.device else ctypes.c_void_p(img.ctypes.data)
+    x0, y0, x1, y1 = (float(v) for v in bbox)
+    st = ctx.lib.ma_draw_laguerre(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.ptrs[3], nc, x0, y0, x1, y1,
+                                  int(width), int(height), ip, a.mem)
+    _check(ctx.lib, ctx.h, st, "ma_draw_laguerre")
+    return img
+
+
 def kantorovich_vjp(mesh, X, weights, cot_value: float = 0.0, cot_mass=None, cot_first=None, y=None, *,
                     grad_rho: bool = True, ctx: Context | None = None):
     """Adjoint of ``(value, masses, first moments)`` (``ma_kantorovich_vjp``; no

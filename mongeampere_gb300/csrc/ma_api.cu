@@ -466,7 +466,8 @@ void ma_ctx_destroy(ma_ctx* c)
     cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->abortf, &c->vjp_cm, &c->vjp_cf,
                       &c->vjp_gx, &c->vjp_gy, &c->vjp_gw, &c->vjp_gr, &c->pc_cnt, &c->pv_cnt,
-                      &c->pc_base, &c->pv_base, &c->pc_site, &c->pc_tri, &c->pc_off, &c->pc_xy, &c->pc_edge, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
+                      &c->pc_base, &c->pv_base, &c->pc_site, &c->pc_tri, &c->pc_off, &c->pc_xy, &c->pc_edge,
+                      &c->raster_col, &c->raster_img, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
                       &c->perm, &c->sites, &c->posf, &c->scan_scratch, &c->fill, &c->t_child, &c->t_range,
                       &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab,
                       &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,

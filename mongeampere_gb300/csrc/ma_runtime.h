@@ -96,6 +96,7 @@ struct Ctx {
     DevBuf pc_cnt, pv_cnt, pc_base, pv_base, pc_site, pc_tri, pc_off, pc_xy, pc_edge;
     int64_t npieces = 0, npverts = 0;
     bool have_pieces = false;
+    DevBuf raster_col, raster_img;  // rasterisation staging (host callers)
     bool aborted = false;                          // the last evaluation stopped at an empty cell
     DevBuf counters;                               // stage-1 search counters (profiling)
     DevBuf info;  // status, nredo, nnz

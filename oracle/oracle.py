@@ -356,3 +356,63 @@ def lloyd(mesh, x, y, w, mode: int = 1):
     m = r.moments[:, 0]
     c = r.moments[:, 1:3] / m[:, None]
     return m, c
+
+
+def _pixel_cover(poly, i, j):
+    """Area of the convex polygon ``poly`` (pixel units) inside [i, i+1] x [j, j+1],
+    clipped and summed relative to the pixel's corner."""
+    pts = [(p[0] - i, p[1] - j) for p in poly]
+    for axis, sgn, c in ((0, 1.0, 0.0), (0, -1.0, -1.0), (1, 1.0, 0.0), (1, -1.0, -1.0)):
+        out = []
+        m = len(pts)
+        for k in range(m):
+            a, b = pts[k], pts[(k + 1) % m]
+            da, db = sgn * a[axis] - c, sgn * b[axis] - c
+            if da >= 0:
+                out.append(a)
+            if (da >= 0) != (db >= 0):
+                t = da / (da - db)
+                out.append((a[0] + t * (b[0] - a[0]), a[1] + t * (b[1] - a[1])))
+        pts = out
+        if not pts:
+            return 0.0
+    x = np.array([p[0] for p in pts])
+    y = np.array([p[1] for p in pts])
+    return 0.5 * float(np.sum(x * np.roll(y, -1) - np.roll(x, -1) * y))
+
+
+def draw_laguerre_diagram(mesh, x, y, w, colors, bbox, width, height):
+    """``MA::draw_laguerre_diagram`` (include/MA/rasterization.hpp:516-547) restated:
+    every piece of the oracle's evaluation, its colour ``colors[site]`` times the mean of
+    the triangle's linear density at the piece's vertices (:530-540), rasterised with
+    exact pixel coverage (rasterize_convex_polygon, :403-480, computes the covered
+    area of each pixel; its 1e-6 nudge off integer coordinates is not reproduced).
+    Returns an ``(height, width, channels)`` image."""
+    colors = np.asarray(colors, dtype=np.float64)
+    if colors.ndim == 1:
+        colors = colors[:, None]
+    r = kantorovich(mesh, x, y, w, keep_pieces=True, arith="dd")
+    P = r.pieces
+    m = mesh.explicit()
+    x0, y0, x1, y1 = bbox
+    sx, sy = width / (x1 - x0), height / (y1 - y0)
+    img = np.zeros((height, width, colors.shape[1]))
+    for k in range(len(P.site)):
+        xy = P.xy[P.offsets[k]:P.offsets[k + 1]]
+        t = m.tri[P.face[k]]
+        a, b, c = t
+        ax, ay, bx, by, cx, cy = m.vx[a], m.vy[a], m.vx[b], m.vy[b], m.vx[c], m.vy[c]
+        det = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax)
+        f1, f2 = m.values[b] - m.values[a], m.values[c] - m.values[a]
+        gx = (f1 * (cy - ay) - f2 * (by - ay)) / det
+        gy = ((bx - ax) * f2 - (cx - ax) * f1) / det
+        ff = np.mean(m.values[a] + gx * (xy[:, 0] - ax) + gy * (xy[:, 1] - ay))
+        pp = np.c_[(xy[:, 0] - x0) * sx, (xy[:, 1] - y0) * sy]
+        i0, i1 = max(0, int(np.floor(pp[:, 0].min()))), min(width - 1, int(np.floor(pp[:, 0].max())))
+        j0, j1 = max(0, int(np.floor(pp[:, 1].min()))), min(height - 1, int(np.floor(pp[:, 1].max())))
+        for j in range(j0, j1 + 1):
+            for i in range(i0, i1 + 1):
+                cov = _pixel_cover(pp, i, j)
+                if cov > 0:
+                    img[j, i] += cov * ff * colors[P.site[k]]
+    return img
