@@ -11,12 +11,14 @@
  *   ma_laplacian_solve MA::solve_laplacian_matrix     include/MA/optimal_transport.hpp:41-87
  *   ma_moments         MA::first_moment / second_moment  include/MA/lloyd.hpp:30-123
  *   ma_lloyd           MA::lloyd                      include/MA/lloyd.hpp:126-144
+ *   ma_w2_flow         the iterated solve + centroid step of tests/test_zeldovich.cpp:99-119
  *   ma_pieces          MA::voronoi_triangulation_intersection
  *                                                     include/MA/voronoi_triangulation_intersection.hpp:315-343
  *   ma_ot_solve_batch  no counterpart in the reference: many problems, solved concurrently
  *   ma_draw_laguerre   MA::draw_laguerre_diagram        include/MA/rasterization.hpp:516-547
  *   ma_kantorovich_vjp no counterpart in the reference: the adjoint of ma_kantorovich
  *                      and ma_moments (vector-Jacobian product)
+ *   ma_mesh_create_image image_to_pl_function           include/MA/functions.hpp:82-120
  *   ma_mesh_create_*   the density: a triangulation plus one linear function per
  *                      face (include/MA/functions.hpp:55-120,
  *                      include/CGAL/Triangulation_incremental_builder_2.h:27-80)
@@ -117,6 +119,13 @@ ma_status ma_mesh_create_grid(ma_ctx* ctx, int nx, int ny, const double* gx, con
 /* Explicit triangulation (nv vertices, nt counter-clockwise triangles).  Host arrays. */
 ma_status ma_mesh_create_triangles(ma_ctx* ctx, int nv, const double* vx, const double* vy,
                                    const double* values, int nt, const int32_t* tri, ma_mesh** out);
+/* image_to_pl_function (functions.hpp:82-120): the density of a grey image,
+ * pixels[height][width] (rows top first, values 0..255, as CImg's image(x, y)), on a
+ * width x height vertex grid of [-1, 1]^2 with vertex values pixel / 255 + 1e-3; the
+ * total mass is ma_mesh_total_mass.  The reference triangulates the grid points with
+ * CGAL's Delaunay triangulation, whose split of each (co-circular) square is CGAL's
+ * choice; here every square is split along its (i, j)-(i+1, j+1) diagonal. */
+ma_status ma_mesh_create_image(ma_ctx* ctx, int width, int height, const double* pixels, ma_mesh** out);
 /* New vertex values for an existing mesh (same geometry): values[nx*ny] for a grid,
  * values[nv] for a triangle mesh, in host or device memory.  The density is a
  * differentiable input of ma_kantorovich_vjp; this updates it without rebuilding the
@@ -210,6 +219,18 @@ typedef struct ma_problem {
 } ma_problem;
 ma_status ma_ot_solve_batch(ma_ctx* ctx, ma_problem* problems, int64_t count, ma_mem mem,
                             const ma_solve_opts* opts, int workers, int* workers_used);
+
+/* A W2 gradient-flow / Lloyd driver (tests/test_zeldovich.cpp:99-119, lloyd.hpp:126-144):
+ * `steps` times, an OT solve of the sites to `nu` (ma_ot_solve with `opts`, warm-started
+ * from the previous weights, or from zero weights when a moved site's cell is empty
+ * there), the cells' centroids c (int rho x / int rho), then
+ * x <- x + tau (x - c) (tau = 0.03 is the reference's Zel'dovich-type step, tau = -1 a
+ * Lloyd step).  x, y and w are updated in place; *stats sums the solves.  The
+ * reference restarts every solve from zero weights and uses the cells' geometric
+ * barycentres; for a constant density the two barycentres agree. */
+ma_status ma_w2_flow(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, double* x, double* y, const double* nu,
+                     double* w, ma_mem mem, int64_t steps, double tau, const ma_solve_opts* opts,
+                     ma_stats* stats);
 
 /* Newton direction of solve_laplacian_matrix: solve H[:n-1,:n-1] d = g[:n-1], d[n-1] = 0,
  * for the Hessian of the last ma_kantorovich call.  Returns the CG iteration count in *iters. */

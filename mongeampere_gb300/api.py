@@ -471,6 +471,44 @@ def ot_solve_batch(problems, eps_g: float = 1e-6, stop: str = "rel", precision: 
     return ws, stats, int(used.value)
 
 
+def w2_flow(mesh, X, nu, steps: int, tau: float, w=None, eps_g: float = 1e-6, stop: str = "rel",
+            precision: str = "fp64", ctx: Context | None = None):
+    """``ma_w2_flow``: ``steps`` times an OT solve then ``x <- x + tau (x - centroid)``
+    (the iteration of tests/test_zeldovich.cpp:99-119; ``tau = -1`` is Lloyd's).
+    Returns ``(X, w, stats)`` after the last step."""
+    ctx = ctx or default_context()
+    dm = _dmesh(ctx, mesh)
+    x, y = _split_xy(X)
+    n = int(np.asarray(nu).shape[0]) if not _is_device(nu) else int(nu.shape[0])
+    if w is None:
+        if _is_device(nu):
+            import torch
+            w = torch.zeros(n, dtype=torch.float64, device=nu.device)
+        else:
+            w = np.zeros(n)
+    a = _Args(x, y, nu, w)
+    xs = a.keep[0] if a.device else a.keep[0].copy()
+    ys = a.keep[1] if a.device else a.keep[1].copy()
+    ws = a.keep[3] if a.device else a.keep[3].copy()
+    ptr = (lambda t: ctypes.c_void_p(t.data_ptr())) if a.device else (lambda t: ctypes.c_void_p(t.ctypes.data))
+    o = L.MaSolveOpts()
+    ctx.lib.ma_solve_opts_default(ctypes.byref(o))
+    o.eps_g = eps_g
+    o.stop_rule = L.MA_STOP_MAX_REL if stop == "rel" else L.MA_STOP_GRAD_NORM
+    o.precision = L.MA_MIXED if precision == "mixed" else L.MA_FP64
+    s = L.MaStats()
+    st = ctx.lib.ma_w2_flow(ctx.h, dm.h, n, ptr(xs), ptr(ys), a.ptrs[2], ptr(ws), a.mem, int(steps), float(tau),
+                            ctypes.byref(o), ctypes.byref(s))
+    _check(ctx.lib, ctx.h, st, "ma_w2_flow")
+    stats = Statistics()
+    for f, _ in L.MaStats._fields_:
+        setattr(stats, f, getattr(s, f))
+    if a.device:
+        import torch
+        return torch.stack([xs, ys], 1), ws, stats
+    return np.c_[xs, ys], ws, stats
+
+
 def solve_laplacian_matrix(g, rtol: float = 1e-10, maxiter: int = 0, ctx: Context | None = None):
     """Newton direction for the Hessian of the context's last evaluation
     (optimal_transport.hpp:41-87): ``H[:n-1,:n-1] d = g[:n-1]``, ``d[n-1] = 0``."""

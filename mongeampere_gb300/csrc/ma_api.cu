@@ -633,6 +633,23 @@ ma_status ma_mesh_create_grid(ma_ctx* c, int nx, int ny, const double* gx, const
     return MA_OK;
 }
 
+ma_status ma_mesh_create_image(ma_ctx* c, int width, int height, const double* pixels, ma_mesh** out)
+{
+    // image_to_pl_function (functions.hpp:82-120): an width x height grid of [-1, 1]^2,
+    // vertex (i, j) at (-1 + 2 i / (width - 1), -1 + 2 j / (height - 1)) carrying
+    // image(i, height - 1 - j) / 255 + 1e-3 (image rows top first)
+    if (!c || !out || !pixels || width < 2 || height < 2) return MA_ERR_INVALID_ARGUMENT;
+    std::vector<double> gx(width), gy(height), v((size_t)width * height);
+    for (int i = 0; i < width; i++) gx[i] = -1.0 + i * (2.0 / (double)(width - 1));
+    for (int j = 0; j < height; j++) gy[j] = -1.0 + j * (2.0 / (double)(height - 1));
+    gx[width - 1] = 1.0;
+    gy[height - 1] = 1.0;
+    for (int j = 0; j < height; j++)
+        for (int i = 0; i < width; i++)
+            v[(size_t)j * width + i] = pixels[(size_t)(height - 1 - j) * width + i] / 255.0 + 1e-3;
+    return ma_mesh_create_grid(c, width, height, gx.data(), gy.data(), v.data(), out);
+}
+
 ma_status ma_mesh_create_triangles(ma_ctx* c, int nv, const double* vx, const double* vy, const double* values,
                                    int nt, const int32_t* tri, ma_mesh** out)
 {

@@ -818,4 +818,64 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     return result;
 }
 
+ma_status ma_w2_flow(ma_ctx* cp, const ma_mesh* mp, int64_t n64, double* x, double* y, const double* nu, double* w,
+                     ma_mem mem, int64_t steps, double tau, const ma_solve_opts* opts, ma_stats* stats)
+{
+    // the iteration of tests/test_zeldovich.cpp:99-119 (and Lloyd's, lloyd.hpp:126-144,
+    // for tau = -1): an OT solve, the cells' centroids c, then x <- x + tau (x - c).
+    // The solve starts from the previous weights, or from zero when a moved site's
+    // cell is empty there.
+    Ctx* c = cp;
+    if (!c || !mp || !x || !y || !nu || !w || n64 < 1 || steps < 0) return MA_ERR_INVALID_ARGUMENT;
+    const size_t n = (size_t)n64;
+    ma_stats total{};
+    std::vector<double> hm(n), hf(2 * n), hx(n), hy(n), hw(n);
+    for (int64_t k = 0; k < steps; k++) {
+        ma_stats st{};
+        ma_status r = ma_ot_solve(cp, mp, n64, x, y, nu, w, mem, opts, &st);
+        if (r == MA_EMPTY_CELL) {
+            // the moved sites left a cell empty at the previous weights: restart from
+            // zero weights (Voronoi cells), as the reference's loop does every step
+            if (mem == MA_MEM_DEVICE)
+                MA_CUDA(c, cudaMemset(w, 0, sizeof(double) * n));
+            else
+                std::fill(w, w + n, 0.0);
+            r = ma_ot_solve(cp, mp, n64, x, y, nu, w, mem, opts, &st);
+        }
+        total.niter += st.niter;
+        total.neval += st.neval;
+        total.neval_fp64 += st.neval_fp64;
+        total.cg_iters += st.cg_iters;
+        total.linesearch_halvings += st.linesearch_halvings;
+        total.t_eval_ms += st.t_eval_ms;
+        total.t_linsolve_ms += st.t_linsolve_ms;
+        total.grad_norm = st.grad_norm;
+        total.max_rel_err = st.max_rel_err;
+        total.value = st.value;
+        if (r != MA_OK) {
+            if (stats) *stats = total;
+            return r;
+        }
+        // the centroids, from host copies of the sites and weights
+        const cudaMemcpyKind toh = mem == MA_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+        const cudaMemcpyKind fromh = mem == MA_MEM_DEVICE ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+        MA_CUDA(c, cudaMemcpy(hx.data(), x, sizeof(double) * n, toh));
+        MA_CUDA(c, cudaMemcpy(hy.data(), y, sizeof(double) * n, toh));
+        MA_CUDA(c, cudaMemcpy(hw.data(), w, sizeof(double) * n, toh));
+        if ((r = ma_moments(cp, mp, n64, hx.data(), hy.data(), hw.data(), MA_MEM_HOST, hm.data(), hf.data(),
+                            nullptr)) != MA_OK)
+            return r;
+        for (size_t i = 0; i < n; i++) {
+            if (!(hm[i] > 0)) continue;  // an empty cell keeps its site
+            const double cx = hf[2 * i] / hm[i], cy = hf[2 * i + 1] / hm[i];
+            hx[i] += tau * (hx[i] - cx);
+            hy[i] += tau * (hy[i] - cy);
+        }
+        MA_CUDA(c, cudaMemcpy(x, hx.data(), sizeof(double) * n, fromh));
+        MA_CUDA(c, cudaMemcpy(y, hy.data(), sizeof(double) * n, fromh));
+    }
+    if (stats) *stats = total;
+    return MA_OK;
+}
+
 }  // extern "C"

@@ -128,3 +128,48 @@ def unit_grid(n: int, values: np.ndarray) -> GridMesh:
     """``n x n`` vertices on [0, 1]^2."""
     g = np.linspace(0.0, 1.0, n)
     return GridMesh(g, g.copy(), values)
+
+
+def read_pgm(path) -> np.ndarray:
+    """A grey image from a PGM file (P2 text or P5 binary, 8 or 16 bit) as a
+    ``(height, width)`` float array, rows top first (the CImg layout of the reference's
+    image inputs, functions.hpp:82-120); 16-bit values are scaled to 0..255."""
+    with open(path, "rb") as fh:
+        data = fh.read()
+    tokens = []
+    pos = 0
+    while len(tokens) < 4:
+        while pos < len(data) and chr(data[pos]).isspace():
+            pos += 1
+        if data[pos:pos + 1] == b"#":
+            while pos < len(data) and data[pos:pos + 1] not in (b"\n", b"\r"):
+                pos += 1
+            continue
+        start = pos
+        while pos < len(data) and not chr(data[pos]).isspace():
+            pos += 1
+        tokens.append(data[start:pos].decode())
+    magic, w, h, maxval = tokens[0], int(tokens[1]), int(tokens[2]), int(tokens[3])
+    if magic == "P5":
+        pos += 1  # the single whitespace after the header
+        dt = np.uint8 if maxval < 256 else np.dtype(">u2")
+        img = np.frombuffer(data, dtype=dt, count=w * h, offset=pos).astype(np.float64)
+    elif magic == "P2":
+        img = np.array(data[pos:].split()[: w * h], dtype=np.float64)
+    else:
+        raise ValueError("not a PGM file: " + magic)
+    img = img.reshape(h, w)
+    if maxval > 255:
+        img = img * (255.0 / maxval)
+    return img
+
+
+def image_grid(pixels) -> GridMesh:
+    """``image_to_pl_function`` (functions.hpp:82-120): the image's vertex grid on
+    [-1, 1]^2 with values ``pixel / 255 + 1e-3``, row ``j`` (bottom up) from image row
+    ``height - 1 - j``; each square split along its (i, j)-(i+1, j+1) diagonal."""
+    p = np.asarray(pixels, dtype=np.float64)
+    h, w = p.shape
+    gx = np.linspace(-1.0, 1.0, w)
+    gy = np.linspace(-1.0, 1.0, h)
+    return GridMesh(gx, gy, p[::-1, :] / 255.0 + 1e-3)
