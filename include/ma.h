@@ -16,6 +16,8 @@
  *                                                     include/MA/voronoi_triangulation_intersection.hpp:315-343
  *   ma_ot_solve_batch  no counterpart in the reference: many problems, solved concurrently
  *   ma_draw_laguerre   MA::draw_laguerre_diagram        include/MA/rasterization.hpp:516-547
+ *   ma_polygon_cells   MA::voronoi_polygon_intersection, for every site at once
+ *                                                     include/MA/voronoi_polygon_intersection.hpp:153-188
  *   ma_kantorovich_vjp no counterpart in the reference: the adjoint of ma_kantorovich
  *                      and ma_moments (vector-Jacobian product)
  *   ma_mesh_create_image image_to_pl_function           include/MA/functions.hpp:82-120
@@ -277,6 +279,27 @@ ma_status ma_pieces(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x
                     const double* w, ma_mem mem, int64_t* npieces, int64_t* nverts);
 ma_status ma_pieces_copy(ma_ctx* ctx, int32_t* site, int32_t* tri, int64_t* off, double* xy, int32_t* edge,
                          ma_mem mem);
+
+/* MA::voronoi_polygon_intersection (voronoi_polygon_intersection.hpp:153-188), run
+ * for every site: the Laguerre cell of each site (weights w, or the Voronoi cell when
+ * w is null) intersected with the polygon (px[e], py[e]), e < k, 3 <= k <= 64 -- the
+ * reference's polygon P, here in host memory.  P need not be convex: as in the
+ * reference's Pgon_intersector (:116-149) it is clipped by the half-planes of the
+ * site's neighbours, so a non-convex P can give a polygon with bridging edges of zero
+ * area.  ma_polygon_cells returns the total vertex count; ma_polygon_cells_copy
+ * fills (each pointer nullable):
+ *   off[n+1]    first vertex of site i's polygon (original order); off[n] = nverts;
+ *               an empty intersection has off[i] = off[i+1]
+ *   xy[2 nv]    vertices (x, y), in P's orientation; P's own corners are copied exactly
+ *   edge[nv]    the edge from vertex k to vertex k+1: the neighbouring site whose
+ *               radical axis it lies on (original index; the reference's DELAUNAY
+ *               edge), or -1-e for edge e (P_e -> P_e+1) of P (the reference's POLYGON
+ *               edge).
+ * The predicates are exact (filters with an exact fallback); MA_ERR_CAPACITY when a
+ * cell needs more than 256 slots or vertices. */
+ma_status ma_polygon_cells(ma_ctx* ctx, int64_t n, const double* x, const double* y, const double* w,
+                           const double* px, const double* py, int k, ma_mem mem, int64_t* nverts);
+ma_status ma_polygon_cells_copy(ma_ctx* ctx, int64_t* off, double* xy, int32_t* edge, ma_mem mem);
 
 /* MA::draw_laguerre_diagram (rasterization.hpp:516-547): every piece rasterised with
  * exact pixel coverage into image[height][width][channels] (row y = 0 first; pixel

@@ -277,6 +277,62 @@ def pieces(mesh, X, weights, y=None, ctx: Context | None = None) -> Pieces:
     return Pieces(site, tri, off, xy, edge)
 
 
+@dataclass
+class PolygonCells:
+    """Every cell clipped to one polygon (``MA::voronoi_polygon_intersection`` for each
+    site): site ``i``'s polygon is ``xy[off[i]:off[i+1]]`` (empty when the cell misses
+    the polygon); ``edge[v]`` labels the edge from vertex ``v`` to the next: the
+    neighbouring site, or ``-1-e`` for edge ``e`` of the clipping polygon."""
+    off: np.ndarray
+    xy: np.ndarray
+    edge: np.ndarray
+
+    def polygon(self, i):
+        return self.xy[self.off[i]:self.off[i + 1]], self.edge[self.off[i]:self.off[i + 1]]
+
+    def areas(self):
+        """Signed shoelace area of every site's polygon."""
+        x, y = self.xy[:, 0], self.xy[:, 1]
+        nxt = np.arange(x.shape[0]) + 1
+        n = self.off.shape[0] - 1
+        a = np.zeros(n)
+        nz = self.off[1:] > self.off[:-1]
+        nxt[self.off[1:][nz] - 1] = self.off[:-1][nz]
+        cr = x * y[nxt] - x[nxt] * y
+        a[nz] = 0.5 * np.add.reduceat(cr, self.off[:-1][nz]) if cr.size else 0.0
+        return a
+
+
+def voronoi_polygon_intersection(polygon, X, weights=None, y=None, ctx: Context | None = None) -> PolygonCells:
+    """``MA::voronoi_polygon_intersection`` (voronoi_polygon_intersection.hpp:153-188)
+    for every site at once (``ma_polygon_cells`` + ``ma_polygon_cells_copy``):
+    ``polygon`` is ``(k, 2)`` corners, 3 <= k <= 64; ``weights`` None gives the Voronoi
+    cells."""
+    ctx = ctx or default_context()
+    P = np.ascontiguousarray(polygon, dtype=np.float64).reshape(-1, 2)
+    qx, qy = np.ascontiguousarray(P[:, 0]), np.ascontiguousarray(P[:, 1])
+    x, yy = _split_xy(X, y)
+    if weights is None:
+        a = _Args(x, yy)
+        wp = ctypes.c_void_p(None)
+    else:
+        a = _Args(x, yy, weights)
+        wp = a.ptrs[2]
+    n = int(a.keep[0].shape[0])
+    nvt = ctypes.c_int64()
+    st = ctx.lib.ma_polygon_cells(ctx.h, n, a.ptrs[0], a.ptrs[1], wp, ctypes.c_void_p(qx.ctypes.data),
+                                  ctypes.c_void_p(qy.ctypes.data), int(P.shape[0]), a.mem, ctypes.byref(nvt))
+    _check(ctx.lib, ctx.h, st, "ma_polygon_cells")
+    nv = int(nvt.value)
+    off = np.empty(n + 1, np.int64)
+    xy = np.empty((nv, 2), np.float64)
+    edge = np.empty(nv, np.int32)
+    vp = lambda arr: ctypes.c_void_p(arr.ctypes.data)
+    st = ctx.lib.ma_polygon_cells_copy(ctx.h, vp(off), vp(xy), vp(edge), L.MA_MEM_HOST)
+    _check(ctx.lib, ctx.h, st, "ma_polygon_cells_copy")
+    return PolygonCells(off, xy, edge)
+
+
 def draw_laguerre_diagram(mesh, X, weights, colors, bbox, width: int, height: int, image=None, y=None,
                           ctx: Context | None = None):
     """``MA::draw_laguerre_diagram`` (``ma_draw_laguerre``): every cell-triangle piece

@@ -67,6 +67,13 @@ MeshTriDev Mesh::tri_dev() const
 // sort, the radix tree and its node boxes.  Positions only: once per set of sites.
 ma_status build_site_index(Ctx* c, const Mesh* m, int n, const double* x, const double* y, const double* w)
 {
+    return build_site_index_box(c, m->X0, m->Y0, m->X1, m->Y1, n, x, y, w);
+}
+
+// the same over the bounding box of the sites and of the box [X0, X1] x [Y0, Y1]
+ma_status build_site_index_box(Ctx* c, double X0, double Y0, double X1, double Y1, int n, const double* x,
+                               const double* y, const double* w)
+{
     cudaStream_t s = c->stream;
     if (n >= (1 << 24)) return fail(c, MA_ERR_INVALID_ARGUMENT, "at most 2^24 - 1 sites per problem");
     MA_CUDA(c, c->keys.ensure(8 * sizeof(unsigned long long)));
@@ -81,10 +88,10 @@ ma_status build_site_index(Ctx* c, const Mesh* m, int n, const double* x, const 
     double xmin = c->hstat[0], xmax = c->hstat[1], ymin = c->hstat[2], ymax = c->hstat[3];
     if (!(std::isfinite(xmin) && std::isfinite(xmax) && std::isfinite(ymin) && std::isfinite(ymax)))
         return fail(c, MA_ERR_INVALID_ARGUMENT, "non-finite site coordinates");
-    xmin = std::min(xmin, m->X0);
-    xmax = std::max(xmax, m->X1);
-    ymin = std::min(ymin, m->Y0);
-    ymax = std::max(ymax, m->Y1);
+    xmin = std::min(xmin, X0);
+    xmax = std::max(xmax, X1);
+    ymin = std::min(ymin, Y0);
+    ymax = std::max(ymax, Y1);
     int nb = radix_sort_blocks(n);
     size_t nn = (size_t)n;
     size_t ni = nn > 1 ? nn - 1 : 1;
@@ -401,6 +408,19 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     return MA_OK;
 }
 
+// stage caller arrays on the device: host arrays are copied into context buffers
+ma_status stage_in(Ctx* c, DevBuf& buf, const double* src, int64_t n, ma_mem mem, const double** dst)
+{
+    if (mem == MA_MEM_DEVICE) {
+        *dst = src;
+        return MA_OK;
+    }
+    MA_CUDA(c, buf.ensure(sizeof(double) * (size_t)n));
+    MA_CUDA(c, cudaMemcpyAsync(buf.p, src, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    *dst = buf.as<double>();
+    return MA_OK;
+}
+
 }  // namespace ma
 
 // ---------------------------------------------------------------------------
@@ -467,7 +487,8 @@ void ma_ctx_destroy(ma_ctx* c)
     DevBuf* bufs[] = {&c->counters, &c->nb_cnt, &c->nb_lab, &c->cell_box, &c->hx, &c->hy, &c->hw, &c->hnu, &c->abortf, &c->vjp_cm, &c->vjp_cf,
                       &c->vjp_gx, &c->vjp_gy, &c->vjp_gw, &c->vjp_gr, &c->pc_cnt, &c->pv_cnt,
                       &c->pc_base, &c->pv_base, &c->pc_site, &c->pc_tri, &c->pc_off, &c->pc_xy, &c->pc_edge,
-                      &c->raster_col, &c->raster_img, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
+                      &c->raster_col, &c->raster_img, &c->pg_poly, &c->pg_cnt, &c->pg_base, &c->pg_off,
+                      &c->pg_xy, &c->pg_edge, &c->pg_list, &c->pg_work, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
                       &c->perm, &c->sites, &c->posf, &c->scan_scratch, &c->fill, &c->t_child, &c->t_range,
                       &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab,
                       &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,
@@ -776,19 +797,6 @@ ma_status ma_mesh_total_mass(const ma_mesh* m, double* out)
 {
     if (!m || !out) return MA_ERR_INVALID_ARGUMENT;
     *out = m->total_mass;
-    return MA_OK;
-}
-
-// stage caller arrays on the device: host arrays are copied into context buffers
-static ma_status stage_in(ma_ctx* c, DevBuf& buf, const double* src, int64_t n, ma_mem mem, const double** dst)
-{
-    if (mem == MA_MEM_DEVICE) {
-        *dst = src;
-        return MA_OK;
-    }
-    MA_CUDA(c, buf.ensure(sizeof(double) * (size_t)n));
-    MA_CUDA(c, cudaMemcpyAsync(buf.p, src, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
-    *dst = buf.as<double>();
     return MA_OK;
 }
 

@@ -59,13 +59,17 @@ struct Owner {
     int self;          // sorted index
 };
 
-// fixed points of the fixed edges: box corners or triangle corners
-struct Fixed {
+// fixed points of the fixed edges: box corners, triangle corners, or the corners of
+// a clipping polygon (FC of them at most)
+template <int FC>
+struct FixedN {
+    static constexpr int kCap = FC;
     int n;
-    float ux[4], uy[4], ur[4];  // owner-relative FP32 and per-component error
-    double rx[4], ry[4];        // owner-relative FP64
-    double ax[4], ay[4];        // absolute (exact input doubles)
+    float ux[FC], uy[FC], ur[FC];  // owner-relative FP32 and per-component error
+    double rx[FC], ry[FC];         // owner-relative FP64
+    double ax[FC], ay[FC];         // absolute (exact input doubles)
 };
+using Fixed = FixedN<4>;
 
 template <int CAP>
 struct Poly {
@@ -105,7 +109,8 @@ MA_HD Slot make_slot(int site, const SiteD& c, const Owner& o)
     return s;
 }
 
-MA_HD void set_fixed(Fixed& f, int k, double ax, double ay, const Owner& o)
+template <class FX>
+MA_HD void set_fixed(FX& f, int k, double ax, double ay, const Owner& o)
 {
     f.ax[k] = ax;
     f.ay[k] = ay;
@@ -310,8 +315,8 @@ MA_HDNI int exact_side2(const Owner& o, const SiteD& a, const SiteD& b, const Si
 // Is the vertex between edges `prev` and `cur` strictly closer to the owner than
 // to slot c's site?  (Tri_intersector::inside, vti.hpp:129-166.)  Without EXACT an
 // undecided filter sets `undecided` (the caller redoes the cell with EXACT).
-template <int CAP, bool EXACT>
-MA_HDNI bool sym_inside(int prev, int cur, const Slot* slots, const Fixed& fx, const Owner& o, const SiteD* sites,
+template <int CAP, bool EXACT, class FX>
+MA_HDNI bool sym_inside(int prev, int cur, const Slot* slots, const FX& fx, const Owner& o, const SiteD* sites,
                         int csite, uint32_t& st, bool& undecided)
 {
     const SiteD c = sites[csite];
@@ -351,7 +356,8 @@ MA_HD void sanitize(float& ux, float& uy, float& ur)
 }
 
 // crossing of fixed edge e (fixed point e -> e+1) with the radical axis of slot a
-MA_HD void vtx_fixed_bis(const Fixed& fx, int e, const Slot& a, float& ux, float& uy, float& ur)
+template <class FX>
+MA_HD void vtx_fixed_bis(const FX& fx, int e, const Slot& a, float& ux, float& uy, float& ur)
 {
     int e1 = (e + 1 == fx.n) ? 0 : e + 1;
     F px{fx.ux[e], fx.ur[e]}, py{fx.uy[e], fx.ur[e]};
@@ -384,8 +390,8 @@ MA_HD void vtx_bis_bis(const Slot& a, const Slot& b, float& ux, float& uy, float
     sanitize(ux, uy, ur);
 }
 
-template <int CAP>
-MA_HD void new_vertex(int edge, int cslot, const Slot* slots, const Fixed& fx, float& ux, float& uy, float& ur)
+template <int CAP, class FX>
+MA_HD void new_vertex(int edge, int cslot, const Slot* slots, const FX& fx, float& ux, float& uy, float& ur)
 {
     if (edge < 0)
         vtx_fixed_bis(fx, -1 - edge, slots[cslot], ux, uy, ur);
@@ -397,8 +403,8 @@ MA_HD void new_vertex(int edge, int cslot, const Slot* slots, const Fixed& fx, f
 // Returns false (and leaves Q untouched) when no vertex lies outside.  Sets
 // `overflow` when the result would exceed CAP, or (without EXACT) when a vertex
 // needs exact arithmetic.
-template <int CAP, bool EXACT>
-MA_HD bool clip_poly(const Poly<CAP>& P, Poly<CAP>& Q, int cs, const Slot* slots, const Fixed& fx,
+template <int CAP, bool EXACT, class FX>
+MA_HD bool clip_poly(const Poly<CAP>& P, Poly<CAP>& Q, int cs, const Slot* slots, const FX& fx,
                      const Owner& o, const SiteD* sites, uint32_t& st, bool& overflow)
 {
     const int n = P.n;
@@ -480,7 +486,8 @@ MA_HD Nb64 make_nb64(const SiteD& c, const Owner& o)
 }
 
 // FP64 vertex between edges prev and cur (owner-relative)
-MA_HD void vtx64(int prev, int cur, const Nb64* nb, const Fixed& fx, double& X, double& Y)
+template <class FX>
+MA_HD void vtx64(int prev, int cur, const Nb64* nb, const FX& fx, double& X, double& Y)
 {
     if (prev < 0 && cur < 0) {
         int e = -1 - cur;

@@ -97,6 +97,10 @@ struct Ctx {
     int64_t npieces = 0, npverts = 0;
     bool have_pieces = false;
     DevBuf raster_col, raster_img;  // rasterisation staging (host callers)
+    // cells clipped to a polygon, of the last ma_polygon_cells call (original site order)
+    DevBuf pg_poly, pg_cnt, pg_base, pg_off, pg_xy, pg_edge, pg_list, pg_work;
+    int64_t pg_n = 0, pg_nv = 0;
+    bool have_pgon = false;
     bool aborted = false;                          // the last evaluation stopped at an empty cell
     DevBuf counters;                               // stage-1 search counters (profiling)
     DevBuf info;  // status, nredo, nnz
@@ -133,6 +137,10 @@ ma_status cuda_fail(Ctx* c, cudaError_t e, const char* what);
 
 // evaluation pipeline (device pointers)
 ma_status build_site_index(Ctx* c, const Mesh* m, int n, const double* x, const double* y, const double* w);
+ma_status build_site_index_box(Ctx* c, double X0, double Y0, double X1, double Y1, int n, const double* x,
+                               const double* y, const double* w);
+// caller arrays on the device: host arrays are copied into `buf`, device arrays used in place
+ma_status stage_in(Ctx* c, DevBuf& buf, const double* src, int64_t n, ma_mem mem, const double** dst);
 // adjoint of one evaluation: cotangents in, gradients out (device, original order)
 struct VjpArgs {
     double cot_value = 0.0;

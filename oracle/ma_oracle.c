@@ -1687,3 +1687,66 @@ int ora_side3(const double *v, const double *u, const double *p, const double *q
     pred_stats st = {0, 0};
     return side3(&A, &U, p[0], p[1], q[0], q[1], &W, &st);
 }
+
+/* ------------------------------------------------------------------------- */
+/* one cell clipped to a polygon (voronoi_polygon_intersection.hpp:27-188)    */
+/* ------------------------------------------------------------------------- */
+
+/* MA::voronoi_polygon_intersection(P, dt, v) for site v: the polygon (qx, qy)[0..k)
+ * as the symbolic edges (e, e+1) (:160-161), clipped in turn by the half-plane of v
+ * against each candidate neighbour (Pgon_intersector::operator(), :116-149, the same
+ * Sutherland-Hodgman step as Tri_intersector's), then each vertex -- the pair of its
+ * two edges -- made a point (vertex_to_point, :64-69).  The reference clips by the
+ * triangulation's neighbours of v; the candidates here are a superset (the regular
+ * triangulation's neighbours and theirs), which changes nothing because every test
+ * is exact.  Coordinates in double-double rounded to double (the corners of P
+ * copied).  Vertex j is the start of edge lab[j]: a neighbour's index, or -1-e for
+ * edge e of P.  Returns the vertex count (0: empty), or -1 beyond `cap`. */
+int ora_polygon_cell(int n, const double *x, const double *y, const double *w, int v, const int *cand,
+                     int ncand, int k, const double *qx, const double *qy, int cap, double *xy, int *lab)
+{
+    site_t *S = (site_t *)malloc(sizeof(site_t) * (size_t)n);
+    pedge *A = (pedge *)malloc(sizeof(pedge) * PMAX), *B = (pedge *)malloc(sizeof(pedge) * PMAX);
+    for (int i = 0; i < n; i++) { S[i].x = x[i]; S[i].y = y[i]; S[i].w = w[i]; }
+    geo_t G;
+    memset(&G, 0, sizeof G);
+    G.px = qx;
+    G.py = qy;
+    G.s = S;
+    int m = k;
+    for (int e = 0; e < k; e++) { A[e].t = 0; A[e].a = e; A[e].b = (e + 1) % k; }
+    for (int c = 0; c < ncand && m > 0; c++) {
+        int u = cand[c];
+        if (u == v) continue;
+        if (S[u].x == S[v].x && S[u].y == S[v].y) {
+            /* coincident sites: the larger weight, then the lower index, keeps the cell */
+            if (S[u].w > S[v].w || (S[u].w == S[v].w && u < v)) m = 0;
+            continue;
+        }
+        m = clip(&G, A, m, v, u, B);
+        pedge *t = A; A = B; B = t;
+    }
+    int out = m;
+    if (m > cap) {
+        out = -1;
+    } else {
+        for (int j = 0; j < m; j++) {
+            pedge e0 = A[(j + m - 1) % m], e1 = A[j];
+            if (e0.t == 0 && e1.t == 0) {
+                int p = common_pt(e0, e1);
+                xy[2 * j] = qx[p];
+                xy[2 * j + 1] = qy[p];
+            } else {
+                dd X, Y;
+                vertex_to_point_dd(&G, e0, e1, &X, &Y);
+                xy[2 * j] = dd_d(X);
+                xy[2 * j + 1] = dd_d(Y);
+            }
+            lab[j] = e1.t == 0 ? -1 - e1.a : e1.b;
+        }
+    }
+    free(S);
+    free(A);
+    free(B);
+    return out;
+}

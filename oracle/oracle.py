@@ -8,7 +8,9 @@ The oracle restates the reference's algorithm on the CPU in FP64:
 * :func:`ot_solve` -- ``MA::ot_solve`` (include/MA/optimal_transport.hpp:89-193) with
   ``solve_laplacian_matrix`` (optimal_transport.hpp:41-87) done by a direct sparse
   factorisation of the Hessian with its last row and column removed;
-* :func:`lloyd` -- ``MA::lloyd`` (lloyd.hpp:126-144).
+* :func:`lloyd` -- ``MA::lloyd`` (lloyd.hpp:126-144);
+* :func:`polygon_cells` -- ``MA::voronoi_polygon_intersection``
+  (include/MA/voronoi_polygon_intersection.hpp:27-188) for every site.
 
 Parity unpinned against reference outputs (the reference cannot be built here and
 its tests hold no golden vectors).  Only the test-suite, the smoke check and the
@@ -70,6 +72,9 @@ def lib():
         L.ora_side2.argtypes = [_dp, _dp, _dp, _dp]
         L.ora_side3.restype = ctypes.c_int
         L.ora_side3.argtypes = [_dp, _dp, _dp, _dp, _dp]
+        L.ora_polygon_cell.restype = ctypes.c_int
+        L.ora_polygon_cell.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int,
+                                       _dp, _dp, ctypes.c_int, _dp, _ip]
         _lib = L
     return _lib
 
@@ -245,6 +250,38 @@ def kantorovich(mesh, x, y, w, mode: int = 1, keep_pieces: bool = False, arith: 
                        L.ora_total_area(h), nbrs, int(st[0]), int(st[1]), pieces)
     finally:
         L.ora_free(h)
+
+
+def polygon_cells(x, y, w, qx, qy):
+    """``MA::voronoi_polygon_intersection`` (voronoi_polygon_intersection.hpp:153-188)
+    for every site: ``(off, xy, lab)`` with site i's polygon at ``xy[off[i]:off[i+1]]``;
+    ``lab[j]`` is the edge starting at vertex j (a neighbour's index, or -1-e for edge e
+    of the polygon).  Candidates: the regular triangulation's neighbours and theirs."""
+    L = lib()
+    x, px = _d(x)
+    y, py = _d(y)
+    w, pw = _d(w)
+    qx, pqx = _d(qx)
+    qy, pqy = _d(qy)
+    n, k = x.shape[0], qx.shape[0]
+    cs, cl = candidates(x, y, w, 2)
+    cap = 512
+    out_xy = np.zeros((cap, 2))
+    out_lab = np.zeros(cap, np.int32)
+    xs, labs, off = [], [], [0]
+    for i in range(n):
+        c = np.ascontiguousarray(cl[cs[i]:cs[i + 1]], dtype=np.int32)
+        if c.size == 0:
+            c = np.zeros(1, np.int32) + i
+        m = L.ora_polygon_cell(n, px, py, pw, i, c.ctypes.data_as(_ip), int(cs[i + 1] - cs[i]), k, pqx, pqy, cap,
+                               out_xy.ctypes.data_as(_dp), out_lab.ctypes.data_as(_ip))
+        if m < 0:
+            raise RuntimeError("oracle polygon capacity")
+        xs.append(out_xy[:m].copy())
+        labs.append(out_lab[:m].copy())
+        off.append(off[-1] + m)
+    return (np.array(off, np.int64), np.concatenate(xs) if xs else np.zeros((0, 2)),
+            np.concatenate(labs) if labs else np.zeros(0, np.int32))
 
 
 def side1(v, w, e):

@@ -254,3 +254,78 @@ def test_cocircular_quadruples_have_no_exact_ties(oracle):
     A = {(int(i), int(j)) for i, j in zip(a.rows, a.cols)}
     B = {(int(perm[i]), int(perm[j])) for i, j in zip(b.rows, b.cols)}
     assert A == B
+
+
+def _shoelace(xy):
+    if xy.shape[0] == 0:
+        return 0.0
+    x, y = xy[:, 0], xy[:, 1]
+    return 0.5 * np.sum(x * np.roll(y, -1) - np.roll(x, -1) * y)
+
+
+def test_polygon_cells_area_invariants(oracle):
+    # voronoi_polygon_intersection over every site: [-1, 1]^2 gives 4
+    # (tests/test_voronoi.cpp:39-50), the 12-corner cross of
+    # tests/test_voronoi_ad.cpp:30-57 gives 12
+    rng = np.random.default_rng(1)
+    X = rng.uniform(-1, 1, (800, 2))
+    sq = np.array([[-1, -1], [1, -1], [1, 1], [-1, 1]], dtype=np.float64)
+    off, xy, _ = oracle.polygon_cells(X[:, 0], X[:, 1], np.zeros(800), sq[:, 0], sq[:, 1])
+    a = np.array([_shoelace(xy[off[i]:off[i + 1]]) for i in range(800)])
+    assert a.min() > 0 and abs(a.sum() - 4.0) < 1e-12
+    cross = np.array([[1, -1], [2, -1], [2, 1], [1, 1], [1, 2], [-1, 2], [-1, 1], [-2, 1], [-2, -1], [-1, -1],
+                      [-1, -2], [1, -2]], dtype=np.float64)
+    off, xy, _ = oracle.polygon_cells(X[:, 0], X[:, 1], np.zeros(800), cross[:, 0], cross[:, 1])
+    a = np.array([_shoelace(xy[off[i]:off[i + 1]]) for i in range(800)])
+    assert abs(a.sum() - 12.0) < 1e-11
+
+
+def test_polygon_cells_agree_with_pieces(oracle):
+    # clipped to the mesh's box, each site's polygon has the area of its pieces, and
+    # its neighbour labels are the site's regular-triangulation neighbours
+    rng = np.random.default_rng(2)
+    n = 300
+    X = rng.uniform(0, 1, (n, 2))
+    w = rng.uniform(-1, 1, n) * 3e-3
+    mesh = unit_grid(9, np.ones(81))
+    r = oracle.kantorovich(mesh, X[:, 0], X[:, 1], w, keep_pieces=True)
+    P = r.pieces
+    piece_area = np.zeros(n)
+    for k in range(P.site.shape[0]):
+        piece_area[P.site[k]] += _shoelace(P.xy[P.offsets[k]:P.offsets[k + 1]])
+    box = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], dtype=np.float64)
+    off, xy, lab = oracle.polygon_cells(X[:, 0], X[:, 1], w, box[:, 0], box[:, 1])
+    a = np.array([_shoelace(xy[off[i]:off[i + 1]]) for i in range(n)])
+    np.testing.assert_allclose(a, piece_area, rtol=0, atol=1e-14)
+    for i in range(n):
+        nb = set(int(v) for v in lab[off[i]:off[i + 1]] if v >= 0)
+        assert nb == set(int(v) for v in r.neighbors[i])
+
+
+def test_polygon_cells_candidates_change_nothing(oracle):
+    # clipping by every other site gives the same polygons as the triangulation's
+    # neighbours: the candidate lists hide no cut
+    rng = np.random.default_rng(3)
+    n = 90
+    X = rng.uniform(-1, 1, (n, 2))
+    w = rng.uniform(-1, 1, n) * 1e-2
+    q = np.array([[-0.8, -0.9], [0.9, -0.7], [0.6, 0.8], [-0.7, 0.5]])
+    off, xy, lab = oracle.polygon_cells(X[:, 0], X[:, 1], w, q[:, 0], q[:, 1])
+    L = oracle.lib()
+    import ctypes
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    xs, ys, ws = (np.ascontiguousarray(v) for v in (X[:, 0], X[:, 1], w))
+    qx, qy = np.ascontiguousarray(q[:, 0]), np.ascontiguousarray(q[:, 1])
+    allc = np.arange(n, dtype=np.int32)
+    out = np.zeros((512, 2))
+    ol = np.zeros(512, np.int32)
+    for i in range(n):
+        m = L.ora_polygon_cell(n, xs.ctypes.data_as(dp), ys.ctypes.data_as(dp), ws.ctypes.data_as(dp), i,
+                               allc.ctypes.data_as(ip), n, 4, qx.ctypes.data_as(dp), qy.ctypes.data_as(dp), 512,
+                               out.ctypes.data_as(dp), ol.ctypes.data_as(ip))
+        assert m == off[i + 1] - off[i]
+        if m:
+            a = xy[off[i]:off[i + 1]]
+            s = int(np.argmin(np.abs(out[:m] - a[0]).max(1)))
+            np.testing.assert_array_equal(np.roll(out[:m], -s, axis=0), a)
