@@ -7,13 +7,24 @@
 // multigrid built on the device at every Newton step:
 //
 //   * the fine level is H copied into Morton order (the order of the site index),
-//     so that neighbouring rows are close in memory; every level is then
-//     aggregated the same way, consecutive rows per aggregate (kAggFine on the fine
-//     level, kAggCoarse below), spatially compact without any graph search;
+//     so that neighbouring rows are close in memory;
+//   * every level is aggregated by strength, in two pairwise passes (pairwise
+//     aggregation, Notay 2010): each pass matches every row with its strongest
+//     neighbour (largest -a_ij) by handshakes -- a row and its strongest free
+//     neighbour pair up when each is the other's choice, over four rounds -- and a
+//     row left alone joins the pair of its strongest matched neighbour (one such
+//     row per pair).  The second pass pairs the first pass's aggregates on their
+//     Galerkin matrix, so an aggregate holds up to nine rows (about 4.6 on the
+//     Hessians of the 100,000-site workload).  Every choice is a deterministic
+//     function of the matrix (ties go to the lower index; claims by atomicMin), and
+//     the aggregates are numbered in the order of their first row.  A level whose
+//     matching stalls (fewer than 1.5 rows per aggregate) is grouped by four
+//     consecutive rows instead;
 //   * the coarse matrices are Galerkin products P^T A P with the piecewise-constant
 //     prolongation P: a coarse entry (I, J) is the sum of the fine entries (i, j)
-//     with i in I and j in J.  Each coarse row is assembled by one warp, its
-//     duplicates summed in a fixed order (reproducible results);
+//     with i in I and j in J.  Each coarse row is assembled by one warp from the
+//     aggregate's member rows, its duplicates summed in a fixed order (reproducible
+//     results);
 //   * smoothing is damped Jacobi (one sweep before, one after), the coarse
 //     correction is scaled by kCoarseScale (piecewise-constant prolongation
 //     underestimates the smooth error), and the coarsest level (at most kCoarsest
@@ -21,8 +32,8 @@
 //   * the whole preconditioned CG -- every level of every V-cycle -- runs in one
 //     cooperative kernel with grid barriers between the phases; no host round trip
 //     per iteration.
-// Rows that are inactive (the gauge row n-1 and empty cells: zero diagonal) are
-// held at zero on every level.
+// Rows that are inactive (the gauge row n-1 and empty cells: zero diagonal) belong
+// to no aggregate and are held at zero on every level.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -33,31 +44,28 @@ namespace cg = cooperative_groups;
 
 namespace ma {
 
-constexpr int kAggFine = 4;    // fine rows per aggregate (four lanes of the fused fine restriction)
-constexpr int kAggCoarse = 4;  // coarse rows per aggregate on the levels below (8 gives fewer
-                               // levels but more iterations: slower on the 100k-site workload)
-__host__ __device__ constexpr int agg_size(int l) { return l == 0 ? kAggFine : kAggCoarse; }
+constexpr int kMatchRounds = 4;     // handshake rounds of a pairwise pass
+constexpr int kAggGroup = 4;        // rows per aggregate where the matching stalls
 constexpr int kCoarsest = 64;       // dense solve at or below this many nodes
 constexpr int kRowCap = 512;        // gathered entries of one coarse row
 constexpr int kRowWarps = 4;        // coarse rows per block in the setup
 constexpr double kOmega = 2.0 / 3.0;
 constexpr double kCoarseScale = 1.5;
-static_assert(kAggFine == 4, "the fine aggregate sums use two shuffle steps");
 
 // ---------------------------------------------------------------------------
 // setup: coarse rows
 // ---------------------------------------------------------------------------
 struct CoarseSrc {
-    int agg;           // rows per aggregate
-    int n;             // fine nodes
+    const int* mp;     // members of aggregate I: mem[mp[I] .. mp[I+1])
+    const int* mem;
+    const int* map;    // fine node -> aggregate (-1: inactive)
     const int* rp;     // fine CSR
     const int* ci;
     const double* va;
-    const double* dinv;  // 0 marks an inactive fine node
 };
 
-// One warp per coarse row: gather the member rows (active columns only) mapped to
-// aggregates, keep the first occurrence of each aggregate, sum its duplicates in
+// One warp per coarse row: gather the member rows' entries in active columns, mapped
+// to aggregates, keep the first occurrence of each aggregate, sum its duplicates in
 // gather order, and place it by rank of its column.  FILL = false counts the
 // distinct columns into cnt[I]; FILL = true writes them at rp[I].
 template <bool FILL>
@@ -75,21 +83,16 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_coarse_rows(CoarseSrc s, int
     unsigned char* lead = slead[wib];
     int E = 0;
     bool over = false;
-    for (int q = 0; q < s.agg && !over; q++) {
-        const int i = I * s.agg + q;
-        if (i >= s.n) break;
-        if (s.dinv[i] == 0.0) continue;
+    for (int q = s.mp[I]; q < s.mp[I + 1] && !over; q++) {
+        const int i = s.mem[q];
         const int k0 = s.rp[i], k1 = s.rp[i + 1];
         for (int b = k0; b < k1; b += 32) {
             const int k = b + lane;
             int c = -1;
             double v = 0.0;
             if (k < k1) {
-                const int j = s.ci[k];
-                if (s.dinv[j] != 0.0) {
-                    c = j / s.agg;
-                    v = s.va[k];
-                }
+                c = s.map[s.ci[k]];
+                v = s.va[k];
             }
             const unsigned bal = __ballot_sync(0xffffffffu, c >= 0);
             const int pos = E + __popc(bal & ((1u << lane) - 1u));
@@ -142,6 +145,146 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_coarse_rows(CoarseSrc s, int
         }
         ci[base + rank] = c;
         va[base + rank] = sum;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// setup: pairwise aggregation
+// ---------------------------------------------------------------------------
+struct LevelCsr {
+    int n;
+    const int* rp;
+    const int* ci;
+    const double* va;
+    const double* dinv;  // 0: inactive row
+};
+
+// For every free active row (mate < 0): the strongest active neighbour (largest
+// -a_ij > 0) among the free rows (MATCHED = false) or among the matched rows
+// (MATCHED = true); ties to the lower index; -1 if there is none.
+template <bool MATCHED>
+__global__ void k_strongest(LevelCsr A, const int* mate, int* best)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    int b = -1;
+    if (A.dinv[i] != 0.0 && mate[i] < 0) {
+        double sb = 0.0;
+        for (int k = A.rp[i]; k < A.rp[i + 1]; k++) {
+            const int j = A.ci[k];
+            if (j == i || A.dinv[j] == 0.0 || (mate[j] >= 0) != MATCHED) continue;
+            const double v = -A.va[k];
+            if (v > sb || (v == sb && b >= 0 && j < b)) {
+                sb = v;
+                b = j;
+            }
+        }
+    }
+    best[i] = b;
+}
+
+// a handshake: rows that chose each other become a pair
+__global__ void k_handshake(int n, const int* best, int* mate)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int j = best[i];
+    if (j >= 0 && best[j] == i) mate[i] = j;
+}
+
+// a free row bids for the pair of its strongest matched neighbour (best from
+// k_strongest<true>); the lowest bidder of each pair joins it
+__global__ void k_bid(int n, const int* best, const int* mate, int* claim)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int j = best[i];
+    if (j >= 0) atomicMin(&claim[min(j, mate[j])], i);
+}
+
+// leaders (the lower row of a pair, or an active row that stays alone) flagged for
+// the numbering scan; join[i] = the pair a row joins, else -1
+__global__ void k_leaders(int n, const double* dinv, const int* mate, const int* best, const int* claim, int* flag,
+                          int* join)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int f = 0, jn = -1;
+    if (dinv[i] != 0.0) {
+        const int m = mate[i];
+        if (m >= 0) {
+            f = i < m;
+        } else {
+            const int j = best[i];
+            const int p = j >= 0 ? min(j, mate[j]) : -1;
+            if (p >= 0 && claim[p] == i)
+                jn = p;
+            else
+                f = 1;
+        }
+    }
+    flag[i] = f;
+    join[i] = jn;
+}
+
+// aggregate of every row from the leaders' numbers (-1: inactive)
+__global__ void k_assign(int n, const double* dinv, const int* mate, const int* join, const int* id, int* agg)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int a = -1;
+    if (dinv[i] != 0.0) {
+        if (mate[i] >= 0)
+            a = id[min(i, mate[i])];
+        else if (join[i] >= 0)
+            a = id[join[i]];
+        else
+            a = id[i];
+    }
+    agg[i] = a;
+}
+
+// groups of kAggGroup consecutive active rows (the fallback where matching stalls)
+__global__ void k_group(int n, const double* dinv, int* agg)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) agg[i] = dinv[i] != 0.0 ? i / kAggGroup : -1;
+}
+
+// agg[i] = second[first[i]] (the two passes composed)
+__global__ void k_compose(int n, const int* first, const int* second, int* agg)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) agg[i] = first[i] >= 0 ? second[first[i]] : -1;
+}
+
+// member lists: counts per aggregate, then each row placed after the scan; the
+// members of an aggregate are then sorted by row (at most a few dozen per aggregate)
+__global__ void k_member_count(int n, const int* agg, int* cnt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && agg[i] >= 0) atomicAdd(&cnt[agg[i]], 1);
+}
+
+__global__ void k_member_fill(int n, const int* agg, const int* mp, int* fill, int* mem)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || agg[i] < 0) return;
+    mem[mp[agg[i]] + atomicAdd(&fill[agg[i]], 1)] = i;
+}
+
+__global__ void k_member_sort(int nc, const int* mp, int* mem)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= nc) return;
+    for (int q = mp[I] + 1; q < mp[I + 1]; q++) {
+        const int v = mem[q];
+        int r = q - 1;
+        while (r >= mp[I] && mem[r] > v) {
+            mem[r + 1] = mem[r];
+            r--;
+        }
+        mem[r + 1] = v;
     }
 }
 
@@ -262,9 +405,9 @@ __global__ void k_sell_fill(const int* rp, const int* ci, const double* va, int 
 // fine level runs one thread per row; a coarse level gives each row a team of
 // T = 1 .. 32 adjacent lanes (sized so that the grid covers the level), the lanes
 // striding over the row's entries and summing by shuffles, so that the small levels
-// are not a chain of dependent loads in a few threads.  The four members of a
-// level-l aggregate are consecutive rows of level l, hence one contiguous entry
-// range.  Grid barriers per CG iteration: 2 (nlev - 2) + 3.
+// are not a chain of dependent loads in a few threads.  An aggregate's members are
+// listed (mem[mp[J] .. mp[J+1])); agg maps a row to its aggregate.  Grid barriers
+// per CG iteration: 2 (nlev - 2) + 4.
 constexpr int kAmgMaxLevels = 16;
 constexpr int kAmgThreads = 256;
 
@@ -278,6 +421,9 @@ struct AmgLevelDev {
     double* xp;  // post-smoothed correction
     int tr;      // team size restricting this level into the next
     int tp;      // team size prolonging into this level
+    const int* agg;  // row -> node of the next level (-1: inactive)
+    const int* mp;   // members of node J of the next level: mem[mp[J] .. mp[J+1])
+    const int* mem;
     // level 0 only: the same matrix as sliced ELL, slices of 32 rows stored
     // entry-major (entry e of row 32 s + r at sp[s] + 32 e + r), padded with
     // zero entries pointing at the row itself
@@ -338,8 +484,6 @@ __device__ __forceinline__ double team_sum(double v, int width)
     return v;
 }
 
-__device__ __forceinline__ int round32(int n) { return (n + 31) & ~31; }
-
 // Loop over rows [0, nrows) with teams of T lanes: calls fn(row, lane_in_team)
 // with row < nrows, or row = -1 for lanes without a row in this round (they still
 // take part in the team's shuffles).  Warp-uniform trip count.
@@ -367,14 +511,31 @@ __device__ __forceinline__ void restrict_level(const AmgPcgArgs& a, int l)
     team_rows(C.n, T, [&](int J, int t) {
         double s = 0.0;
         if (J >= 0) {
-            const int S = agg_size(l);
-            const int I0 = J * S, I1 = min(I0 + S, A.n);
-            for (int q = t; q < I1 - I0; q += T) s += A.b[I0 + q];
-            for (int k = A.rp[I0] + t; k < A.rp[I1]; k += T) {
-                const int K = A.ci[k];
-                s -= A.va[k] * (kOmega * A.dinv[K] * A.b[K]);
+            for (int q = A.mp[J]; q < A.mp[J + 1]; q++) {
+                const int I = A.mem[q];
+                if (t == 0) s += A.b[I];
+                for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) {
+                    const int K = A.ci[k];
+                    s -= A.va[k] * (kOmega * A.dinv[K] * A.b[K]);
+                }
             }
         }
+        s = team_sum(s, T);
+        if (J >= 0 && t == 0) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
+    });
+}
+
+// b_1 from the fine level: the fine residuals of the pre-smoothed correction (in s)
+// summed over each aggregate
+__device__ __forceinline__ void restrict_fine(const AmgPcgArgs& a, const double* s_fine)
+{
+    const AmgLevelDev& F = a.L[0];
+    const AmgLevelDev& C = a.L[1];
+    const int T = F.tr;
+    team_rows(C.n, T, [&](int J, int t) {
+        double s = 0.0;
+        if (J >= 0)
+            for (int q = F.mp[J] + t; q < F.mp[J + 1]; q += T) s += s_fine[F.mem[q]];
         s = team_sum(s, T);
         if (J >= 0 && t == 0) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
     });
@@ -398,6 +559,7 @@ __device__ __forceinline__ void coarsest_solve(const AmgPcgArgs& a, double* xc)
 // the coarse correction of aggregate J of level l, i.e. node J of level l+1
 __device__ __forceinline__ double coarse_corr(const AmgPcgArgs& a, int l, int J, const double* xc)
 {
+    if (J < 0) return 0.0;  // a row in no aggregate
     return (l + 2 < a.nlev) ? a.L[l + 1].xp[J] : xc[J];
 }
 
@@ -416,10 +578,11 @@ __device__ __forceinline__ void prolong_level(const AmgPcgArgs& a, int l, double
                 for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) {
                     const int K = A.ci[k];
                     const double dK = A.dinv[K];
-                    const double yK = dK != 0.0 ? kOmega * dK * A.b[K] + kCoarseScale * coarse_corr(a, l, K / agg_size(l), xc) : 0.0;
+                    const double yK = dK != 0.0 ? kOmega * dK * A.b[K] + kCoarseScale * coarse_corr(a, l, A.agg[K], xc)
+                                                : 0.0;
                     s -= A.va[k] * yK;
                 }
-                if (t == 0) yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, I / agg_size(l), xc);
+                if (t == 0) yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, A.agg[I], xc);
             }
         }
         s = team_sum(s, T);
@@ -459,33 +622,27 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
     double alpha = 0.0, rz = 0.0, rr = 0.0, bnorm = 0.0, tol = 0.0;
     int it = 0;
     for (;;) {
-        // ---- x += alpha p, r -= alpha q, and the fine restriction ----------------
+        // ---- x += alpha p, r -= alpha q, and the fine residual of the pre-smoothed
+        // correction (into z, free until the preconditioner writes it) -------------
         {
             double l_rr = 0.0;
-            const AmgLevelDev& C = a.L[1];
-            for (int k = tid; k < round32(n); k += stride) {
+            for (int k = tid; k < n; k += stride) {
+                const double rk = rc[k] - alpha * a.q[k];
+                a.xs[k] += alpha * a.p[k];
+                rn[k] = rk;
+                l_rr += rk * rk;
+                const double dk = F.dinv[k];
                 double s = 0.0;
-                if (k < n) {
-                    const double rk = rc[k] - alpha * a.q[k];
-                    a.xs[k] += alpha * a.p[k];
-                    rn[k] = rk;
-                    l_rr += rk * rk;
-                    const double dk = F.dinv[k];
-                    if (!jacobi && dk != 0.0) {
-                        s = rk;
-                        const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
+                if (!jacobi && dk != 0.0) {
+                    s = rk;
+                    const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
 #pragma unroll 4
-                        for (int e = 0; e < w; e++) {
-                            const int j = F.eci[b0 + 32 * e];
-                            s -= F.eva[b0 + 32 * e] * (kOmega * F.dinv[j] * (rc[j] - alpha * a.q[j]));
-                        }
+                    for (int e = 0; e < w; e++) {
+                        const int j = F.eci[b0 + 32 * e];
+                        s -= F.eva[b0 + 32 * e] * (kOmega * F.dinv[j] * (rc[j] - alpha * a.q[j]));
                     }
                 }
-                if (!jacobi) {
-                    s = team_sum(s, kAggFine);
-                    const int J = k / kAggFine;
-                    if ((k & (kAggFine - 1)) == 0 && J < C.n) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
-                }
+                if (!jacobi) a.z[k] = s;
             }
             const double t = amg_block_sum(l_rr, sh);
             if (threadIdx.x == 0) part_rr[blockIdx.x] = t;
@@ -511,6 +668,8 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                 l_rz += zk * rc[k];
             }
         } else {
+            restrict_fine(a, a.z);
+            grid.sync();
             for (int l = 1; l + 1 < a.nlev; l++) {
                 restrict_level(a, l);
                 grid.sync();
@@ -524,7 +683,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                 const double dk = F.dinv[k];
                 double zk = 0.0;
                 if (dk != 0.0) {
-                    const double yk = kOmega * dk * rc[k] + kCoarseScale * coarse_corr(a, 0, k / kAggFine, xc);
+                    const double yk = kOmega * dk * rc[k] + kCoarseScale * coarse_corr(a, 0, F.agg[k], xc);
                     double s = rc[k];
                     const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
 #pragma unroll 4
@@ -532,7 +691,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                         const int j = F.eci[b0 + 32 * e];
                         const double dj = F.dinv[j];
                         const double yj =
-                            dj != 0.0 ? kOmega * dj * rc[j] + kCoarseScale * coarse_corr(a, 0, j / kAggFine, xc)
+                            dj != 0.0 ? kOmega * dj * rc[j] + kCoarseScale * coarse_corr(a, 0, F.agg[j], xc)
                                       : 0.0;
                         s -= F.eva[b0 + 32 * e] * yj;
                     }
@@ -588,26 +747,75 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-int amg_levels(int n)
+int amg_levels(int n) { return n > kCoarsest ? 2 : 1; }
+
+// one pairwise pass over level A: agg[i] for every row, the number of aggregates
+static ma_status pair_pass(Ctx* c, const LevelCsr& A, int* agg, int* nagg)
 {
-    int L = 1;
-    int m = n;
-    while (m > kCoarsest && L < kAmgMaxLevels) {
-        m = (m + agg_size(L - 1) - 1) / agg_size(L - 1);
-        L++;
+    cudaStream_t s = c->stream;
+    Amg& G = c->amg;
+    const int n = A.n;
+    const unsigned g = (unsigned)((n + 255) / 256);
+    MA_CUDA(c, cudaMemsetAsync(G.mate.p, 0xFF, sizeof(int) * n, s));
+    for (int r = 0; r < kMatchRounds; r++) {
+        k_strongest<false><<<g, 256, 0, s>>>(A, G.mate.as<int>(), G.best.as<int>());
+        k_handshake<<<g, 256, 0, s>>>(n, G.best.as<int>(), G.mate.as<int>());
     }
-    return L;
+    k_strongest<true><<<g, 256, 0, s>>>(A, G.mate.as<int>(), G.best.as<int>());
+    MA_CUDA(c, cudaMemsetAsync(G.claim.p, 0x7F, sizeof(int) * n, s));
+    k_bid<<<g, 256, 0, s>>>(n, G.best.as<int>(), G.mate.as<int>(), G.claim.as<int>());
+    k_leaders<<<g, 256, 0, s>>>(n, A.dinv, G.mate.as<int>(), G.best.as<int>(), G.claim.as<int>(), G.mflag.as<int>(),
+                                G.join.as<int>());
+    launch_scan(G.mflag.as<int>(), G.mid.as<int>(), n, c->scan_scratch.as<int>(), s);
+    k_assign<<<g, 256, 0, s>>>(n, A.dinv, G.mate.as<int>(), G.join.as<int>(), G.mid.as<int>(), agg);
+    c->launches += 2 * kMatchRounds + 8;
+    MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 7, G.mid.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaStreamSynchronize(s));
+    *nagg = c->hinfo[7];
+    return MA_OK;
+}
+
+// member lists of nc aggregates of n rows
+static ma_status members(Ctx* c, const int* agg, int n, int nc, int* mp, int* mem)
+{
+    cudaStream_t s = c->stream;
+    Amg& G = c->amg;
+    const unsigned g = (unsigned)((n + 255) / 256);
+    MA_CUDA(c, cudaMemsetAsync(G.cnt.p, 0, sizeof(int) * (nc + 1), s));
+    k_member_count<<<g, 256, 0, s>>>(n, agg, G.cnt.as<int>());
+    launch_scan(G.cnt.as<int>(), mp, nc, c->scan_scratch.as<int>(), s);
+    MA_CUDA(c, cudaMemsetAsync(G.mfill.p, 0, sizeof(int) * (nc + 1), s));
+    k_member_fill<<<g, 256, 0, s>>>(n, agg, mp, G.mfill.as<int>(), mem);
+    k_member_sort<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(nc, mp, mem);
+    c->launches += 6;
+    return MA_OK;
+}
+
+// the Galerkin matrix of the aggregates (rows rp[nc+1], ci, va; dinv[nc])
+static ma_status galerkin(Ctx* c, const LevelCsr& A, const int* mp, const int* mem, const int* agg, int nc, int* rp,
+                          int* ci, double* va, double* dinv)
+{
+    cudaStream_t s = c->stream;
+    Amg& G = c->amg;
+    CoarseSrc src{mp, mem, agg, A.rp, A.ci, A.va};
+    const unsigned g = (unsigned)((nc + kRowWarps - 1) / kRowWarps);
+    k_coarse_rows<false><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), nullptr, nullptr, nullptr,
+                                                       G.flag.as<int>());
+    launch_scan(G.cnt.as<int>(), rp, nc, c->scan_scratch.as<int>(), s);
+    k_coarse_rows<true><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), rp, ci, va, G.flag.as<int>());
+    k_level_dinv<<<(nc + 255) / 256, 256, 0, s>>>(rp, ci, va, nc, dinv);
+    c->launches += 6;
+    return MA_OK;
 }
 
 // Build the hierarchy for the Hessian in c->rowptr/col/val (n rows) and run the
-// preconditioned CG.  Matrices of level l >= 1 never have more entries than the
-// fine one, so every level is sized by the fine nnz and nothing is read back.
+// preconditioned CG.  Matrices of level l >= 1 never have more rows or entries than
+// the fine one, so every level is sized by the fine level.
 ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int* iters,
                         double* relres)
 {
     cudaStream_t s = c->stream;
-    const int nlev = amg_levels(n);
-    if (nlev < 2 || nlev > kAmgMaxLevels) return MA_ERR_INVALID_ARGUMENT;
+    if (n <= kCoarsest) return MA_ERR_INVALID_ARGUMENT;
     Amg& G = c->amg;
     const size_t nnz = (size_t)(c->nnz > 0 ? c->nnz : 1);
     MA_CUDA(c, c->cg_r.ensure(sizeof(double) * n));
@@ -624,6 +832,12 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     MA_CUDA(c, G.ci0.ensure(sizeof(int) * nnz));
     MA_CUDA(c, G.va0.ensure(sizeof(double) * nnz));
     MA_CUDA(c, G.flag.ensure(sizeof(int) * 4));
+    for (DevBuf* d : {&G.mate, &G.best, &G.claim, &G.mflag, &G.join, &G.agg1, &G.agg2, &G.mem1})
+        MA_CUDA(c, d->ensure(sizeof(int) * (n + 1)));
+    for (DevBuf* d : {&G.mid, &G.mp1, &G.mfill, &G.rp1}) MA_CUDA(c, d->ensure(sizeof(int) * (n + 2)));
+    MA_CUDA(c, G.ci1.ensure(sizeof(int) * nnz));
+    MA_CUDA(c, G.va1.ensure(sizeof(double) * nnz));
+    MA_CUDA(c, G.dinv1.ensure(sizeof(double) * n));
     MA_CUDA(c, cudaMemsetAsync(G.flag.p, 0, sizeof(int) * 4, s));
     const int* perm = c->perm.as<int>();
     const unsigned g1 = (unsigned)((n + 255) / 256);
@@ -651,35 +865,60 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     c->launches += 9;
 
     AmgPcgArgs a{};
-    a.nlev = nlev;
     a.L[0] = AmgLevelDev{n,       G.rp0.as<int>(), G.ci0.as<int>(), G.va0.as<double>(), c->cg_dinv.as<double>(),
-                         nullptr, nullptr,         1,               1,                 G.sp.as<int>(),
-                         G.eci.as<int>(), G.eva.as<double>()};
-    int nl = n;
-    for (int l = 1; l < nlev; l++) {
-        const int nc = (nl + agg_size(l - 1) - 1) / agg_size(l - 1);
-        AmgBuf& B = G.lev[l];
-        MA_CUDA(c, B.rp.ensure(sizeof(int) * (nc + 1)));
-        MA_CUDA(c, B.ci.ensure(sizeof(int) * nnz));
-        MA_CUDA(c, B.va.ensure(sizeof(double) * nnz));
-        MA_CUDA(c, B.dinv.ensure(sizeof(double) * nc));
-        MA_CUDA(c, B.b.ensure(sizeof(double) * nc));
-        MA_CUDA(c, B.xp.ensure(sizeof(double) * nc));
-        const AmgLevelDev& A = a.L[l - 1];
-        CoarseSrc src{agg_size(l - 1), nl, A.rp, A.ci, A.va, A.dinv};
-        const unsigned g = (unsigned)((nc + kRowWarps - 1) / kRowWarps);
-        k_coarse_rows<false><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), nullptr, nullptr, nullptr,
-                                                           G.flag.as<int>());
-        launch_scan(G.cnt.as<int>(), B.rp.as<int>(), nc, c->scan_scratch.as<int>(), s);
-        k_coarse_rows<true><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), B.rp.as<int>(), B.ci.as<int>(),
-                                                          B.va.as<double>(), G.flag.as<int>());
-        k_level_dinv<<<(nc + 255) / 256, 256, 0, s>>>(B.rp.as<int>(), B.ci.as<int>(), B.va.as<double>(), nc,
-                                                      B.dinv.as<double>());
-        c->launches += 5;
-        a.L[l] = AmgLevelDev{nc, B.rp.as<int>(), B.ci.as<int>(), B.va.as<double>(), B.dinv.as<double>(),
-                             B.b.as<double>(), B.xp.as<double>(), 1, 1, nullptr, nullptr, nullptr};
-        nl = nc;
+                         nullptr, nullptr,         1,               1,                 nullptr,
+                         nullptr, nullptr,         G.sp.as<int>(),  G.eci.as<int>(),   G.eva.as<double>()};
+    int nlev = 1;
+    while (a.L[nlev - 1].n > kCoarsest && nlev < kAmgMaxLevels) {
+        const int l = nlev - 1;
+        AmgLevelDev& A = a.L[l];
+        const LevelCsr LA{A.n, A.rp, A.ci, A.va, A.dinv};
+        AmgBuf& B = G.lev[l];  // this level's aggregates
+        MA_CUDA(c, B.agg.ensure(sizeof(int) * (A.n + 1)));
+        MA_CUDA(c, B.mem.ensure(sizeof(int) * (A.n + 1)));
+        MA_CUDA(c, B.mp.ensure(sizeof(int) * (A.n + 2)));
+        ma_status st;
+        // pass 1: pairs of rows; pass 2: pairs of those, on their Galerkin matrix
+        int n1 = 0, nc = 0;
+        if ((st = pair_pass(c, LA, G.agg1.as<int>(), &n1)) != MA_OK) return st;
+        if (n1 > 0 && 3 * n1 < 2 * A.n) {
+            if ((st = members(c, G.agg1.as<int>(), A.n, n1, G.mp1.as<int>(), G.mem1.as<int>())) != MA_OK) return st;
+            if ((st = galerkin(c, LA, G.mp1.as<int>(), G.mem1.as<int>(), G.agg1.as<int>(), n1, G.rp1.as<int>(),
+                               G.ci1.as<int>(), G.va1.as<double>(), G.dinv1.as<double>())) != MA_OK)
+                return st;
+            const LevelCsr L1{n1, G.rp1.as<int>(), G.ci1.as<int>(), G.va1.as<double>(), G.dinv1.as<double>()};
+            if ((st = pair_pass(c, L1, G.agg2.as<int>(), &nc)) != MA_OK) return st;
+            k_compose<<<(unsigned)((A.n + 255) / 256), 256, 0, s>>>(A.n, G.agg1.as<int>(), G.agg2.as<int>(),
+                                                                     B.agg.as<int>());
+            c->launches += 1;
+        }
+        if (!(nc > 0 && 3 * nc < 2 * A.n)) {
+            // the matching stalled: consecutive groups
+            nc = (A.n + kAggGroup - 1) / kAggGroup;
+            k_group<<<(unsigned)((A.n + 255) / 256), 256, 0, s>>>(A.n, A.dinv, B.agg.as<int>());
+            c->launches += 1;
+        }
+        if ((st = members(c, B.agg.as<int>(), A.n, nc, B.mp.as<int>(), B.mem.as<int>())) != MA_OK) return st;
+        AmgBuf& Cb = G.lev[l + 1];  // the next level's matrix
+        MA_CUDA(c, Cb.rp.ensure(sizeof(int) * (nc + 1)));
+        MA_CUDA(c, Cb.ci.ensure(sizeof(int) * nnz));
+        MA_CUDA(c, Cb.va.ensure(sizeof(double) * nnz));
+        MA_CUDA(c, Cb.dinv.ensure(sizeof(double) * nc));
+        MA_CUDA(c, Cb.b.ensure(sizeof(double) * nc));
+        MA_CUDA(c, Cb.xp.ensure(sizeof(double) * nc));
+        if ((st = galerkin(c, LA, B.mp.as<int>(), B.mem.as<int>(), B.agg.as<int>(), nc, Cb.rp.as<int>(),
+                           Cb.ci.as<int>(), Cb.va.as<double>(), Cb.dinv.as<double>())) != MA_OK)
+            return st;
+        A.agg = B.agg.as<int>();
+        A.mp = B.mp.as<int>();
+        A.mem = B.mem.as<int>();
+        a.L[l + 1] = AmgLevelDev{nc,      Cb.rp.as<int>(), Cb.ci.as<int>(), Cb.va.as<double>(), Cb.dinv.as<double>(),
+                                 Cb.b.as<double>(), Cb.xp.as<double>(), 1, 1, nullptr, nullptr, nullptr,
+                                 nullptr, nullptr, nullptr};
+        nlev++;
     }
+    if (a.L[nlev - 1].n > kCoarsest) return fail(c, MA_ERR_CAPACITY, "multigrid coarsest level too large");
+    a.nlev = nlev;
     const AmgLevelDev& C = a.L[nlev - 1];
     MA_CUDA(c, G.cinv.ensure(sizeof(double) * kCoarsest * kCoarsest));
     k_dense_inverse<<<1, 256, 0, s>>>(C.rp, C.ci, C.va, C.dinv, C.n, G.cinv.as<double>());
@@ -708,6 +947,7 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         while (t < 32 && (int64_t)rows * t * 2 <= threads) t <<= 1;
         return t;
     };
+    a.L[0].tr = team(a.L[1].n);
     for (int l = 1; l < nlev; l++) {
         a.L[l].tp = team(a.L[l].n);
         if (l + 1 < nlev) a.L[l].tr = team(a.L[l + 1].n);
