@@ -1,7 +1,8 @@
 // MA/gb300.hpp -- the reference's C++ entry points over the GB300 C ABI.
 //
 // A MongeAmpere++ caller keeps its call sites: MA::kantorovich, MA::ot_solve,
-// MA::first_moment, MA::second_moment, MA::lloyd, MA::solve_laplacian_matrix keep
+// MA::first_moment, MA::second_moment, MA::lloyd, MA::solve_laplacian_matrix,
+// MA::voronoi_triangulation_intersection, MA::voronoi_polygon_intersection keep
 // their names, argument order and argument meaning (include/MA/kantorovich.hpp:35-42,
 // include/MA/optimal_transport.hpp:35-39, 41-44, 89-99, include/MA/lloyd.hpp:30-36,
 // 71-78, 126-132).  The triangulation + per-face linear functions of the reference
@@ -308,6 +309,40 @@ void voronoi_triangulation_intersection(const Density& density, const Matrix& X,
         }
         out(p);
     }
+}
+
+// MA::voronoi_polygon_intersection (voronoi_polygon_intersection.hpp:153-188), for
+// every site at once: result[i] is the Laguerre cell of site i (weights w) clipped to
+// the polygon P, a sequence of (x, y) corners (3 to 64 of them); an empty result when
+// the cell misses P.  The reference takes one Vertex_handle of a triangulation per
+// call and returns one Polygon; the triangulation here is implicit in the sites and
+// weights.  Zero weights give the Delaunay case (Voronoi cells).
+using Polygon = std::vector<std::pair<double, double>>;
+
+template <class Matrix, class Vector>
+std::vector<Polygon> voronoi_polygon_intersection(const Polygon& P, const Matrix& X, const Vector& weights,
+                                                  Engine& e = Engine::instance())
+{
+    std::vector<double> x, y;
+    detail::split_sites(X, x, y);
+    const int64_t n = (int64_t)x.size();
+    std::vector<double> w = detail::to_vec(weights, n), px, py;
+    for (const auto& c : P) {
+        px.push_back(c.first);
+        py.push_back(c.second);
+    }
+    int64_t nv = 0;
+    check(ma_polygon_cells(e.get(), n, x.data(), y.data(), w.data(), px.data(), py.data(), (int)P.size(),
+                           MA_MEM_HOST, &nv),
+          e.get(), "ma_polygon_cells");
+    std::vector<int64_t> off(n + 1);
+    std::vector<double> xy(2 * nv);
+    check(ma_polygon_cells_copy(e.get(), off.data(), xy.data(), nullptr, MA_MEM_HOST), e.get(),
+          "ma_polygon_cells_copy");
+    std::vector<Polygon> r((size_t)n);
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t v = off[i]; v < off[i + 1]; v++) r[(size_t)i].emplace_back(xy[2 * v], xy[2 * v + 1]);
+    return r;
 }
 
 // MA::solve_laplacian_matrix (optimal_transport.hpp:41-87) for the Hessian of the

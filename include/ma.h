@@ -108,6 +108,8 @@ typedef struct ma_profile {
                                  final neighbours */
     int64_t amg_fallbacks;    /* Newton solves whose multigrid setup met a coarse row beyond its
                                  capacity and ran with the diagonal preconditioner */
+    double amg_setup_ms;      /* multigrid hierarchy: fine matrix, aggregation, Galerkin levels */
+    int64_t amg_levels;       /* levels of the last hierarchy */
 } ma_profile;
 /* enable != 0: reset the profile and start recording; 0: stop. */
 ma_status ma_ctx_profile(ma_ctx* ctx, int enable);

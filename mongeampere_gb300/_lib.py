@@ -42,7 +42,8 @@ class MaProfile(ctypes.Structure):
                 ("bounds_ms", ctypes.c_double), ("bounds_launches", ctypes.c_int64),
                 ("pcg_ms", ctypes.c_double), ("pcg_launches", ctypes.c_int64), ("pcg_iters", ctypes.c_int64),
                 ("large_sites", ctypes.c_int64), ("search", ctypes.c_int64 * 6),
-                ("amg_fallbacks", ctypes.c_int64)]
+                ("amg_fallbacks", ctypes.c_int64), ("amg_setup_ms", ctypes.c_double),
+                ("amg_levels", ctypes.c_int64)]
 
 
 # every symbol include/ma.h declares, with its ctypes signature

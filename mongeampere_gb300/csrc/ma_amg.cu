@@ -68,19 +68,20 @@ struct CoarseSrc {
 // to aggregates, keep the first occurrence of each aggregate, sum its duplicates in
 // gather order, and place it by rank of its column.  FILL = false counts the
 // distinct columns into cnt[I]; FILL = true writes them at rp[I].
+struct RowScratch {  // one warp's gather space
+    int col[kRowCap];
+    double val[kRowCap];
+    unsigned char lead[kRowCap];
+};
+
 template <bool FILL>
-__global__ void __launch_bounds__(32 * kRowWarps) k_coarse_rows(CoarseSrc s, int nc, int* cnt, const int* rp,
-                                                                 int* ci, double* va, int* overflow)
+__device__ void coarse_row(const CoarseSrc& s, int I, int lane, RowScratch& w, int* cnt, const int* rp, int* ci,
+                           double* va, int* overflow)
 {
-    __shared__ int scol[kRowWarps][kRowCap];
-    __shared__ double sval[kRowWarps][kRowCap];
-    __shared__ unsigned char slead[kRowWarps][kRowCap];
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int I = blockIdx.x * kRowWarps + wib;
-    if (I >= nc) return;
-    int* col = scol[wib];
-    double* val = sval[wib];
-    unsigned char* lead = slead[wib];
+    int* col = w.col;
+    double* val = w.val;
+    unsigned char* lead = w.lead;
+    __syncwarp();  // the warp's previous row is done with the scratch
     int E = 0;
     bool over = false;
     for (int q = s.mp[I]; q < s.mp[I + 1] && !over; q++) {
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_coarse_rows(CoarseSrc s, int
 }
 
 // ---------------------------------------------------------------------------
-// setup: pairwise aggregation
+// setup: pairwise aggregation, one cooperative launch per level
 // ---------------------------------------------------------------------------
 struct LevelCsr {
     int n;
@@ -159,14 +160,35 @@ struct LevelCsr {
     const double* dinv;  // 0: inactive row
 };
 
-// For every free active row (mate < 0): the strongest active neighbour (largest
-// -a_ij > 0) among the free rows (MATCHED = false) or among the matched rows
-// (MATCHED = true); ties to the lower index; -1 if there is none.
+constexpr int kSetupThreads = 32 * kRowWarps;
+
+struct SetupArgs {
+    LevelCsr A;  // the level to aggregate
+    // scratch, n + 2 entries each (rp1: n + 2, ci1 / va1: the level's entries)
+    int *mate, *best, *claim, *flag, *id, *join, *agg1, *agg2, *mp1, *mem1, *fill, *cnt;
+    int* rp1;
+    int* ci1;
+    double* va1;
+    double* dinv1;
+    int* part;    // one int per block
+    int* counts;  // [0] first-pass aggregates, [1] second-pass aggregates, [2] the level's aggregates
+    // outputs: the level's aggregates and the next level's matrix
+    int *agg, *mp, *mem;
+    int* rp;
+    int* ci;
+    double* va;
+    double* dinv;
+    int* overflow;
+    int reuse;  // keep agg / mp / mem (nc aggregates) and rebuild only the next level's matrix
+    int nc;
+};
+
+// the strongest active neighbour (largest -a_ij > 0) of free active row i among the
+// free rows (MATCHED = false) or the matched rows (MATCHED = true); ties to the
+// lower index; -1 if there is none or row i is not free
 template <bool MATCHED>
-__global__ void k_strongest(LevelCsr A, const int* mate, int* best)
+__device__ int strongest(const LevelCsr& A, const int* mate, int i)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.n) return;
     int b = -1;
     if (A.dinv[i] != 0.0 && mate[i] < 0) {
         double sb = 0.0;
@@ -180,123 +202,212 @@ __global__ void k_strongest(LevelCsr A, const int* mate, int* best)
             }
         }
     }
-    best[i] = b;
+    return b;
 }
 
-// a handshake: rows that chose each other become a pair
-__global__ void k_handshake(int n, const int* best, int* mate)
+// exclusive block-wide scan of v (kSetupThreads threads); *total gets the sum
+__device__ __forceinline__ int block_scan(int v, int* sh, int* total)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int j = best[i];
-    if (j >= 0 && best[j] == i) mate[i] = j;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[wid] = x;
+    __syncthreads();
+    int before = 0, all = 0;
+    for (int q = 0; q < kSetupThreads / 32; q++) {
+        if (q < wid) before += sh[q];
+        all += sh[q];
+    }
+    __syncthreads();
+    *total = all;
+    return before + x - v;
 }
 
-// a free row bids for the pair of its strongest matched neighbour (best from
-// k_strongest<true>); the lowest bidder of each pair joins it
-__global__ void k_bid(int n, const int* best, const int* mate, int* claim)
+// exclusive scan of in[0, n) into out[0, n] (out[n] = total) by the whole grid: each
+// block scans a contiguous chunk after the totals of the chunks before it
+__device__ void grid_scan(cg::grid_group& grid, const int* in, int* out, int n, int* part, int* sh)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int j = best[i];
-    if (j >= 0) atomicMin(&claim[min(j, mate[j])], i);
+    const int nb = gridDim.x, chunk = (n + nb - 1) / nb;
+    const int b0 = min(n, blockIdx.x * chunk), b1 = min(n, b0 + chunk);
+    int t = 0;
+    for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) t += in[i];
+    int tot;
+    block_scan(t, sh, &tot);
+    if (threadIdx.x == 0) part[blockIdx.x] = tot;
+    grid.sync();
+    int off = 0;
+    for (int q = threadIdx.x; q < blockIdx.x; q += blockDim.x) off += part[q];
+    block_scan(off, sh, &off);
+    for (int base = b0; base < b1; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int v = i < b1 ? in[i] : 0;
+        int tile;
+        const int ex = block_scan(v, sh, &tile);
+        if (i < b1) out[i] = off + ex;
+        off += tile;
+    }
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) out[n] = off;
+    grid.sync();
 }
 
-// leaders (the lower row of a pair, or an active row that stays alone) flagged for
-// the numbering scan; join[i] = the pair a row joins, else -1
-__global__ void k_leaders(int n, const double* dinv, const int* mate, const int* best, const int* claim, int* flag,
-                          int* join)
+// One pairwise pass over A: kMatchRounds handshake rounds (a row and its strongest
+// free neighbour pair up when each is the other's choice), then every row left alone
+// bids for the pair of its strongest matched neighbour and the lowest bidder joins
+// it; leaders (the lower row of a pair, or a row that stays alone) are numbered in
+// row order.  agg[i] = aggregate of row i (-1: inactive), *count = aggregates.
+__device__ void pair_pass(cg::grid_group& grid, const LevelCsr& A, const SetupArgs& a, int* agg, int* count, int* sh)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int f = 0, jn = -1;
-    if (dinv[i] != 0.0) {
-        const int m = mate[i];
-        if (m >= 0) {
-            f = i < m;
-        } else {
-            const int j = best[i];
-            const int p = j >= 0 ? min(j, mate[j]) : -1;
-            if (p >= 0 && claim[p] == i)
-                jn = p;
-            else
-                f = 1;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    for (int i = tid; i < A.n; i += stride) {
+        a.mate[i] = -1;
+        a.claim[i] = INT_MAX;
+    }
+    grid.sync();
+    for (int r = 0; r < kMatchRounds; r++) {
+        for (int i = tid; i < A.n; i += stride) a.best[i] = strongest<false>(A, a.mate, i);
+        grid.sync();
+        for (int i = tid; i < A.n; i += stride) {
+            const int j = a.best[i];
+            if (j >= 0 && a.best[j] == i) a.mate[i] = j;
         }
+        grid.sync();
     }
-    flag[i] = f;
-    join[i] = jn;
-}
-
-// aggregate of every row from the leaders' numbers (-1: inactive)
-__global__ void k_assign(int n, const double* dinv, const int* mate, const int* join, const int* id, int* agg)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int a = -1;
-    if (dinv[i] != 0.0) {
-        if (mate[i] >= 0)
-            a = id[min(i, mate[i])];
-        else if (join[i] >= 0)
-            a = id[join[i]];
-        else
-            a = id[i];
+    for (int i = tid; i < A.n; i += stride) a.best[i] = strongest<true>(A, a.mate, i);
+    grid.sync();
+    for (int i = tid; i < A.n; i += stride) {
+        const int j = a.best[i];
+        if (j >= 0) atomicMin(&a.claim[min(j, a.mate[j])], i);
     }
-    agg[i] = a;
-}
-
-// groups of kAggGroup consecutive active rows (the fallback where matching stalls)
-__global__ void k_group(int n, const double* dinv, int* agg)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) agg[i] = dinv[i] != 0.0 ? i / kAggGroup : -1;
-}
-
-// agg[i] = second[first[i]] (the two passes composed)
-__global__ void k_compose(int n, const int* first, const int* second, int* agg)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) agg[i] = first[i] >= 0 ? second[first[i]] : -1;
-}
-
-// member lists: counts per aggregate, then each row placed after the scan; the
-// members of an aggregate are then sorted by row (at most a few dozen per aggregate)
-__global__ void k_member_count(int n, const int* agg, int* cnt)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && agg[i] >= 0) atomicAdd(&cnt[agg[i]], 1);
-}
-
-__global__ void k_member_fill(int n, const int* agg, const int* mp, int* fill, int* mem)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || agg[i] < 0) return;
-    mem[mp[agg[i]] + atomicAdd(&fill[agg[i]], 1)] = i;
-}
-
-__global__ void k_member_sort(int nc, const int* mp, int* mem)
-{
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= nc) return;
-    for (int q = mp[I] + 1; q < mp[I + 1]; q++) {
-        const int v = mem[q];
-        int r = q - 1;
-        while (r >= mp[I] && mem[r] > v) {
-            mem[r + 1] = mem[r];
-            r--;
+    grid.sync();
+    for (int i = tid; i < A.n; i += stride) {
+        int f = 0, jn = -1;
+        if (A.dinv[i] != 0.0) {
+            const int m = a.mate[i];
+            if (m >= 0) {
+                f = i < m;
+            } else {
+                const int j = a.best[i];
+                const int p = j >= 0 ? min(j, a.mate[j]) : -1;
+                if (p >= 0 && a.claim[p] == i)
+                    jn = p;
+                else
+                    f = 1;
+            }
         }
-        mem[r + 1] = v;
+        a.flag[i] = f;
+        a.join[i] = jn;
     }
+    grid.sync();
+    grid_scan(grid, a.flag, a.id, A.n, a.part, sh);
+    for (int i = tid; i < A.n; i += stride) {
+        int g = -1;
+        if (A.dinv[i] != 0.0) {
+            const int m = a.mate[i];
+            g = m >= 0 ? a.id[min(i, m)] : (a.join[i] >= 0 ? a.id[a.join[i]] : a.id[i]);
+        }
+        agg[i] = g;
+    }
+    if (tid == 0) *count = a.id[A.n];
+    grid.sync();
 }
 
-// inverse diagonal of a coarse level (0 for rows without a positive diagonal)
-__global__ void k_level_dinv(const int* rp, const int* ci, const double* va, int n, double* dinv)
+// member lists of nc aggregates of n rows, each sorted by row
+__device__ void member_lists(cg::grid_group& grid, const int* agg, int n, int nc, int* mp, int* mem,
+                             const SetupArgs& a, int* sh)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    for (int I = tid; I < nc; I += stride) {
+        a.cnt[I] = 0;
+        a.fill[I] = 0;
+    }
+    grid.sync();
+    for (int i = tid; i < n; i += stride)
+        if (agg[i] >= 0) atomicAdd(&a.cnt[agg[i]], 1);
+    grid.sync();
+    grid_scan(grid, a.cnt, mp, nc, a.part, sh);
+    for (int i = tid; i < n; i += stride)
+        if (agg[i] >= 0) mem[mp[agg[i]] + atomicAdd(&a.fill[agg[i]], 1)] = i;
+    grid.sync();
+    for (int I = tid; I < nc; I += stride)
+        for (int q = mp[I] + 1; q < mp[I + 1]; q++) {
+            const int v = mem[q];
+            int r = q - 1;
+            while (r >= mp[I] && mem[r] > v) {
+                mem[r + 1] = mem[r];
+                r--;
+            }
+            mem[r + 1] = v;
+        }
+    grid.sync();
+}
+
+__device__ __forceinline__ double level_dinv(const int* rp, const int* ci, const double* va, int i)
+{
     double d = 0.0;
     for (int k = rp[i]; k < rp[i + 1]; k++)
         if (ci[k] == i) d = va[k];
-    dinv[i] = d > 0.0 ? 1.0 / d : 0.0;
+    return d > 0.0 ? 1.0 / d : 0.0;
+}
+
+// the Galerkin matrix of nc aggregates (warp per coarse row: count, place, fill) and
+// its inverse diagonal (0 for rows without a positive diagonal)
+__device__ void galerkin(cg::grid_group& grid, const LevelCsr& A, const int* mp, const int* mem, const int* map,
+                         int nc, int* rp, int* ci, double* va, double* dinv, const SetupArgs& a, RowScratch* sw,
+                         int* sh)
+{
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kRowWarps + wib, nw = gridDim.x * kRowWarps;
+    const CoarseSrc src{mp, mem, map, A.rp, A.ci, A.va};
+    for (int I = gw; I < nc; I += nw) coarse_row<false>(src, I, lane, sw[wib], a.cnt, nullptr, nullptr, nullptr, a.overflow);
+    grid.sync();
+    grid_scan(grid, a.cnt, rp, nc, a.part, sh);
+    for (int I = gw; I < nc; I += nw) coarse_row<true>(src, I, lane, sw[wib], a.cnt, rp, ci, va, a.overflow);
+    grid.sync();
+    for (int I = tid; I < nc; I += stride) dinv[I] = level_dinv(rp, ci, va, I);
+    grid.sync();
+}
+
+// One level: a pairwise pass over A, the Galerkin matrix of its pairs, a second
+// pairwise pass over that, the two composed; where a pass leaves more than 2/3 of the
+// rows (the matching stalls), groups of kAggGroup consecutive rows instead.  Then the
+// member lists and the next level's matrix.  With `reuse`, the aggregates of the
+// previous call stay and only the next level's matrix is rebuilt.  Every branch is
+// grid-uniform.
+__global__ void __launch_bounds__(kSetupThreads) k_level_setup(SetupArgs a)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ RowScratch sw[kRowWarps];
+    __shared__ int sh[kSetupThreads / 32];
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const int n = a.A.n;
+    if (a.reuse) {
+        galerkin(grid, a.A, a.mp, a.mem, a.agg, a.nc, a.rp, a.ci, a.va, a.dinv, a, sw, sh);
+        if (tid == 0) a.counts[2] = a.nc;
+        return;
+    }
+    pair_pass(grid, a.A, a, a.agg1, &a.counts[0], sh);
+    const int n1 = *(volatile const int*)&a.counts[0];
+    int nc = 0;
+    if (n1 > 0 && 3 * n1 < 2 * n) {
+        member_lists(grid, a.agg1, n, n1, a.mp1, a.mem1, a, sh);
+        galerkin(grid, a.A, a.mp1, a.mem1, a.agg1, n1, a.rp1, a.ci1, a.va1, a.dinv1, a, sw, sh);
+        const LevelCsr L1{n1, a.rp1, a.ci1, a.va1, a.dinv1};
+        pair_pass(grid, L1, a, a.agg2, &a.counts[1], sh);
+        nc = *(volatile const int*)&a.counts[1];
+        for (int i = tid; i < n; i += stride) a.agg[i] = a.agg1[i] >= 0 ? a.agg2[a.agg1[i]] : -1;
+    }
+    if (!(nc > 0 && 3 * nc < 2 * n)) {
+        nc = (n + kAggGroup - 1) / kAggGroup;
+        for (int i = tid; i < n; i += stride) a.agg[i] = a.A.dinv[i] != 0.0 ? i / kAggGroup : -1;
+    }
+    grid.sync();
+    member_lists(grid, a.agg, n, nc, a.mp, a.mem, a, sh);
+    galerkin(grid, a.A, a.mp, a.mem, a.agg, nc, a.rp, a.ci, a.va, a.dinv, a, sw, sh);
+    if (tid == 0) a.counts[2] = nc;
 }
 
 // dense inverse of the coarsest level (n <= kCoarsest, SPD on its active rows;
@@ -749,69 +860,10 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
 // ---------------------------------------------------------------------------
 int amg_levels(int n) { return n > kCoarsest ? 2 : 1; }
 
-// one pairwise pass over level A: agg[i] for every row, the number of aggregates
-static ma_status pair_pass(Ctx* c, const LevelCsr& A, int* agg, int* nagg)
-{
-    cudaStream_t s = c->stream;
-    Amg& G = c->amg;
-    const int n = A.n;
-    const unsigned g = (unsigned)((n + 255) / 256);
-    MA_CUDA(c, cudaMemsetAsync(G.mate.p, 0xFF, sizeof(int) * n, s));
-    for (int r = 0; r < kMatchRounds; r++) {
-        k_strongest<false><<<g, 256, 0, s>>>(A, G.mate.as<int>(), G.best.as<int>());
-        k_handshake<<<g, 256, 0, s>>>(n, G.best.as<int>(), G.mate.as<int>());
-    }
-    k_strongest<true><<<g, 256, 0, s>>>(A, G.mate.as<int>(), G.best.as<int>());
-    MA_CUDA(c, cudaMemsetAsync(G.claim.p, 0x7F, sizeof(int) * n, s));
-    k_bid<<<g, 256, 0, s>>>(n, G.best.as<int>(), G.mate.as<int>(), G.claim.as<int>());
-    k_leaders<<<g, 256, 0, s>>>(n, A.dinv, G.mate.as<int>(), G.best.as<int>(), G.claim.as<int>(), G.mflag.as<int>(),
-                                G.join.as<int>());
-    launch_scan(G.mflag.as<int>(), G.mid.as<int>(), n, c->scan_scratch.as<int>(), s);
-    k_assign<<<g, 256, 0, s>>>(n, A.dinv, G.mate.as<int>(), G.join.as<int>(), G.mid.as<int>(), agg);
-    c->launches += 2 * kMatchRounds + 8;
-    MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 7, G.mid.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MA_CUDA(c, cudaStreamSynchronize(s));
-    *nagg = c->hinfo[7];
-    return MA_OK;
-}
-
-// member lists of nc aggregates of n rows
-static ma_status members(Ctx* c, const int* agg, int n, int nc, int* mp, int* mem)
-{
-    cudaStream_t s = c->stream;
-    Amg& G = c->amg;
-    const unsigned g = (unsigned)((n + 255) / 256);
-    MA_CUDA(c, cudaMemsetAsync(G.cnt.p, 0, sizeof(int) * (nc + 1), s));
-    k_member_count<<<g, 256, 0, s>>>(n, agg, G.cnt.as<int>());
-    launch_scan(G.cnt.as<int>(), mp, nc, c->scan_scratch.as<int>(), s);
-    MA_CUDA(c, cudaMemsetAsync(G.mfill.p, 0, sizeof(int) * (nc + 1), s));
-    k_member_fill<<<g, 256, 0, s>>>(n, agg, mp, G.mfill.as<int>(), mem);
-    k_member_sort<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(nc, mp, mem);
-    c->launches += 6;
-    return MA_OK;
-}
-
-// the Galerkin matrix of the aggregates (rows rp[nc+1], ci, va; dinv[nc])
-static ma_status galerkin(Ctx* c, const LevelCsr& A, const int* mp, const int* mem, const int* agg, int nc, int* rp,
-                          int* ci, double* va, double* dinv)
-{
-    cudaStream_t s = c->stream;
-    Amg& G = c->amg;
-    CoarseSrc src{mp, mem, agg, A.rp, A.ci, A.va};
-    const unsigned g = (unsigned)((nc + kRowWarps - 1) / kRowWarps);
-    k_coarse_rows<false><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), nullptr, nullptr, nullptr,
-                                                       G.flag.as<int>());
-    launch_scan(G.cnt.as<int>(), rp, nc, c->scan_scratch.as<int>(), s);
-    k_coarse_rows<true><<<g, 32 * kRowWarps, 0, s>>>(src, nc, G.cnt.as<int>(), rp, ci, va, G.flag.as<int>());
-    k_level_dinv<<<(nc + 255) / 256, 256, 0, s>>>(rp, ci, va, nc, dinv);
-    c->launches += 6;
-    return MA_OK;
-}
-
 // Build the hierarchy for the Hessian in c->rowptr/col/val (n rows) and run the
 // preconditioned CG.  Matrices of level l >= 1 never have more rows or entries than
 // the fine one, so every level is sized by the fine level.
-ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int* iters,
+ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int reuse, int* iters,
                         double* relres)
 {
     cudaStream_t s = c->stream;
@@ -838,9 +890,11 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     MA_CUDA(c, G.ci1.ensure(sizeof(int) * nnz));
     MA_CUDA(c, G.va1.ensure(sizeof(double) * nnz));
     MA_CUDA(c, G.dinv1.ensure(sizeof(double) * n));
+    MA_CUDA(c, G.counts.ensure(sizeof(int) * 4));
     MA_CUDA(c, cudaMemsetAsync(G.flag.p, 0, sizeof(int) * 4, s));
     const int* perm = c->perm.as<int>();
     const unsigned g1 = (unsigned)((n + 255) / 256);
+    ProfScope setup_scope(c, &c->profile.amg_setup_ms, nullptr);
     k_inv_perm<<<g1, 256, 0, s>>>(perm, n, G.inv.as<int>());
     k_fine_count<<<g1, 256, 0, s>>>(c->rowptr.as<int>(), perm, n, G.cnt.as<int>());
     launch_scan(G.cnt.as<int>(), G.rp0.as<int>(), n, c->scan_scratch.as<int>(), s);
@@ -868,47 +922,73 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     a.L[0] = AmgLevelDev{n,       G.rp0.as<int>(), G.ci0.as<int>(), G.va0.as<double>(), c->cg_dinv.as<double>(),
                          nullptr, nullptr,         1,               1,                 nullptr,
                          nullptr, nullptr,         G.sp.as<int>(),  G.eci.as<int>(),   G.eva.as<double>()};
+    // the level setup's cooperative grid: co-resident blocks, at most one row per thread
+    int setup_max = 0, sms = 0;
+    {
+        int per_sm = 0;
+        MA_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_level_setup, kSetupThreads, 0));
+        MA_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+        setup_max = std::max(1, per_sm * sms / std::max(1, c->grid_share));
+    }
+    MA_CUDA(c, G.part.ensure(sizeof(int) * (size_t)setup_max));
+    // the aggregates of the last hierarchy serve again for the same site index
+    const bool keep = reuse && G.agg_epoch == c->index_epoch && G.agg_nlev >= 2 && G.agg_n[0] == n;
+    if (!keep) G.agg_epoch = -1;  // the level buffers are about to change
     int nlev = 1;
-    while (a.L[nlev - 1].n > kCoarsest && nlev < kAmgMaxLevels) {
+    while (keep ? nlev < G.agg_nlev : (a.L[nlev - 1].n > kCoarsest && nlev < kAmgMaxLevels)) {
         const int l = nlev - 1;
         AmgLevelDev& A = a.L[l];
-        const LevelCsr LA{A.n, A.rp, A.ci, A.va, A.dinv};
         AmgBuf& B = G.lev[l];  // this level's aggregates
         MA_CUDA(c, B.agg.ensure(sizeof(int) * (A.n + 1)));
         MA_CUDA(c, B.mem.ensure(sizeof(int) * (A.n + 1)));
         MA_CUDA(c, B.mp.ensure(sizeof(int) * (A.n + 2)));
-        ma_status st;
-        // pass 1: pairs of rows; pass 2: pairs of those, on their Galerkin matrix
-        int n1 = 0, nc = 0;
-        if ((st = pair_pass(c, LA, G.agg1.as<int>(), &n1)) != MA_OK) return st;
-        if (n1 > 0 && 3 * n1 < 2 * A.n) {
-            if ((st = members(c, G.agg1.as<int>(), A.n, n1, G.mp1.as<int>(), G.mem1.as<int>())) != MA_OK) return st;
-            if ((st = galerkin(c, LA, G.mp1.as<int>(), G.mem1.as<int>(), G.agg1.as<int>(), n1, G.rp1.as<int>(),
-                               G.ci1.as<int>(), G.va1.as<double>(), G.dinv1.as<double>())) != MA_OK)
-                return st;
-            const LevelCsr L1{n1, G.rp1.as<int>(), G.ci1.as<int>(), G.va1.as<double>(), G.dinv1.as<double>()};
-            if ((st = pair_pass(c, L1, G.agg2.as<int>(), &nc)) != MA_OK) return st;
-            k_compose<<<(unsigned)((A.n + 255) / 256), 256, 0, s>>>(A.n, G.agg1.as<int>(), G.agg2.as<int>(),
-                                                                     B.agg.as<int>());
-            c->launches += 1;
-        }
-        if (!(nc > 0 && 3 * nc < 2 * A.n)) {
-            // the matching stalled: consecutive groups
-            nc = (A.n + kAggGroup - 1) / kAggGroup;
-            k_group<<<(unsigned)((A.n + 255) / 256), 256, 0, s>>>(A.n, A.dinv, B.agg.as<int>());
-            c->launches += 1;
-        }
-        if ((st = members(c, B.agg.as<int>(), A.n, nc, B.mp.as<int>(), B.mem.as<int>())) != MA_OK) return st;
-        AmgBuf& Cb = G.lev[l + 1];  // the next level's matrix
-        MA_CUDA(c, Cb.rp.ensure(sizeof(int) * (nc + 1)));
+        AmgBuf& Cb = G.lev[l + 1];  // the next level's matrix, sized by this level
+        MA_CUDA(c, Cb.rp.ensure(sizeof(int) * (A.n + 2)));
         MA_CUDA(c, Cb.ci.ensure(sizeof(int) * nnz));
         MA_CUDA(c, Cb.va.ensure(sizeof(double) * nnz));
-        MA_CUDA(c, Cb.dinv.ensure(sizeof(double) * nc));
-        MA_CUDA(c, Cb.b.ensure(sizeof(double) * nc));
-        MA_CUDA(c, Cb.xp.ensure(sizeof(double) * nc));
-        if ((st = galerkin(c, LA, B.mp.as<int>(), B.mem.as<int>(), B.agg.as<int>(), nc, Cb.rp.as<int>(),
-                           Cb.ci.as<int>(), Cb.va.as<double>(), Cb.dinv.as<double>())) != MA_OK)
-            return st;
+        MA_CUDA(c, Cb.dinv.ensure(sizeof(double) * A.n));
+        MA_CUDA(c, Cb.b.ensure(sizeof(double) * A.n));
+        MA_CUDA(c, Cb.xp.ensure(sizeof(double) * A.n));
+        SetupArgs sa;
+        sa.A = LevelCsr{A.n, A.rp, A.ci, A.va, A.dinv};
+        sa.mate = G.mate.as<int>();
+        sa.best = G.best.as<int>();
+        sa.claim = G.claim.as<int>();
+        sa.flag = G.mflag.as<int>();
+        sa.id = G.mid.as<int>();
+        sa.join = G.join.as<int>();
+        sa.agg1 = G.agg1.as<int>();
+        sa.agg2 = G.agg2.as<int>();
+        sa.mp1 = G.mp1.as<int>();
+        sa.mem1 = G.mem1.as<int>();
+        sa.fill = G.mfill.as<int>();
+        sa.cnt = G.cnt.as<int>();
+        sa.rp1 = G.rp1.as<int>();
+        sa.ci1 = G.ci1.as<int>();
+        sa.va1 = G.va1.as<double>();
+        sa.dinv1 = G.dinv1.as<double>();
+        sa.part = G.part.as<int>();
+        sa.counts = G.counts.as<int>();
+        sa.agg = B.agg.as<int>();
+        sa.mp = B.mp.as<int>();
+        sa.mem = B.mem.as<int>();
+        sa.rp = Cb.rp.as<int>();
+        sa.ci = Cb.ci.as<int>();
+        sa.va = Cb.va.as<double>();
+        sa.dinv = Cb.dinv.as<double>();
+        sa.overflow = G.flag.as<int>();
+        sa.reuse = keep ? 1 : 0;
+        sa.nc = keep ? G.agg_n[l + 1] : 0;
+        const int nbs = std::max(1, std::min(setup_max, (A.n + kSetupThreads - 1) / kSetupThreads));
+        void* sargs[] = {&sa};
+        MA_CUDA(c, cudaLaunchCooperativeKernel((void*)k_level_setup, dim3(nbs), dim3(kSetupThreads), sargs, 0, s));
+        c->launches += 1;
+        int nc = sa.nc;
+        if (!keep) {  // the next level's size decides the next iteration
+            MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 7, G.counts.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+            MA_CUDA(c, cudaStreamSynchronize(s));
+            nc = c->hinfo[7];
+        }
         A.agg = B.agg.as<int>();
         A.mp = B.mp.as<int>();
         A.mem = B.mem.as<int>();
@@ -917,12 +997,22 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
                                  nullptr, nullptr, nullptr};
         nlev++;
     }
-    if (a.L[nlev - 1].n > kCoarsest) return fail(c, MA_ERR_CAPACITY, "multigrid coarsest level too large");
+    if (a.L[nlev - 1].n > kCoarsest) {
+        G.agg_epoch = -1;
+        return fail(c, MA_ERR_CAPACITY, "multigrid coarsest level too large");
+    }
     a.nlev = nlev;
+    if (!keep) {
+        G.agg_epoch = c->index_epoch;
+        G.agg_nlev = nlev;
+        for (int l = 0; l < nlev; l++) G.agg_n[l] = a.L[l].n;
+    }
     const AmgLevelDev& C = a.L[nlev - 1];
     MA_CUDA(c, G.cinv.ensure(sizeof(double) * kCoarsest * kCoarsest));
     k_dense_inverse<<<1, 256, 0, s>>>(C.rp, C.ci, C.va, C.dinv, C.n, G.cinv.as<double>());
     c->launches += 1;
+    setup_scope.end();
+    c->profile.amg_levels = nlev;
 
     // the co-resident grid, at most kBlocksPerSm blocks per SM: every grid barrier
     // waits for all blocks, and the coarse levels' teams want the lanes

@@ -129,6 +129,7 @@ ma_status build_site_index_box(Ctx* c, double X0, double Y0, double X1, double Y
                       c->t_boxf.as<float4>(), s);
     c->launches += 1 + 8 * 5 + 1 + 2;
     c->n = n;
+    c->index_epoch++;
     c->prev_valid = false;
     return MA_OK;
 }
@@ -504,7 +505,8 @@ void ma_ctx_destroy(ma_ctx* c)
     DevBuf* ab[] = {&c->amg.r1, &c->amg.xs, &c->amg.inv, &c->amg.cnt, &c->amg.rp0, &c->amg.ci0, &c->amg.va0, &c->amg.sp, &c->amg.eci, &c->amg.eva,
                     &c->amg.flag, &c->amg.cinv, &c->amg.mate, &c->amg.best, &c->amg.claim, &c->amg.mflag,
                     &c->amg.mid, &c->amg.join, &c->amg.agg1, &c->amg.agg2, &c->amg.mp1, &c->amg.mem1,
-                    &c->amg.mfill, &c->amg.rp1, &c->amg.ci1, &c->amg.va1, &c->amg.dinv1};
+                    &c->amg.mfill, &c->amg.rp1, &c->amg.ci1, &c->amg.va1, &c->amg.dinv1, &c->amg.part,
+                    &c->amg.counts};
     for (DevBuf* b : ab) b->release();
     if (c->pev[0]) cudaEventDestroy(c->pev[0]);
     if (c->pev[1]) cudaEventDestroy(c->pev[1]);

@@ -72,7 +72,12 @@ struct Amg {
     DevBuf r1, xs, inv, cnt, rp0, ci0, va0, sp, eci, eva, flag, cinv;
     // aggregation scratch: the matching state, the first pass's aggregates and
     // their Galerkin matrix
-    DevBuf mate, best, claim, mflag, mid, join, agg1, agg2, mp1, mem1, mfill, rp1, ci1, va1, dinv1;
+    DevBuf mate, best, claim, mflag, mid, join, agg1, agg2, mp1, mem1, mfill, rp1, ci1, va1, dinv1, part, counts;
+    // the aggregates in lev[].agg/mp/mem: built for the site index of epoch agg_epoch,
+    // agg_nlev levels of agg_n[] rows
+    int64_t agg_epoch = -1;
+    int agg_nlev = 0;
+    int agg_n[16] = {};
 };
 
 struct Ctx {
@@ -86,6 +91,7 @@ struct Ctx {
     DevBuf hx, hy, hw, hnu;
     // site index: Morton-sorted sites and their radix tree
     int n = 0;
+    int64_t index_epoch = 0;  // counts site-index builds
     DevBuf mkeys, mkeys_tmp, hist, hist_scan, perm, sites, posf, scan_scratch, fill;
     DevBuf t_child, t_range, t_parent, t_leaf_parent, t_flag, t_box, t_boxf, t_mom, t_ab;
     DevBuf keys, bboxd;  // ordered keys and their doubles
@@ -170,30 +176,36 @@ struct EvalFlags {
     bool abort_on_empty = false;
 };
 ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlags& f);
-// Newton linear solve H[:n-1,:n-1] x = b with the multigrid-preconditioned CG (ma_amg.cu)
+// Newton linear solve H[:n-1,:n-1] x = b with the multigrid-preconditioned CG (ma_amg.cu);
+// reuse != 0 keeps the aggregates of the last hierarchy built for the same site index
+// (only the Galerkin matrices are rebuilt)
 int amg_levels(int n);
-ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int* iters,
+ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int reuse, int* iters,
                         double* relres);
 
 // bracket an enqueue with profiling events; the elapsed time is added after a sync
 struct ProfScope {
     Ctx* c;
     double* ms;
-    int64_t* cnt;
+    int64_t* cnt;  // nullable
+    bool done = false;
     ProfScope(Ctx* c_, double* ms_, int64_t* cnt_) : c(c_), ms(ms_), cnt(cnt_)
     {
         if (c->prof) cudaEventRecord(c->pev[0], c->stream);
     }
-    ~ProfScope()
+    void end()
     {
+        if (done) return;
+        done = true;
         if (!c->prof) return;
         cudaEventRecord(c->pev[1], c->stream);
         cudaEventSynchronize(c->pev[1]);
         float t = 0;
         cudaEventElapsedTime(&t, c->pev[0], c->pev[1]);
         *ms += t;
-        (*cnt)++;
+        if (cnt) (*cnt)++;
     }
+    ~ProfScope() { end(); }
 };
 
 }  // namespace ma

@@ -201,10 +201,10 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs a)
 
 // solve H[:n-1,:n-1] x = b (b, x device vectors of length n; x[n-1] = 0)
 static ma_status pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, int maxiter, int* iters,
-                           double* relres, int precond)
+                           double* relres, int precond, int reuse = 0)
 {
     if (precond == MA_PRECOND_MULTIGRID && amg_levels(n) >= 2)
-        return amg_pcg_solve(c, n, b, x, rtol, maxiter, iters, relres);
+        return amg_pcg_solve(c, n, b, x, rtol, maxiter, reuse, iters, relres);
     cudaStream_t s = c->stream;
     MA_CUDA(c, c->cg_r.ensure(sizeof(double) * n));
     MA_CUDA(c, c->cg_z.ensure(sizeof(double) * n));
@@ -311,6 +311,8 @@ using namespace ma;
 
 // The Newton iteration of MA::ot_solve on one set of sites (device arrays; w in/out).
 constexpr double kForcing = 1e-2;  // relative CG residual of a Newton direction (cg_rtol = 0)
+constexpr int kAggRefresh = 4;  // Newton steps per multigrid aggregation (the sites do not move; the
+                                // Hessian's strengths drift: +1 to 4 CG iterations by the fourth step)
 
 static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, const double* dy, const double* dnu,
                              double* w, const ma_solve_opts& o, ma_stats& S)
@@ -421,8 +423,11 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
             // 64^2 / 1,000-site, 512^2 / 100,000-site and 2048^2 / 1M-site workloads)
             // while tighter solves only cost CG iterations
             double rtol = default_forcing ? kForcing : o.cg_rtol;
+            // the multigrid's aggregates are rebuilt every kAggRefresh Newton steps of
+            // this solve; the steps between rebuild only its Galerkin matrices
+            const int reuse = (niter - 1) % kAggRefresh != 0;
             if ((st = pcg_solve(c, n, c->g.as<double>(), c->dirn.as<double>(), rtol, (int)o.cg_maxiter, &it,
-                                &rr, o.precond)) != MA_OK) {
+                                &rr, o.precond, reuse)) != MA_OK) {
                 result = st;
                 break;
             }
