@@ -204,7 +204,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
                            c->t_parent.as<int>(), c->t_leaf_parent.as<int>(), c->t_flag.as<int>(),
                            c->t_box.as<double4>(), c->t_mom.p, c->t_ab.as<double4>(), s);
     }
-    c->launches += 2;
+    c->launches += 1 + tree_bounds_launches(n);
     MA_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * 4, s));
     MA_CUDA(c, cudaMemsetAsync(c->nredo.p, 0, sizeof(int) * 4, s));
     MA_CUDA(c, cudaMemsetAsync(c->big_index.p, 0xFF, sizeof(int) * (size_t)n, s));

@@ -174,23 +174,25 @@ __global__ void k_tree_boxes(const SiteD* sites, int n, const int2* child, const
 }
 
 // moments for the least-squares slope of phi: count, mean x, mean y, Sxx, Sxy, Syy,
-// mean phi, Sxphi, Syphi (centred sums, merged with Chan's update)
+// mean phi, Sxphi, Syphi (centred sums, merged with Chan's update).  FP32: the slope
+// only has to fit, the offset alpha below is exact for whatever slope is chosen.
 struct Mom {
-    double c, mx, my, sxx, sxy, syy, mf, sxf, syf;
+    float c, mx, my, sxx, sxy, syy, mf, sxf, syf;
 };
 
-__device__ __forceinline__ Mom mom_leaf(double x, double y, double f)
+__device__ __forceinline__ Mom mom_leaf(const SiteD& s)
 {
-    return Mom{1.0, x, y, 0.0, 0.0, 0.0, f, 0.0, 0.0};
+    const float x = (float)s.x, y = (float)s.y;
+    return Mom{1.0f, x, y, 0.0f, 0.0f, 0.0f, 0.5f * (x * x + y * y - (float)s.w), 0.0f, 0.0f};
 }
 
 __device__ __forceinline__ Mom mom_merge(const Mom& a, const Mom& b)
 {
     Mom r;
     r.c = a.c + b.c;
-    double ra = a.c / r.c, rb = b.c / r.c;
-    double dx = b.mx - a.mx, dy = b.my - a.my, df = b.mf - a.mf;
-    double w = a.c * b.c / r.c;
+    const float rb = b.c / r.c;
+    const float dx = b.mx - a.mx, dy = b.my - a.my, df = b.mf - a.mf;
+    const float w = a.c * b.c / r.c;
     r.mx = a.mx + dx * rb;
     r.my = a.my + dy * rb;
     r.mf = a.mf + df * rb;
@@ -199,7 +201,6 @@ __device__ __forceinline__ Mom mom_merge(const Mom& a, const Mom& b)
     r.syy = a.syy + b.syy + w * dy * dy;
     r.sxf = a.sxf + b.sxf + w * dx * df;
     r.syf = a.syf + b.syf + w * dy * df;
-    (void)ra;
     return r;
 }
 
@@ -212,7 +213,7 @@ __device__ __forceinline__ double site_alpha(const SiteD& s, double bx, double b
     return v - 1e-15 * (s.x * s.x + s.y * s.y + fabs(s.w) + fabs(bx * s.x) + fabs(by * s.y));
 }
 
-// Nodes of at most this many sites take the exact offset alpha = min over their
+// Nodes of fewer than this many sites take the exact offset alpha = min over their
 // sites of phi_j - beta . x_j; larger ones combine their children's bounds, which
 // adds the spread of the child's slope over the child's box.  Propagated through
 // every level that spread compounds to several squared site spacings and lets an
@@ -220,22 +221,26 @@ __device__ __forceinline__ double site_alpha(const SiteD& s, double bx, double b
 // nodes are far enough from the cells that test them for it not to matter.
 constexpr int kExactAlpha = 64;
 
-// alpha bound contributed by one child for the parent's slope beta
-__device__ __forceinline__ double child_alpha(int c, const SiteD* sites, const double4* box, const double4* ab,
-                                              double bx, double by)
+__device__ __forceinline__ bool small_node(const int2* range, int nd) { return range[nd].y - range[nd].x < kExactAlpha; }
+
+// doubles as unsigned keys in the same order (for atomicMin)
+__device__ __forceinline__ unsigned long long ord_key(double v)
 {
-    if (c < 0) return site_alpha(sites[c & 0x7fffffff], bx, by);
-    double4 a = load_published(&ab[c]);
-    if (!(a.x < INFINITY)) return INFINITY;
-    double4 b = load_published(&box[c]);
-    double gx = a.y - bx, gy = a.z - by;
-    double mx = fmin(gx * b.x, gx * b.z), my = fmin(gy * b.y, gy * b.w);
-    double v = a.x + mx + my;
-    return v - 1e-15 * (fabs(a.x) + fabs(mx) + fabs(my));
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
-__global__ void k_tree_bounds(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
-                              const int* leaf_parent, int* flag, const double4* box, Mom* mom, double4* ab)
+__device__ __forceinline__ double ord_val(unsigned long long k)
+{
+    const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+// pass 1, bottom-up (the second thread to reach a node computes it): moments and the
+// least-squares slope beta of every internal node; the exact-offset slots of the
+// small nodes set to +infinity
+__global__ void k_tree_slopes(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
+                              const int* leaf_parent, int* flag, Mom* mom, unsigned long long* amin, double4* ab)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -244,40 +249,102 @@ __global__ void k_tree_bounds(const SiteD* sites, int n, const int2* child, cons
         __threadfence();
         if (atomicAdd(&flag[nd], 1) == 0) return;
         __threadfence();
-        int2 c = child[nd];
+        const int2 c = child[nd];
         Mom m[2];
-        int cs[2] = {c.x, c.y};
+        const int cs[2] = {c.x, c.y};
         for (int q = 0; q < 2; q++) {
             if (cs[q] < 0) {
-                SiteD s = sites[cs[q] & 0x7fffffff];
-                m[q] = mom_leaf(s.x, s.y, phi_of(s));
+                m[q] = mom_leaf(sites[cs[q] & 0x7fffffff]);
             } else {
-                volatile Mom* vm = (volatile Mom*)&mom[cs[q]];
+                const volatile Mom* vm = (const volatile Mom*)&mom[cs[q]];
                 m[q] = Mom{vm->c, vm->mx, vm->my, vm->sxx, vm->sxy, vm->syy, vm->mf, vm->sxf, vm->syf};
             }
         }
-        Mom r = mom_merge(m[0], m[1]);
+        const Mom r = mom_merge(m[0], m[1]);
         mom[nd] = r;
         // least-squares slope; the centroid (slope of |x|^2/2) when the fit is degenerate
-        double det = r.sxx * r.syy - r.sxy * r.sxy;
-        double bx = r.mx, by = r.my;
-        if (r.c >= 3.0 && det > 1e-9 * (r.sxx * r.syy) && det > 0.0) {
+        const float det = r.sxx * r.syy - r.sxy * r.sxy;
+        float bx = r.mx, by = r.my;
+        if (r.c >= 3.0f && det > 1e-6f * (r.sxx * r.syy) && det > 0.0f) {
             bx = (r.syy * r.sxf - r.sxy * r.syf) / det;
             by = (r.sxx * r.syf - r.sxy * r.sxf) / det;
         }
-        double al;
-        const int2 rg = range[nd];
-        if (rg.y - rg.x < kExactAlpha) {
-            // small node: the exact minimum over its own sites (a contiguous Morton range)
-            al = INFINITY;
-            for (int q = rg.x; q <= rg.y; q++) al = fmin(al, site_alpha(sites[q], bx, by));
-        } else {
-            // large node: from the children's bounds, widened by the child boxes
-            al = fmin(child_alpha(c.x, sites, box, ab, bx, by), child_alpha(c.y, sites, box, ab, bx, by));
+        if (!(isfinite(bx) && isfinite(by))) {
+            bx = r.mx;
+            by = r.my;
         }
-        if (!(al == al)) al = -INFINITY;  // never prune a node whose bound is not finite
-        ab[nd] = make_double4(al, bx, by, 0.0);
+        ab[nd] = make_double4(-INFINITY, (double)bx, (double)by, 0.0);
+        amin[nd] = ord_key(INFINITY);
         nd = parent[nd];
+    }
+}
+
+// pass 2, one thread per site: its term phi_j - beta . x_j in every small ancestor's
+// minimum (exact FP64, every lane busy)
+__global__ void k_tree_small_alpha(const SiteD* sites, int n, const int2* range, const int* parent,
+                                   const int* leaf_parent, const double4* ab, unsigned long long* amin)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const SiteD s = sites[k];
+    for (int nd = leaf_parent[k]; nd >= 0 && small_node(range, nd); nd = parent[nd]) {
+        double v = site_alpha(s, ab[nd].y, ab[nd].z);
+        if (!(v == v)) v = -INFINITY;  // never prune a node whose bound is not finite
+        atomicMin(&amin[nd], ord_key(v));
+    }
+}
+
+// alpha bound contributed by one child for the parent's slope beta: a site's own
+// term, a small node's exact offset, or a large node's bound widened over its box
+__device__ __forceinline__ double child_alpha(int c, const SiteD* sites, const int2* range, const double4* box,
+                                              const double4* ab, const unsigned long long* amin, double bx, double by)
+{
+    if (c < 0) return site_alpha(sites[c & 0x7fffffff], bx, by);
+    double4 a = load_published(&ab[c]);
+    if (small_node(range, c)) a.x = ord_val(amin[c]);
+    if (!(a.x < INFINITY)) return INFINITY;
+    const double4 b = box[c];
+    const double gx = a.y - bx, gy = a.z - by;
+    const double mx = fmin(gx * b.x, gx * b.z), my = fmin(gy * b.y, gy * b.w);
+    const double v = a.x + mx + my;
+    return v - 1e-15 * (fabs(a.x) + fabs(mx) + fabs(my));
+}
+
+// pass 3, one thread per internal node: a small node takes its exact minimum; the
+// large nodes are computed bottom-up from their children (the second arrival
+// computes a node; a child that is a site or a small node is there from the start)
+__global__ void k_tree_large_alpha(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
+                                   int* flag, const double4* box, const unsigned long long* amin, double4* ab)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n - 1) return;
+    if (small_node(range, t)) {
+        double a = ord_val(amin[t]);
+        if (!(a == a)) a = -INFINITY;
+        ab[t].x = a;
+        return;
+    }
+    const int2 c0 = child[t];
+    const int ready = (c0.x < 0 || small_node(range, c0.x)) + (c0.y < 0 || small_node(range, c0.y));
+    if (ready == 0) return;
+    int nd = t;
+    if (ready == 1) {
+        __threadfence();
+        if (atomicAdd(&flag[nd], 1) == 0) return;
+        __threadfence();
+    }
+    while (true) {
+        const int2 c = child[nd];
+        const double4 own = ab[nd];
+        double al = fmin(child_alpha(c.x, sites, range, box, ab, amin, own.y, own.z),
+                         child_alpha(c.y, sites, range, box, ab, amin, own.y, own.z));
+        if (!(al == al)) al = -INFINITY;
+        ab[nd].x = al;
+        nd = parent[nd];
+        if (nd < 0) return;
+        __threadfence();
+        if (atomicAdd(&flag[nd], 1) == 0) return;
+        __threadfence();
     }
 }
 
@@ -348,14 +415,22 @@ void launch_perm_gather(const uint64_t* keys, const double* x, const double* y, 
     k_perm_gather<<<(n + 255) / 256, 256, 0, s>>>(keys, x, y, w, n, perm, sites, posf);
 }
 
-size_t tree_mom_bytes(int n) { return sizeof(Mom) * (size_t)(n > 1 ? n - 1 : 1); }
+// per internal node: its moments, then (8-byte aligned) its exact-offset slot
+static size_t mom_part(int n) { return (sizeof(Mom) * (size_t)(n > 1 ? n - 1 : 1) + 15) & ~(size_t)15; }
+size_t tree_mom_bytes(int n) { return mom_part(n) + sizeof(unsigned long long) * (size_t)(n > 1 ? n - 1 : 1); }
 
 void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
                         const int* leaf_parent, int* flag, const double4* box, void* mom, double4* ab, cudaStream_t s)
 {
     if (n < 2) return;
+    Mom* m = (Mom*)mom;
+    unsigned long long* amin = (unsigned long long*)((char*)mom + mom_part(n));
+    const unsigned g = (unsigned)((n + 255) / 256);
     cudaMemsetAsync(flag, 0, sizeof(int) * (n - 1), s);
-    k_tree_bounds<<<(n + 255) / 256, 256, 0, s>>>(sites, n, child, range, parent, leaf_parent, flag, box, (Mom*)mom, ab);
+    k_tree_slopes<<<g, 256, 0, s>>>(sites, n, child, range, parent, leaf_parent, flag, m, amin, ab);
+    k_tree_small_alpha<<<g, 256, 0, s>>>(sites, n, range, parent, leaf_parent, ab, amin);
+    cudaMemsetAsync(flag, 0, sizeof(int) * (n - 1), s);
+    k_tree_large_alpha<<<g, 256, 0, s>>>(sites, n, child, range, parent, flag, box, amin, ab);
 }
 
 }  // namespace ma

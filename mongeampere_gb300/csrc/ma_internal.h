@@ -116,6 +116,7 @@ void launch_tree(const uint64_t* keys, int n, int2* child, int2* range, int* par
 void launch_tree_boxes(const SiteD* sites, int n, const int2* child, const int* parent, const int* leaf_parent,
                        int* flag, double4* box, float4* boxf, cudaStream_t s);
 size_t tree_mom_bytes(int n);
+inline int tree_bounds_launches(int n) { return n < 2 ? 0 : 3; }
 void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
                         const int* leaf_parent, int* flag, const double4* box, void* mom, double4* ab, cudaStream_t s);
 void launch_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);  // exclusive, out has n+1

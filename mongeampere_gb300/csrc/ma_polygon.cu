@@ -174,7 +174,7 @@ ma_status ma_polygon_cells(ma_ctx* cp, int64_t n, const double* x, const double*
     launch_tree_bounds(c->sites.as<SiteD>(), nn, c->t_child.as<int2>(), c->t_range.as<int2>(),
                        c->t_parent.as<int>(), c->t_leaf_parent.as<int>(), c->t_flag.as<int>(),
                        c->t_box.as<double4>(), c->t_mom.p, c->t_ab.as<double4>(), s);
-    c->launches += 2;
+    c->launches += 1 + tree_bounds_launches(nn);
 
     MA_CUDA(c, c->pg_poly.ensure(sizeof(double) * 2 * kPgonMax));
     MA_CUDA(c, cudaMemcpyAsync(c->pg_poly.p, px, sizeof(double) * k, cudaMemcpyHostToDevice, s));
