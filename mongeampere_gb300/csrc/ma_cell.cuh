@@ -355,13 +355,13 @@ MA_HD void sanitize(float& ux, float& uy, float& ur)
     }
 }
 
-// crossing of fixed edge e (fixed point e -> e+1) with the radical axis of slot a
-template <class FX>
-MA_HD void vtx_fixed_bis(const FX& fx, int e, const Slot& a, float& ux, float& uy, float& ur)
+// crossing of the segment p -> q (owner-relative FP32 points with error radii) with
+// the radical axis of slot a
+MA_HD void vtx_seg_bis(float pxv, float pyv, float pr, float qxv, float qyv, float qr, const Slot& a, float& ux,
+                       float& uy, float& ur)
 {
-    int e1 = (e + 1 == fx.n) ? 0 : e + 1;
-    F px{fx.ux[e], fx.ur[e]}, py{fx.uy[e], fx.ur[e]};
-    F qx{fx.ux[e1], fx.ur[e1]}, qy{fx.uy[e1], fx.ur[e1]};
+    F px{pxv, pr}, py{pyv, pr};
+    F qx{qxv, qr}, qy{qyv, qr};
     F dx{a.dx, a.ed}, dy{a.dy, a.ed}, z{a.z, a.ez};
     F Ap = f_sub(f_scale2(f_add(f_mul(px, dx), f_mul(py, dy))), z);
     F ex = f_sub(qx, px), ey = f_sub(qy, py);
@@ -373,6 +373,14 @@ MA_HD void vtx_fixed_bis(const FX& fx, int e, const Slot& a, float& ux, float& u
     uy = Y.v;
     ur = fmaxf(X.e, Y.e);
     sanitize(ux, uy, ur);
+}
+
+// crossing of fixed edge e (fixed point e -> e+1) with the radical axis of slot a
+template <class FX>
+MA_HD void vtx_fixed_bis(const FX& fx, int e, const Slot& a, float& ux, float& uy, float& ur)
+{
+    int e1 = (e + 1 == fx.n) ? 0 : e + 1;
+    vtx_seg_bis(fx.ux[e], fx.uy[e], fx.ur[e], fx.ux[e1], fx.uy[e1], fx.ur[e1], a, ux, uy, ur);
 }
 
 // crossing of the radical axes of slots a and b (weighted circumcentre)

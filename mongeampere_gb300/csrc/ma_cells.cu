@@ -96,6 +96,41 @@ __device__ __forceinline__ void tri_triangle(const MeshTriDev& m, int t, const O
     c0 = l0 - gx * T.rx[0] - gy * T.ry[0];
 }
 
+// FP32 owner-relative corners of a triangle with their error radii (the values
+// set_fixed gives), in registers
+struct Corners {
+    float ux[3], uy[3], ur[3];
+};
+
+__device__ __forceinline__ float corner_radius(float ux, float uy) { return kU32 * fmaxf(fabsf(ux), fabsf(uy)) + 1e-37f; }
+
+__device__ __forceinline__ Corners grid_corners(const MeshGridDev& m, int i, int j, int tt, const Owner& o)
+{
+    const float x0 = (float)dsub(m.gx[i], o.x), x1 = (float)dsub(m.gx[i + 1], o.x);
+    const float y0 = (float)dsub(m.gy[j], o.y), y1 = (float)dsub(m.gy[j + 1], o.y);
+    Corners c;
+    c.ux[0] = x0;
+    c.uy[0] = y0;
+    c.ux[1] = x1;
+    c.uy[1] = tt == 0 ? y0 : y1;
+    c.ux[2] = tt == 0 ? x1 : x0;
+    c.uy[2] = y1;
+    for (int e = 0; e < 3; e++) c.ur[e] = corner_radius(c.ux[e], c.uy[e]);
+    return c;
+}
+
+__device__ __forceinline__ Corners tri_corners(const MeshTriDev& m, int t, const Owner& o)
+{
+    Corners c;
+    for (int e = 0; e < 3; e++) {
+        const int a = m.tri[3 * t + e];
+        c.ux[e] = (float)dsub(m.vx[a], o.x);
+        c.uy[e] = (float)dsub(m.vy[a], o.y);
+        c.ur[e] = corner_radius(c.ux[e], c.uy[e]);
+    }
+    return c;
+}
+
 struct GridVisitor {
     MeshGridDev m;
     template <class Fn>
@@ -427,9 +462,19 @@ struct CellInfo {
 // the two passes that materialise the pieces (count per cell, then emit)
 constexpr int kModeEval = 0, kModeMoments = 1, kModeVjp = 2, kModeCount = 3, kModeEmit = 4, kModeMixed = 5;
 
+// phase A's cooperative clip: the polygon being clipped (one vertex per lane) passes
+// through here between clip steps; the round's clipped pieces wait here for the list
+struct ClipStage {
+    float ux[32], uy[32], ur[32];
+    int lab[32];
+    int8_t res_lab[32][kPV];
+    int8_t res_n[32];  // vertices of the clipped piece of each lane's entry; -1: needs the large pass
+};
+
 template <int MODE>
 struct PieceWarp {
     static constexpr int kAcc = MODE == kModeVjp ? 3 : (MODE == kModeMoments ? 7 : 2);
+    ClipStage cs;
     Slot slot[kSlotPool];
     Nb64 nb[kSlotPool];
     PieceRec rec[kList];
@@ -460,6 +505,11 @@ struct GridPieces {
     {
         int sq = id >> 1;
         grid_fixed(m, sq % (m.nx - 1), sq / (m.nx - 1), id & 1, o, T);
+    }
+    __device__ __forceinline__ Corners corners(int id, const Owner& o) const
+    {
+        int sq = id >> 1;
+        return grid_corners(m, sq % (m.nx - 1), sq / (m.nx - 1), id & 1, o);
     }
     __device__ __forceinline__ void triangle(int id, const Owner& o, Fixed& T, double& c0, double& gx,
                                              double& gy) const
@@ -511,6 +561,7 @@ struct TriPieces {
         return -1;
     }
     __device__ __forceinline__ void fixed(int id, const Owner& o, Fixed& T) const { tri_fixed(m, id, o, T); }
+    __device__ __forceinline__ Corners corners(int id, const Owner& o) const { return tri_corners(m, id, o); }
     __device__ __forceinline__ void triangle(int id, const Owner& o, Fixed& T, double& c0, double& gx,
                                              double& gy) const
     {
@@ -716,10 +767,10 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
             int L = 0;
             while (f < total && L <= kList - 32) {
                 const int idx = f + lane;
-                bool keep = false, bad = false;
                 int cc = 0, id = -1;
-                Poly<kClipCap> PA, PB;
-                Poly<kClipCap>* P = &PA;
+                bool out = true;  // no triangle, or one outside the cell
+                uint64_t cut = 0;
+                Corners K;
                 if (idx < total) {
                     while (W.ci[cc + 1].pre <= idx) cc++;
                     const CellInfo& C = W.ci[cc];
@@ -727,61 +778,160 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                     if (id >= 0) {
                         const SiteD S = A.sites[C.k];
                         const Owner o{S.x, S.y, S.w, C.k};
-                        Fixed T;
-                        mesh.fixed(id, o, T);
-                        P->n = 3;
-                        for (int e = 0; e < 3; e++) {
-                            P->lab[e] = -1 - e;
-                            P->ux[e] = T.ux[e];
-                            P->uy[e] = T.uy[e];
-                            P->ur[e] = T.ur[e];
-                        }
-                        Poly<kClipCap>* Q = &PB;
                         const Slot* sl = W.slot + C.soff;
-                        // certified corner tests first, in registers: a slot with all three
-                        // corners outside rejects the triangle, a slot with all three inside
-                        // contains every sub-polygon of it and needs no clip
-                        uint64_t cut = 0;
+                        // certified corner tests: a slot with all three corners outside
+                        // rejects the triangle; a slot with all three inside contains every
+                        // sub-polygon of it and needs no clip
+                        K = mesh.corners(id, o);
+                        out = false;
                         for (int s = 0; s < C.m; s++) {
                             const Slot cs = sl[s];
-                            const int t0 = test32(T.ux[0], T.uy[0], T.ur[0], cs);
-                            const int t1 = test32(T.ux[1], T.uy[1], T.ur[1], cs);
-                            const int t2 = test32(T.ux[2], T.uy[2], T.ur[2], cs);
+                            const int t0 = test32(K.ux[0], K.uy[0], K.ur[0], cs);
+                            const int t1 = test32(K.ux[1], K.uy[1], K.ur[1], cs);
+                            const int t2 = test32(K.ux[2], K.uy[2], K.ur[2], cs);
                             if (t0 > 0 && t1 > 0 && t2 > 0) {
-                                P->n = 0;
+                                out = true;
                                 break;
                             }
                             if (!(t0 < 0 && t1 < 0 && t2 < 0)) cut |= 1ull << s;
                         }
-                        while (cut && P->n > 0) {
-                            const int s = __ffsll((long long)cut) - 1;
-                            cut &= cut - 1;
-                            if (clip_poly<kClipCap, false>(*P, *Q, s, sl, T, o, A.sites, st, bad)) {
-                                if (bad) break;
-                                Poly<kClipCap>* t = P;
-                                P = Q;
-                                Q = t;
-                            }
-                        }
-                        if (!bad && P->n > kPV) bad = true;
-                        keep = !bad && P->n > 0;
                     }
                 }
+                // the triangles that some radical axis crosses, clipped one at a time by
+                // the whole warp: lane v holds vertex v, a clip step is a ballot of the
+                // vertices outside, an exclusive scan of the Sutherland-Hodgman outputs
+                // (vtx_* of ma_cell.cuh for the new vertices) and a pass through the stage
+                unsigned pend = __ballot_sync(kFull, !out && cut != 0);
+                while (pend) {
+                    const int src = __ffs(pend) - 1;
+                    pend &= pend - 1;
+                    const int ecc = __shfl_sync(kFull, cc, src), eid = __shfl_sync(kFull, id, src);
+                    uint64_t ecut = ((uint64_t)__shfl_sync(kFull, (unsigned)(cut >> 32), src) << 32) |
+                                    (uint64_t)__shfl_sync(kFull, (unsigned)cut, src);
+                    float cx[3], cy[3], cr[3];
+                    for (int e = 0; e < 3; e++) {
+                        cx[e] = __shfl_sync(kFull, K.ux[e], src);
+                        cy[e] = __shfl_sync(kFull, K.uy[e], src);
+                        cr[e] = __shfl_sync(kFull, K.ur[e], src);
+                    }
+                    const CellInfo& C = W.ci[ecc];
+                    const SiteD S = A.sites[C.k];
+                    const Owner o{S.x, S.y, S.w, C.k};
+                    const Slot* sl = W.slot + C.soff;
+                    int n = 3;
+                    float pux = lane == 0 ? cx[0] : (lane == 1 ? cx[1] : cx[2]);
+                    float puy = lane == 0 ? cy[0] : (lane == 1 ? cy[1] : cy[2]);
+                    float pur = lane == 0 ? cr[0] : (lane == 1 ? cr[1] : cr[2]);
+                    int plab = -1 - min(lane, 2);
+                    bool ebad = false;
+                    while (ecut && n > 0) {
+                        const int s = __ffsll((long long)ecut) - 1;
+                        ecut &= ecut - 1;
+                        const Slot c = sl[s];
+                        const bool act = lane < n;
+                        const int prevlab = __shfl_sync(kFull, plab, lane == 0 ? n - 1 : lane - 1);
+                        bool vout = false, und = false;
+                        if (act) {
+                            const int t = test32(pux, puy, pur, c);
+                            if (t != 0) {
+                                vout = t > 0;
+                            } else {
+                                Fixed T;  // the exact corners, only for an undecided vertex
+                                mesh.fixed(eid, o, T);
+                                vout = !sym_inside<kClipCap, false>(prevlab, plab, sl, T, o, A.sites, c.site, st, und);
+                            }
+                        }
+                        if (__any_sync(kFull, und)) {
+                            // an exact decision is needed: the cell is redone by the exact pass
+                            st |= ST_NEED_EXACT;
+                            ebad = true;
+                            break;
+                        }
+                        const unsigned om = __ballot_sync(kFull, act && vout);
+                        const int nout = __popc(om);
+                        if (nout == 0) continue;
+                        if (nout == n) {
+                            n = 0;
+                            break;
+                        }
+                        const int v1 = lane + 1 == n ? 0 : lane + 1;
+                        const bool in0 = act && !vout, in1 = !((om >> v1) & 1u);
+                        const int cnt = act ? (in0 ? (in1 ? 1 : 2) : (in1 ? 1 : 0)) : 0;
+                        int pos = cnt;
+                        for (int d = 1; d < 32; d <<= 1) {
+                            const int y = __shfl_up_sync(kFull, pos, d);
+                            if (lane >= d) pos += y;
+                        }
+                        const int m = __shfl_sync(kFull, pos, 31);
+                        pos -= cnt;
+                        if (m > kClipCap) {
+                            ebad = true;
+                            break;
+                        }
+                        if (act) {
+                            int q = pos;
+                            if (in0) {
+                                W.cs.ux[q] = pux;
+                                W.cs.uy[q] = puy;
+                                W.cs.ur[q] = pur;
+                                W.cs.lab[q] = plab;
+                                q++;
+                            }
+                            if (in0 != in1) {
+                                float nx, ny, nr;
+                                if (plab < 0) {
+                                    const int e = -1 - plab, e1 = e == 2 ? 0 : e + 1;
+                                    vtx_seg_bis(cx[e], cy[e], cr[e], cx[e1], cy[e1], cr[e1], c, nx, ny, nr);
+                                } else {
+                                    vtx_bis_bis(sl[plab], c, nx, ny, nr);
+                                }
+                                W.cs.ux[q] = nx;
+                                W.cs.uy[q] = ny;
+                                W.cs.ur[q] = nr;
+                                W.cs.lab[q] = in0 ? s : plab;
+                            }
+                        }
+                        __syncwarp();
+                        n = m;
+                        if (lane < n) {
+                            pux = W.cs.ux[lane];
+                            puy = W.cs.uy[lane];
+                            pur = W.cs.ur[lane];
+                            plab = W.cs.lab[lane];
+                        }
+                        __syncwarp();
+                    }
+                    if (!ebad && n > kPV) ebad = true;
+                    if (lane == 0) W.cs.res_n[src] = (int8_t)(ebad ? -1 : n);
+                    if (!ebad && lane < n) W.cs.res_lab[src][lane] = (int8_t)plab;
+                }
+                __syncwarp();
+                const bool whole = !out && cut == 0;
+                const int rn = (!out && cut != 0) ? (int)W.cs.res_n[lane] : 0;
+                const bool bad = rn < 0;
+                const bool keep = whole || rn > 0;
                 redo |= __reduce_or_sync(kFull, bad ? (1u << (g0 + cc)) : 0u);
                 const unsigned bal = __ballot_sync(kFull, keep);
+                const int pn = whole ? 3 : (keep ? rn : 0);
                 if (keep) {
                     PieceRec& R = W.rec[L + __popc(bal & ((1u << lane) - 1u))];
                     R.tri = id;
                     R.cell = (int8_t)cc;
-                    R.n = (int8_t)P->n;
-                    for (int e = 0; e < P->n; e++) R.lab[e] = (int8_t)P->lab[e];
+                    R.n = (int8_t)pn;
+                    if (whole) {
+                        R.lab[0] = -1;
+                        R.lab[1] = -2;
+                        R.lab[2] = -3;
+                    } else {
+                        for (int e = 0; e < pn; e++) R.lab[e] = W.cs.res_lab[lane][e];
+                    }
                 }
                 if (LISTING) {
                     // rank of each kept piece within its cell, and the vertices of the
                     // cell's earlier pieces (the lanes of one cell are adjacent)
                     const unsigned same = __match_any_sync(kFull, keep ? cc : -1 - lane);
                     const unsigned before = same & bal & ((1u << lane) - 1u);
-                    const int nk = keep ? P->n : 0;
+                    const int nk = pn;
                     int vpre = 0;
                     for (int j = 0; j < 32; j++) {
                         const int nj = __shfl_sync(kFull, nk, j);
