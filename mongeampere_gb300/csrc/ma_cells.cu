@@ -797,39 +797,54 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                         }
                     }
                 }
-                // the triangles that some radical axis crosses, clipped one at a time by
-                // the whole warp: lane v holds vertex v, a clip step is a ballot of the
-                // vertices outside, an exclusive scan of the Sutherland-Hodgman outputs
-                // (vtx_* of ma_cell.cuh for the new vertices) and a pass through the stage
+                // the triangles that some radical axis crosses, clipped two at a time, one
+                // per half-warp: lane v of the half holds vertex v, a clip step is a ballot
+                // of the vertices outside, an exclusive scan of the Sutherland-Hodgman
+                // outputs (vtx_* of ma_cell.cuh for the new vertices) and a pass through
+                // the half's part of the stage
+                static_assert(kClipCap == 16, "one polygon vertex per lane of a half-warp");
+                const int hw = lane >> 4, hl = lane & 15;
+                const unsigned hmask = 0xFFFFu << (16 * hw);
                 unsigned pend = __ballot_sync(kFull, !out && cut != 0);
                 while (pend) {
-                    const int src = __ffs(pend) - 1;
+                    const int s0 = __ffs(pend) - 1;
                     pend &= pend - 1;
-                    const int ecc = __shfl_sync(kFull, cc, src), eid = __shfl_sync(kFull, id, src);
-                    uint64_t ecut = ((uint64_t)__shfl_sync(kFull, (unsigned)(cut >> 32), src) << 32) |
-                                    (uint64_t)__shfl_sync(kFull, (unsigned)cut, src);
+                    int s1 = -1;
+                    if (pend) {
+                        s1 = __ffs(pend) - 1;
+                        pend &= pend - 1;
+                    }
+                    const int src = hw == 0 ? s0 : s1;
+                    const int srcq = src < 0 ? s0 : src;
+                    const int ecc = __shfl_sync(kFull, cc, srcq), eid = __shfl_sync(kFull, id, srcq);
+                    uint64_t ecut = ((uint64_t)__shfl_sync(kFull, (unsigned)(cut >> 32), srcq) << 32) |
+                                    (uint64_t)__shfl_sync(kFull, (unsigned)cut, srcq);
                     float cx[3], cy[3], cr[3];
                     for (int e = 0; e < 3; e++) {
-                        cx[e] = __shfl_sync(kFull, K.ux[e], src);
-                        cy[e] = __shfl_sync(kFull, K.uy[e], src);
-                        cr[e] = __shfl_sync(kFull, K.ur[e], src);
+                        cx[e] = __shfl_sync(kFull, K.ux[e], srcq);
+                        cy[e] = __shfl_sync(kFull, K.uy[e], srcq);
+                        cr[e] = __shfl_sync(kFull, K.ur[e], srcq);
                     }
                     const CellInfo& C = W.ci[ecc];
                     const SiteD S = A.sites[C.k];
                     const Owner o{S.x, S.y, S.w, C.k};
                     const Slot* sl = W.slot + C.soff;
-                    int n = 3;
-                    float pux = lane == 0 ? cx[0] : (lane == 1 ? cx[1] : cx[2]);
-                    float puy = lane == 0 ? cy[0] : (lane == 1 ? cy[1] : cy[2]);
-                    float pur = lane == 0 ? cr[0] : (lane == 1 ? cr[1] : cr[2]);
-                    int plab = -1 - min(lane, 2);
+                    float* sux = W.cs.ux + 16 * hw;
+                    float* suy = W.cs.uy + 16 * hw;
+                    float* sur = W.cs.ur + 16 * hw;
+                    int* slab = W.cs.lab + 16 * hw;
+                    int n = src < 0 ? 0 : 3;
+                    float pux = hl == 0 ? cx[0] : (hl == 1 ? cx[1] : cx[2]);
+                    float puy = hl == 0 ? cy[0] : (hl == 1 ? cy[1] : cy[2]);
+                    float pur = hl == 0 ? cr[0] : (hl == 1 ? cr[1] : cr[2]);
+                    int plab = -1 - min(hl, 2);
                     bool ebad = false;
                     while (ecut && n > 0) {
                         const int s = __ffsll((long long)ecut) - 1;
                         ecut &= ecut - 1;
                         const Slot c = sl[s];
-                        const bool act = lane < n;
-                        const int prevlab = __shfl_sync(kFull, plab, lane == 0 ? n - 1 : lane - 1);
+                        const bool act = hl < n;
+                        const int prevlab = __shfl_sync(hmask, plab, hl == 0 ? n - 1 : hl - 1, 16);
                         bool vout = false, und = false;
                         if (act) {
                             const int t = test32(pux, puy, pur, c);
@@ -841,28 +856,28 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                                 vout = !sym_inside<kClipCap, false>(prevlab, plab, sl, T, o, A.sites, c.site, st, und);
                             }
                         }
-                        if (__any_sync(kFull, und)) {
+                        if (__any_sync(hmask, und)) {
                             // an exact decision is needed: the cell is redone by the exact pass
                             st |= ST_NEED_EXACT;
                             ebad = true;
                             break;
                         }
-                        const unsigned om = __ballot_sync(kFull, act && vout);
+                        const unsigned om = (__ballot_sync(hmask, act && vout) >> (16 * hw)) & 0xFFFFu;
                         const int nout = __popc(om);
                         if (nout == 0) continue;
                         if (nout == n) {
                             n = 0;
                             break;
                         }
-                        const int v1 = lane + 1 == n ? 0 : lane + 1;
+                        const int v1 = hl + 1 == n ? 0 : hl + 1;
                         const bool in0 = act && !vout, in1 = !((om >> v1) & 1u);
                         const int cnt = act ? (in0 ? (in1 ? 1 : 2) : (in1 ? 1 : 0)) : 0;
                         int pos = cnt;
-                        for (int d = 1; d < 32; d <<= 1) {
-                            const int y = __shfl_up_sync(kFull, pos, d);
-                            if (lane >= d) pos += y;
+                        for (int d = 1; d < 16; d <<= 1) {
+                            const int y = __shfl_up_sync(hmask, pos, d, 16);
+                            if (hl >= d) pos += y;
                         }
-                        const int m = __shfl_sync(kFull, pos, 31);
+                        const int m = __shfl_sync(hmask, pos, 15, 16);
                         pos -= cnt;
                         if (m > kClipCap) {
                             ebad = true;
@@ -871,10 +886,10 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                         if (act) {
                             int q = pos;
                             if (in0) {
-                                W.cs.ux[q] = pux;
-                                W.cs.uy[q] = puy;
-                                W.cs.ur[q] = pur;
-                                W.cs.lab[q] = plab;
+                                sux[q] = pux;
+                                suy[q] = puy;
+                                sur[q] = pur;
+                                slab[q] = plab;
                                 q++;
                             }
                             if (in0 != in1) {
@@ -885,25 +900,28 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                                 } else {
                                     vtx_bis_bis(sl[plab], c, nx, ny, nr);
                                 }
-                                W.cs.ux[q] = nx;
-                                W.cs.uy[q] = ny;
-                                W.cs.ur[q] = nr;
-                                W.cs.lab[q] = in0 ? s : plab;
+                                sux[q] = nx;
+                                suy[q] = ny;
+                                sur[q] = nr;
+                                slab[q] = in0 ? s : plab;
                             }
                         }
-                        __syncwarp();
+                        __syncwarp(hmask);
                         n = m;
-                        if (lane < n) {
-                            pux = W.cs.ux[lane];
-                            puy = W.cs.uy[lane];
-                            pur = W.cs.ur[lane];
-                            plab = W.cs.lab[lane];
+                        if (hl < n) {
+                            pux = sux[hl];
+                            puy = suy[hl];
+                            pur = sur[hl];
+                            plab = slab[hl];
                         }
-                        __syncwarp();
+                        __syncwarp(hmask);
                     }
                     if (!ebad && n > kPV) ebad = true;
-                    if (lane == 0) W.cs.res_n[src] = (int8_t)(ebad ? -1 : n);
-                    if (!ebad && lane < n) W.cs.res_lab[src][lane] = (int8_t)plab;
+                    if (src >= 0) {
+                        if (hl == 0) W.cs.res_n[src] = (int8_t)(ebad ? -1 : n);
+                        if (!ebad && hl < n) W.cs.res_lab[src][hl] = (int8_t)plab;
+                    }
+                    __syncwarp();
                 }
                 __syncwarp();
                 const bool whole = !out && cut == 0;
