@@ -113,6 +113,7 @@ ma_status build_site_index_box(Ctx* c, double X0, double Y0, double X1, double Y
     MA_CUDA(c, c->t_boxf.ensure(sizeof(float4) * ni));
     MA_CUDA(c, c->t_mom.ensure(tree_mom_bytes(n)));
     MA_CUDA(c, c->t_ab.ensure(sizeof(double4) * ni));
+    MA_CUDA(c, c->t_nk.ensure(sizeof(float4) * ni));
     launch_morton(x, y, n, xmin, ymin, xmax, ymax, c->mkeys.as<uint64_t>(), s);
     launch_radix_sort(c->mkeys.as<uint64_t>(), c->mkeys_tmp.as<uint64_t>(), n, c->hist.as<int>(),
                       c->hist_scan.as<int>(), c->scan_scratch.as<int>(), s);
@@ -202,7 +203,8 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         ProfScope ps(c, &c->profile.bounds_ms, &c->profile.bounds_launches);
         launch_tree_bounds(c->sites.as<SiteD>(), n, c->t_child.as<int2>(), c->t_range.as<int2>(),
                            c->t_parent.as<int>(), c->t_leaf_parent.as<int>(), c->t_flag.as<int>(),
-                           c->t_box.as<double4>(), c->t_mom.p, c->t_ab.as<double4>(), s);
+                           c->t_box.as<double4>(), c->t_boxf.as<float4>(), c->t_mom.p,
+                           c->t_ab.as<double4>(), c->t_nk.as<float4>(), s);
     }
     c->launches += 1 + tree_bounds_launches(n);
     MA_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * 4, s));
@@ -219,6 +221,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     a.tree.box = c->t_box.as<double4>();
     a.tree.boxf = c->t_boxf.as<float4>();
     a.tree.ab = c->t_ab.as<double4>();
+    a.tree.nk = c->t_nk.as<float4>();
     a.tree.posf = c->posf.as<float2>();
     a.X0 = m->X0;
     a.Y0 = m->Y0;
@@ -491,7 +494,7 @@ void ma_ctx_destroy(ma_ctx* c)
                       &c->raster_col, &c->raster_img, &c->pg_poly, &c->pg_cnt, &c->pg_base, &c->pg_off,
                       &c->pg_xy, &c->pg_edge, &c->pg_list, &c->pg_work, &c->mkeys, &c->mkeys_tmp, &c->hist, &c->hist_scan,
                       &c->perm, &c->sites, &c->posf, &c->scan_scratch, &c->fill, &c->t_child, &c->t_range,
-                      &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab,
+                      &c->t_parent, &c->t_leaf_parent, &c->t_flag, &c->t_box, &c->t_boxf, &c->t_mom, &c->t_ab, &c->t_nk,
                       &c->keys, &c->bboxd, &c->mass, &c->vpart, &c->mom, &c->rowcnt,
                       &c->st_col, &c->st_val, &c->rowptr, &c->col, &c->val, &c->status, &c->redo, &c->nredo,
                       &c->stat_partial, &c->stat_out, &c->info, &c->big_index, &c->big_col, &c->big_val, &c->big_work, &c->wcur, &c->w0, &c->dirn, &c->g, &c->cg_r,

@@ -310,11 +310,23 @@ __device__ __forceinline__ double child_alpha(int c, const SiteD* sites, const i
     return v - 1e-15 * (fabs(a.x) + fabs(mx) + fabs(my));
 }
 
+// the bound about the node's FP32 box centre, for the FP32 node test of the cell stage
+__device__ __forceinline__ float4 node_k(double al, double bx, double by, const float4 bf)
+{
+    if (!(al > -INFINITY)) return make_float4(-INFINITY, 0.0f, 0.0f, 0.0f);
+    const double cx = (double)(0.5f * (bf.x + bf.z)), cy = (double)(0.5f * (bf.y + bf.w));
+    const double q = 0.5 * (cx * cx + cy * cy);
+    const double A = al + bx * cx + by * cy - q;
+    const double e = 8e-16 * (fabs(al) + fabs(bx * cx) + fabs(by * cy) + q);
+    return make_float4(__double2float_rd(A - e), (float)(bx - cx), (float)(by - cy), 0.0f);
+}
+
 // pass 3, one thread per internal node: a small node takes its exact minimum; the
 // large nodes are computed bottom-up from their children (the second arrival
 // computes a node; a child that is a site or a small node is there from the start)
 __global__ void k_tree_large_alpha(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
-                                   int* flag, const double4* box, const unsigned long long* amin, double4* ab)
+                                   int* flag, const double4* box, const float4* boxf, const unsigned long long* amin,
+                                   double4* ab, float4* nk)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n - 1) return;
@@ -322,6 +334,7 @@ __global__ void k_tree_large_alpha(const SiteD* sites, int n, const int2* child,
         double a = ord_val(amin[t]);
         if (!(a == a)) a = -INFINITY;
         ab[t].x = a;
+        nk[t] = node_k(a, ab[t].y, ab[t].z, boxf[t]);
         return;
     }
     const int2 c0 = child[t];
@@ -340,6 +353,7 @@ __global__ void k_tree_large_alpha(const SiteD* sites, int n, const int2* child,
                          child_alpha(c.y, sites, range, box, ab, amin, own.y, own.z));
         if (!(al == al)) al = -INFINITY;
         ab[nd].x = al;
+        nk[nd] = node_k(al, own.y, own.z, boxf[nd]);
         nd = parent[nd];
         if (nd < 0) return;
         __threadfence();
@@ -420,7 +434,8 @@ static size_t mom_part(int n) { return (sizeof(Mom) * (size_t)(n > 1 ? n - 1 : 1
 size_t tree_mom_bytes(int n) { return mom_part(n) + sizeof(unsigned long long) * (size_t)(n > 1 ? n - 1 : 1); }
 
 void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
-                        const int* leaf_parent, int* flag, const double4* box, void* mom, double4* ab, cudaStream_t s)
+                        const int* leaf_parent, int* flag, const double4* box, const float4* boxf, void* mom,
+                        double4* ab, float4* nk, cudaStream_t s)
 {
     if (n < 2) return;
     Mom* m = (Mom*)mom;
@@ -430,7 +445,7 @@ void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int2
     k_tree_slopes<<<g, 256, 0, s>>>(sites, n, child, range, parent, leaf_parent, flag, m, amin, ab);
     k_tree_small_alpha<<<g, 256, 0, s>>>(sites, n, range, parent, leaf_parent, ab, amin);
     cudaMemsetAsync(flag, 0, sizeof(int) * (n - 1), s);
-    k_tree_large_alpha<<<g, 256, 0, s>>>(sites, n, child, range, parent, flag, box, amin, ab);
+    k_tree_large_alpha<<<g, 256, 0, s>>>(sites, n, child, range, parent, flag, box, boxf, amin, ab, nk);
 }
 
 }  // namespace ma

@@ -18,6 +18,8 @@ struct SiteTree {
     const double4* box;   // x0, y0, x1, y1 (exact)
     const float4* boxf;   // the same rounded outwards
     const double4* ab;    // alpha, beta_x, beta_y: phi_j >= alpha + beta . x_j over the node
+    const float4* nk;     // the same about the FP32 box centre c: A = alpha + beta.c - |c|^2/2
+                          // (rounded down), beta_x - c_x, beta_y - c_y, 0
     const float2* posf;   // sorted site positions (FP32)
 };
 
@@ -118,7 +120,8 @@ void launch_tree_boxes(const SiteD* sites, int n, const int2* child, const int* 
 size_t tree_mom_bytes(int n);
 inline int tree_bounds_launches(int n) { return n < 2 ? 0 : 3; }
 void launch_tree_bounds(const SiteD* sites, int n, const int2* child, const int2* range, const int* parent,
-                        const int* leaf_parent, int* flag, const double4* box, void* mom, double4* ab, cudaStream_t s);
+                        const int* leaf_parent, int* flag, const double4* box, const float4* boxf, void* mom,
+                        double4* ab, float4* nk, cudaStream_t s);
 void launch_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);  // exclusive, out has n+1
 size_t scan_scratch_ints(int n);
 // cell kernels (ma_cells.cu)

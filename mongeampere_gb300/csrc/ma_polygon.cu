@@ -173,7 +173,8 @@ ma_status ma_polygon_cells(ma_ctx* cp, int64_t n, const double* x, const double*
     launch_update_weights(dw, c->perm.as<int>(), nn, c->sites.as<SiteD>(), s);
     launch_tree_bounds(c->sites.as<SiteD>(), nn, c->t_child.as<int2>(), c->t_range.as<int2>(),
                        c->t_parent.as<int>(), c->t_leaf_parent.as<int>(), c->t_flag.as<int>(),
-                       c->t_box.as<double4>(), c->t_mom.p, c->t_ab.as<double4>(), s);
+                       c->t_box.as<double4>(), c->t_boxf.as<float4>(), c->t_mom.p,
+                           c->t_ab.as<double4>(), c->t_nk.as<float4>(), s);
     c->launches += 1 + tree_bounds_launches(nn);
 
     MA_CUDA(c, c->pg_poly.ensure(sizeof(double) * 2 * kPgonMax));
@@ -201,6 +202,7 @@ ma_status ma_polygon_cells(ma_ctx* cp, int64_t n, const double* x, const double*
     a.tree.box = c->t_box.as<double4>();
     a.tree.boxf = c->t_boxf.as<float4>();
     a.tree.ab = c->t_ab.as<double4>();
+    a.tree.nk = c->t_nk.as<float4>();
     a.tree.posf = c->posf.as<float2>();
     a.X0 = X0;
     a.Y0 = Y0;

@@ -93,7 +93,7 @@ struct Ctx {
     int n = 0;
     int64_t index_epoch = 0;  // counts site-index builds
     DevBuf mkeys, mkeys_tmp, hist, hist_scan, perm, sites, posf, scan_scratch, fill;
-    DevBuf t_child, t_range, t_parent, t_leaf_parent, t_flag, t_box, t_boxf, t_mom, t_ab;
+    DevBuf t_child, t_range, t_parent, t_leaf_parent, t_flag, t_box, t_boxf, t_mom, t_ab, t_nk;
     DevBuf keys, bboxd;  // ordered keys and their doubles
     // evaluation outputs
     DevBuf mass, vpart, mom, rowcnt, st_col, st_val, rowptr, col, val, status, redo, nredo, stat_partial, stat_out;

@@ -56,31 +56,34 @@ __device__ __forceinline__ void compact_slots(Poly<CAP>& P, Slot* slots, int* ma
 //   pi_ij(p) / 2 = p.(x_j - x_i) + phi_i - phi_j
 //              <= (p - beta).(c - x_i) + |p_x - beta_x| h_x + |p_y - beta_y| h_y - K,
 //   K = alpha + beta.x_i - phi_i,
-// convex in p, so it suffices that it is negative at every vertex of P.  K and
-// x_i - beta are formed in FP64; the box enters through its FP32 copy (rounded
-// outwards, so it contains the node's sites) relative to the FP32 site position,
-// with the conversion errors absorbed into a wider box; every FP32 rounding of the
-// per-vertex loop is bounded.
+// convex in p, so it suffices that it is negative at every vertex of P.  Everything is
+// FP32 with bounded rounding.  K comes from the node's expansion about its box centre c
+// (nk, written with the bounds): with d = x_i - c and g = beta - c,
+//   K = A + g.d - |d|^2 / 2 + w_i / 2,   A = alpha + beta.c - |c|^2 / 2 (rounded down),
+// whose terms are all small where the test is close; x_i - beta = d - g.  The box enters
+// relative to the FP32 site position, with the conversion errors absorbed into a wider
+// box.
 template <int CAP>
-__device__ __forceinline__ bool node_harmless(const Poly<CAP>& P, const Owner& o, double phi_o, float ox, float oy,
-                                              const float4 bf, const double4 ab)
+__device__ __forceinline__ bool node_harmless(const Poly<CAP>& P, float ox, float oy, float owh, float oxa,
+                                              const float4 bf, const float4 nk)
 {
-    if (!(ab.x > -INFINITY)) return false;
-    double t = fma(ab.y, o.x, fma(ab.z, o.y, ab.x));
-    double K = t - phi_o;
-    float fK = (float)K;
-    float fke = 1.2e-16f * (fabsf((float)ab.x) + fabsf((float)t) + fabsf((float)phi_o)) * 8.0f + 1e-37f;
-    float fex = (float)(o.x - ab.y), fey = (float)(o.y - ab.z);
-    // box relative to the FP32 owner position; widen by the FP32 errors of the
-    // owner position and of the subtraction
-    float cx = 0.5f * (bf.x + bf.z) - ox, cy = 0.5f * (bf.y + bf.w) - oy;
+    if (!(nk.x > -INFINITY)) return false;
+    const float ccx = 0.5f * (bf.x + bf.z), ccy = 0.5f * (bf.y + bf.w);
+    const float dx = ox - ccx, dy = oy - ccy;
+    const float gdx = nk.y * dx, gdy = nk.z * dy, dd = 0.5f * (dx * dx + dy * dy);
+    const float fK = nk.x + (gdx + gdy) - dd + owh;
+    const float sg = fabsf(nk.y) + fabsf(nk.z), sd = fabsf(dx) + fabsf(dy);
+    const float fke = 1e-6f * (fabsf(nk.x) + fabsf(gdx) + fabsf(gdy) + dd + fabsf(owh)) +
+                      1.2e-7f * (sg + sd) * (oxa + sd) + 1e-37f;
+    const float fex = dx - nk.y, fey = dy - nk.z;
+    const float cx = -dx, cy = -dy;
     float hx = 0.5f * (bf.z - bf.x), hy = 0.5f * (bf.w - bf.y);
     float wx = 1.2e-7f * (fabsf(bf.x) + fabsf(bf.z) + 2.0f * fabsf(ox)) + 1e-37f;
     float wy = 1.2e-7f * (fabsf(bf.y) + fabsf(bf.w) + 2.0f * fabsf(oy)) + 1e-37f;
     hx = hx * 1.000001f + wx;
     hy = hy * 1.000001f + wy;
-    float L = fabsf(cx) + fabsf(cy) + hx + hy;
-    float e0 = 1.2e-7f * (fabsf(fex) + fabsf(fey));
+    const float L = fabsf(cx) + fabsf(cy) + hx + hy;
+    const float e0 = 1.2e-7f * (fabsf(fex) + fabsf(fey) + sd + sg + 2.0f * oxa);
     for (int v = 0; v < P.n; v++) {
         float qx = fex + P.ux[v], qy = fey + P.uy[v];
         float T = qx * cx + qy * cy + fabsf(qx) * hx + fabsf(qy) * hy - fK;
@@ -142,8 +145,8 @@ __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Ow
     }
     int ns = 0;
     const SiteTree& T = A.tree;
-    const double phi_o = 0.5 * (S.x * S.x + S.y * S.y - S.w);
     const float ox = (float)S.x, oy = (float)S.y;
+    const float owh = (float)(0.5 * S.w), oxa = fabsf(ox) + fabsf(oy);
     constexpr int kStack = 80;
     constexpr int kBucket = 4;
     constexpr int kWindow = 8;
@@ -229,7 +232,7 @@ __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Ow
         bool contains = rg.x <= k && k <= rg.y;
         if (!contains) {
             r.tested++;
-            if (node_harmless(*P, o, phi_o, ox, oy, T.boxf[nd], T.ab[nd])) {
+            if (node_harmless(*P, ox, oy, owh, oxa, T.boxf[nd], T.nk[nd])) {
                 r.pruned++;
                 continue;
             }

@@ -52,9 +52,19 @@ int main()
                 area += 0.5 * (P.first * Q.second - Q.first * P.second);
             }
         });
-        std::printf("total mass %.15g, solve error %.3g after %zu Newton steps, %d pieces of area %.15g\n", tot, err,
-                    stats.niter, np, area);
-        if (std::fabs(tot - 1.0) > 1e-12 || err > 1e-12 || std::fabs(area - 1.0) > 1e-12 || h.nonZeros() != 9)
+        // the cells clipped to the unit square add up to its area
+        MA::Polygon sq{{0.0, 0.0}, {1.0, 0.0}, {1.0, 1.0}, {0.0, 1.0}};
+        double parea = 0;
+        for (const MA::Polygon& R : MA::voronoi_polygon_intersection(sq, X, x)) {
+            const size_t k = R.size();
+            for (size_t a = 0; a < k; a++)
+                parea += 0.5 * (R[a].first * R[(a + 1) % k].second - R[(a + 1) % k].first * R[a].second);
+        }
+        std::printf("total mass %.15g, solve error %.3g after %zu Newton steps, %d pieces of area %.15g, "
+                    "clipped cells of area %.15g\n",
+                    tot, err, stats.niter, np, area, parea);
+        if (std::fabs(tot - 1.0) > 1e-12 || err > 1e-12 || std::fabs(area - 1.0) > 1e-12 || h.nonZeros() != 9 ||
+            std::fabs(parea - 1.0) > 1e-12)
             return 4;
     } catch (const MA::Error& e) {
         std::printf("MA::Error: %s\n", e.what());
