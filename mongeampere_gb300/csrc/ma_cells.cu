@@ -481,6 +481,8 @@ struct PieceWarp {
     double out[kAcc][kList];
     double hvc[kPV][kList];
     CellInfo ci[kWarpCells + 1];
+    short epre[kList + 1];  // phase C: first contribution of each of the cell's listed pieces
+    signed char lead[64];   // phase C: the lane holding each slot's sum of a batch, or -1
 };
 
 // triangles of the grid mesh under a box: squares [i0, i0+nsx) x [j0, j0+nsy),
@@ -1056,17 +1058,73 @@ __global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
                     for (int p = p0 + lane; p < p1; p += 32) v += W.out[q][p];
                     run[q] += warp_sum(v);
                 }
-                for (int p = p0; p < p1 && !VJP && !LISTING; p++) {
-                    const int n = W.rec[p].n;
-                    for (int e = 0; e < n; e++) {
-                        const int l = W.rec[p].lab[e];
-                        if (l == lane) {
-                            h0 += W.hvc[e][p];
+                if (!VJP && !LISTING) {
+                    // the Hessian part of every edge (piece p, vertex e) of the cell's listed
+                    // pieces, 32 at a time in list order: the lanes with the same slot are
+                    // summed in lane order by the lowest of them, and lane l (l + 32) adds
+                    // the sums of slot l (l + 32) -- a fixed order, so the rows reproduce
+                    int eb = 0;
+                    for (int q = p0; q < p1; q += 32) {
+                        const int pp = q + lane;
+                        const int cnt = pp < p1 ? (int)W.rec[pp].n : 0;
+                        int x = cnt;
+                        for (int d = 1; d < 32; d <<= 1) {
+                            const int y = __shfl_up_sync(kFull, x, d);
+                            if (lane >= d) x += y;
+                        }
+                        if (pp < p1) W.epre[pp - p0] = (short)(eb + x - cnt);
+                        eb += __shfl_sync(kFull, x, 31);
+                    }
+                    if (lane == 0) W.epre[p1 - p0] = (short)eb;
+                    W.lead[lane] = -1;
+                    W.lead[lane + 32] = -1;
+                    __syncwarp();
+                    const int np = p1 - p0;
+                    for (int t0b = 0; t0b < eb; t0b += 32) {
+                        const int t = t0b + lane;
+                        int l = -1;
+                        double v = 0.0;
+                        if (t < eb) {
+                            int lo = 0, hi = np - 1;  // the piece: last epre <= t
+                            while (lo < hi) {
+                                const int mid = (lo + hi + 1) >> 1;
+                                if (W.epre[mid] <= t)
+                                    lo = mid;
+                                else
+                                    hi = mid - 1;
+                            }
+                            const int pq = p0 + lo, e = t - W.epre[lo];
+                            l = W.rec[pq].lab[e];
+                            if (l >= 0) v = W.hvc[e][pq];
+                        }
+                        const unsigned grp = __match_any_sync(kFull, l >= 0 ? l : -1 - lane);
+                        const bool leader = l >= 0 && (grp & ((1u << lane) - 1u)) == 0u;
+                        const int gmax = __reduce_max_sync(kFull, __popc(grp));
+                        double gs = 0.0;
+                        unsigned rem = grp;
+                        for (int r = 0; r < gmax; r++) {
+                            const int src = rem ? __ffs(rem) - 1 : lane;
+                            rem &= rem - 1;
+                            const double vr = __shfl_sync(kFull, v, src);
+                            if (leader && r < __popc(grp)) gs += vr;
+                        }
+                        if (leader) W.lead[l] = (signed char)lane;
+                        __syncwarp();
+                        const int l0 = W.lead[lane], l1 = W.lead[lane + 32];
+                        const double g0v = __shfl_sync(kFull, gs, l0 >= 0 ? l0 : lane);
+                        const double g1v = __shfl_sync(kFull, gs, l1 >= 0 ? l1 : lane);
+                        if (l0 >= 0) {
+                            h0 += g0v;
                             t0 = true;
-                        } else if (l == lane + 32) {
-                            h1 += W.hvc[e][p];
+                        }
+                        if (l1 >= 0) {
+                            h1 += g1v;
                             t1 = true;
                         }
+                        __syncwarp();
+                        W.lead[lane] = -1;
+                        W.lead[lane + 32] = -1;
+                        __syncwarp();
                     }
                 }
                 p0 = p1;
