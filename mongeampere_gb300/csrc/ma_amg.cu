@@ -84,14 +84,34 @@ __device__ void coarse_row(const CoarseSrc& s, int I, int lane, RowScratch& w, i
     __syncwarp();  // the warp's previous row is done with the scratch
     int E = 0;
     bool over = false;
-    for (int q = s.mp[I]; q < s.mp[I + 1] && !over; q++) {
-        const int i = s.mem[q];
-        const int k0 = s.rp[i], k1 = s.rp[i + 1];
-        for (int b = k0; b < k1; b += 32) {
-            const int k = b + lane;
+    // the members' row ranges at once (one member per lane), then their entries in
+    // member order, 32 at a time
+    const int M = s.mp[I + 1] - s.mp[I];
+    for (int m0 = 0; m0 < M && !over; m0 += 32) {
+        const int mm = min(32, M - m0);
+        int rb = 0, len = 0;
+        if (lane < mm) {
+            const int i = s.mem[s.mp[I] + m0 + lane];
+            rb = s.rp[i];
+            len = s.rp[i + 1] - rb;
+        }
+        int off = len;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, off, d);
+            if (lane >= d) off += y;
+        }
+        const int tot = __shfl_sync(0xffffffffu, off, 31);
+        off -= len;
+        for (int b = 0; b < tot; b += 32) {
+            const int t = b + lane;
+            int who = 0;
+            for (int m = 1; m < mm; m++)
+                if (t >= __shfl_sync(0xffffffffu, off, m)) who = m;
+            const int kb = __shfl_sync(0xffffffffu, rb, who), ko = __shfl_sync(0xffffffffu, off, who);
             int c = -1;
             double v = 0.0;
-            if (k < k1) {
+            if (t < tot) {
+                const int k = kb + (t - ko);
                 c = s.map[s.ci[k]];
                 v = s.va[k];
             }
@@ -653,16 +673,17 @@ __device__ __forceinline__ void restrict_fine(const AmgPcgArgs& a, const double*
 }
 
 // the coarsest level's solution cinv b, computed by every block into shared memory
-// before the phase that prolongs it
-__device__ __forceinline__ void coarsest_solve(const AmgPcgArgs& a, double* xc)
+// (xc) before the phase that prolongs it; cinv itself stays in shared memory (sinv)
+// for the whole kernel.  Thread r < n forms row r, its b[k] from shared memory.
+__device__ __forceinline__ void coarsest_solve(const AmgPcgArgs& a, double* xc, const double* sinv, double* sb)
 {
     const AmgLevelDev& C = a.L[a.nlev - 1];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int r = wid; r < C.n; r += kAmgThreads / 32) {
+    for (int k = threadIdx.x; k < C.n; k += kAmgThreads) sb[k] = C.b[k];
+    __syncthreads();
+    for (int r = threadIdx.x; r < C.n; r += kAmgThreads) {
         double v = 0.0;
-        for (int k = lane; k < C.n; k += 32) v += a.cinv[r * C.n + k] * C.b[k];
-        v = team_sum(v, 32);
-        if (lane == 0) xc[r] = v;
+        for (int k = 0; k < C.n; k++) v += sinv[k * C.n + r] * sb[k];
+        xc[r] = v;
     }
     __syncthreads();
 }
@@ -676,11 +697,11 @@ __device__ __forceinline__ double coarse_corr(const AmgPcgArgs& a, int l, int J,
 
 // xp_l for level l >= 1: pre-smoothed plus scaled coarse correction, then one
 // damped Jacobi sweep
-__device__ __forceinline__ void prolong_level(const AmgPcgArgs& a, int l, double* xc)
+__device__ __forceinline__ void prolong_level(const AmgPcgArgs& a, int l, double* xc, const double* sinv, double* sb)
 {
     const AmgLevelDev& A = a.L[l];
     const int T = A.tp;
-    if (l + 2 == a.nlev) coarsest_solve(a, xc);
+    if (l + 2 == a.nlev) coarsest_solve(a, xc, sinv, sb);
     team_rows(A.n, T, [&](int I, int t) {
         double s = 0.0, yI = 0.0, dI = 0.0;
         if (I >= 0) {
@@ -706,6 +727,8 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
     cg::grid_group grid = cg::this_grid();
     __shared__ double sh[40];
     __shared__ double xc[kCoarsest];
+    __shared__ double sb[kCoarsest];
+    __shared__ double sinv[kCoarsest * kCoarsest];  // the coarsest inverse, transposed
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
@@ -721,6 +744,10 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
     double* rc = a.r0;  // current residual
     double* rn = a.r1;  // next residual
 
+    if (!jacobi) {  // the coarsest inverse into shared memory, transposed
+        const int cn = a.L[a.nlev - 1].n;
+        for (int t = threadIdx.x; t < cn * cn; t += kAmgThreads) sinv[(t % cn) * cn + t / cn] = a.cinv[t];
+    }
     // x = 0, p = q = 0, r = b (active rows); the first pass below is a CG update
     // with alpha = 0
     for (int k = tid; k < n; k += stride) {
@@ -786,10 +813,10 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                 grid.sync();
             }
             for (int l = a.nlev - 2; l >= 1; l--) {
-                prolong_level(a, l, xc);
+                prolong_level(a, l, xc, sinv, sb);
                 grid.sync();
             }
-            if (a.nlev == 2) coarsest_solve(a, xc);
+            if (a.nlev == 2) coarsest_solve(a, xc, sinv, sb);
             for (int k = tid; k < n; k += stride) {
                 const double dk = F.dinv[k];
                 double zk = 0.0;
