@@ -615,6 +615,16 @@ __device__ __forceinline__ double team_sum(double v, int width)
     return v;
 }
 
+// inclusive sum of v over the lanes of a team of T (lanes below t included)
+__device__ __forceinline__ int team_scan(int v, int t, int T)
+{
+    for (int d = 1; d < T; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, v, d, T);
+        if (t >= d) v += y;
+    }
+    return v;
+}
+
 // Loop over rows [0, nrows) with teams of T lanes: calls fn(row, lane_in_team)
 // with row < nrows, or row = -1 for lanes without a row in this round (they still
 // take part in the team's shuffles).  Warp-uniform trip count.
@@ -640,12 +650,34 @@ __device__ __forceinline__ void restrict_level(const AmgPcgArgs& a, int l)
     const AmgLevelDev& C = a.L[l + 1];
     const int T = A.tr;
     team_rows(C.n, T, [&](int J, int t) {
+        // the members' rows at once (member q on team lane q), then their entries in
+        // member order, T at a time
+        // every loop bound is a maximum over the warp (teams of one warp share it)
+        const int q0 = J >= 0 ? A.mp[J] : 0, M = J >= 0 ? A.mp[J + 1] - q0 : 0;
+        const int Mmax = __reduce_max_sync(0xffffffffu, M);
         double s = 0.0;
-        if (J >= 0) {
-            for (int q = A.mp[J]; q < A.mp[J + 1]; q++) {
-                const int I = A.mem[q];
-                if (t == 0) s += A.b[I];
-                for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) {
+        for (int m0 = 0; m0 < Mmax; m0 += T) {
+            const int mm = max(0, min(T, M - m0));
+            int rb = 0, len = 0;
+            if (t < mm) {
+                const int I = A.mem[q0 + m0 + t];
+                s += A.b[I];
+                rb = A.rp[I];
+                len = A.rp[I + 1] - rb;
+            }
+            int off = team_scan(len, t, T);
+            const int tot = __shfl_sync(0xffffffffu, off, T - 1, T);
+            off -= len;
+            const int mw = __reduce_max_sync(0xffffffffu, mm);
+            const int totw = __reduce_max_sync(0xffffffffu, tot);
+            for (int b = 0; b < totw; b += T) {
+                const int e = b + t;
+                int who = 0;
+                for (int m = 1; m < mw; m++)
+                    if (e >= __shfl_sync(0xffffffffu, off, m, T)) who = m;
+                const int kb = __shfl_sync(0xffffffffu, rb, who, T), ko = __shfl_sync(0xffffffffu, off, who, T);
+                if (e < tot && J >= 0) {
+                    const int k = kb + (e - ko);
                     const int K = A.ci[k];
                     s -= A.va[k] * (kOmega * A.dinv[K] * A.b[K]);
                 }
