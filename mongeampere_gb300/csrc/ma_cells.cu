@@ -349,11 +349,22 @@ __device__ void process_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>&
     touched.clear();
     const int m = c.empty ? 0 : c.ns;
     if (!c.empty && P->n > 0) {
+        double4 bb = cell_box(*P, S, A);
+        // the neighbours by site index, whatever order the walk met them in: the pieces
+        // are clipped in slot order, so this keeps their sums independent of the seeds
+        for (int s = 1; s < m; s++) {
+            const Slot v = W.slots[s];
+            int r = s - 1;
+            while (r >= 0 && W.slots[r].site > v.site) {
+                W.slots[r + 1] = W.slots[r];
+                r--;
+            }
+            W.slots[r + 1] = v;
+        }
         for (int s = 0; s < m; s++) {
             W.nb[s] = make_nb64(A.sites[W.slots[s].site], o);
             W.hv[s] = 0.0;
         }
-        double4 bb = cell_box(*P, S, A);
         bool bad = false;
         M.visit(o, bb.x, bb.y, bb.z, bb.w, [&](const Fixed& T, double c0, double gx, double gy) {
             if (bad) return;
@@ -405,8 +416,19 @@ __global__ void __launch_bounds__(128) k_cells_stage1(CellArgs A)
         A.nb_cnt[k] = -1;
         return;
     }
+    // the neighbour list by site index (the seeds of the next evaluation set the
+    // order the walk meets them in; the pieces are clipped in list order, so a fixed
+    // order keeps their sums independent of the seeds)
     int* lab = A.nb_lab + (size_t)k * kCapSmall;
-    for (int s = 0; s < c.ns; s++) lab[s] = W.slots[s].site;
+    for (int s = 0; s < c.ns; s++) {
+        const int v = W.slots[s].site;
+        int r = s - 1;
+        while (r >= 0 && lab[r] > v) {
+            lab[r + 1] = lab[r];
+            r--;
+        }
+        lab[r + 1] = v;
+    }
     A.nb_cnt[k] = c.ns;
     A.cell_box[k] = cell_box(*P, S, A);
 }
@@ -690,7 +712,7 @@ __device__ __forceinline__ void vjp_piece(const CellArgs& A, const E& mesh, cons
 }
 
 template <int MODE, class E>
-__global__ void __launch_bounds__(32 * kPieceWarps) k_pieces(CellArgs A, E mesh)
+__global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E mesh)
 {
     constexpr bool MOM = MODE == kModeMoments, VJP = MODE == kModeVjp;
     constexpr bool LISTING = MODE == kModeCount || MODE == kModeEmit;

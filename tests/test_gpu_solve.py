@@ -206,3 +206,21 @@ def test_batch_matches_sequential_solves(ctx):
     ws2, stats2, used2 = api.ot_solve_batch(items, eps_g=1e-6, stop="rel", workers=0, ctx=ctx)
     assert used2 in (4, 8, 16, 32)
     assert all(s.status == 0 for s in stats2)
+
+
+def test_solve_is_reproducible(ctx):
+    # the same problem solved again -- after other solves, in a fresh context -- gives the
+    # same weights bit for bit and the same Newton path: line-search trials stopped at an
+    # empty cell leave seeds that vary with timing, and the neighbour lists are kept in
+    # site order so that nothing downstream depends on them
+    from mongeampere_gb300 import api
+    p = W.make_problem(256, 30000, "gauss", "uniform", "random", seed=5)
+    X = np.c_[p.x, p.y]
+    runs = []
+    for c in (ctx, ctx, api.Context(0)):
+        st = api.Statistics()
+        w = api.ot_solve(p.mesh, X, p.nu, eps_g=1e-6, stop="rel", stats=st, ctx=c)
+        runs.append((w, st.niter, st.neval, st.cg_iters))
+    for w, ni, ne, cg in runs[1:]:
+        np.testing.assert_array_equal(w, runs[0][0])
+        assert (ni, ne, cg) == runs[0][1:]
