@@ -231,6 +231,73 @@ def run_c3(args, ctx, dev, rank):
         print(json.dumps(out))
 
 
+def run_c4(args, ctx, dev, rank):
+    """The adjoint and the W2 flow at 200,000 sites on a 256^2 density (workloads.c4):
+    (a) vector-Jacobian products of (value, masses, first moments) against forward
+    evaluations, per second, with cotangents N(0, 1), and the adjoint's directional
+    derivative against a central difference of the GPU forward pass (h = 1e-6 along a
+    random direction of the sites and weights); (b) 50 steps of the W2 flow
+    x <- x + tau (x - centroid) with tau = -0.5 (half of Lloyd's step towards the
+    centroids), each a warm-started solve to max relative mass error 1e-6."""
+    import numpy as np
+    import torch
+
+    from mongeampere_gb300 import api
+    from mongeampere_gb300 import workloads as W
+    out = {"metric": METRIC, "workload": "c4", "n_gpus": 1}
+    p = W.c4(0)
+    dm = ctx.mesh(p.mesh)
+    X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
+    w = torch.zeros(p.n, dtype=torch.float64, device=dev)
+    rng = np.random.default_rng(4)
+    a = float(rng.normal())
+    b = torch.tensor(rng.normal(size=p.n), device=dev)
+    e = torch.tensor(rng.normal(size=(p.n, 2)), device=dev)
+
+    def rate(fn):
+        for _ in range(args.warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return args.steps / (e0.elapsed_time(e1) * 1e-3)
+
+    fwd = rate(lambda: api.kantorovich(dm, X, w, hessian=False, ctx=ctx))
+    vjp = rate(lambda: api.kantorovich_vjp(dm, X, w, a, b, e, ctx=ctx))
+    gX, gw, _ = api.kantorovich_vjp(dm, X, w, a, b, e, ctx=ctx)
+    vX = torch.tensor(rng.normal(size=(p.n, 2)) * 1e-3, device=dev)
+    vw = torch.tensor(rng.normal(size=p.n) * 1e-5, device=dev)
+
+    def f(t):
+        v, g, _ = api.kantorovich(dm, X + t * vX, w + t * vw, hessian=False, ctx=ctx)
+        _, first = api.first_moment(dm, X + t * vX, w + t * vw, ctx=ctx)
+        return a * v + float((b * g).sum()) + float((e * first).sum())
+
+    h = 1e-6
+    fd = (f(h) - f(-h)) / (2 * h)
+    ad = float((gX * vX).sum() + (gw * vw).sum())
+    out["adjoint"] = {"config": "200,000 uniform sites, 256^2 grid U[0.5,1.5], w = 0", "forward_evals_per_s": fwd,
+                      "vjp_per_s": vjp, "directional_derivative": ad, "central_difference": fd,
+                      "relative_difference": abs(ad - fd) / abs(fd)}
+    nu = torch.tensor(p.nu, device=dev)
+    st = api.Statistics()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    Xf, wf, st = api.w2_flow(dm, X, nu, steps=50, tau=-0.5, ctx=ctx)
+    e1.record()
+    torch.cuda.synchronize()
+    secs = e0.elapsed_time(e1) * 1e-3
+    out["w2_flow"] = {"config": "50 steps, tau = -0.5, each solve warm-started to max rel mass err 1e-6",
+                      "seconds": secs, "steps_per_s": 50 / secs, "newton_iters": st.niter, "evals": st.neval}
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def run_c5(args, ctx, dev, rank):
     """512 independent problems (workloads.c5: grid side log-uniform in [32, 512], values
     U[0.5, 1.5], 500 .. 50,000 uniform sites, equal masses) solved to max relative mass
@@ -293,7 +360,7 @@ def main():
                          "solution weights and print per-kernel device times (no benchmark line)")
     ap.add_argument("--profile-solve", action="store_true",
                     help="profiling driver: one solve with per-kernel device times (no benchmark line)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
                     help="c3: the 1M-site mixed-precision comparison (evaluations of the clustered "
                          "1M-site / 2048^2 workload, and a 1M-uniform-site solve); c5: 512 independent "
                          "problems, batched against sequential solves; one JSON line each")
@@ -325,6 +392,9 @@ def main():
     ctx.use_torch_stream()
     if args.workload == "c3":
         run_c3(args, ctx, dev, rank)
+        return
+    if args.workload == "c4":
+        run_c4(args, ctx, dev, rank)
         return
     if args.workload == "c5":
         run_c5(args, ctx, dev, rank)

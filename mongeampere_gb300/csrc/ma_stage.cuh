@@ -228,11 +228,15 @@ __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Ow
             if (!is_seed(q) && !visit(q)) r.empty = true;
             continue;
         }
-        int2 rg = T.range[nd];
+        // everything the node may need, loaded at once (one round trip, not three)
+        const int2 rg = T.range[nd];
+        const int2 ch = T.child[nd];
+        const float4 nbf = T.boxf[nd];
+        const float4 nnk = T.nk[nd];
         bool contains = rg.x <= k && k <= rg.y;
         if (!contains) {
             r.tested++;
-            if (node_harmless(*P, ox, oy, owh, oxa, T.boxf[nd], T.nk[nd])) {
+            if (node_harmless(*P, ox, oy, owh, oxa, nbf, nnk)) {
                 r.pruned++;
                 continue;
             }
@@ -242,7 +246,6 @@ __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Ow
                 if (!is_seed(q) && !visit(q)) r.empty = true;
             continue;
         }
-        int2 ch = T.child[nd];
         if (sp > kStack - 2) {
             r.overflow = true;
             break;
