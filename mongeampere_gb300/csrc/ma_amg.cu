@@ -626,7 +626,7 @@ __device__ __forceinline__ int team_scan(int v, int t, int T)
 }
 
 // Loop over rows [0, nrows) with teams of T lanes: calls fn(row, lane_in_team)
-// with row < nrows, or row = -1 for lanes without a row in this round (they still
+// with row < nrows, or row = -1 for lanes without a row in this pass (they still
 // take part in the team's shuffles).  Warp-uniform trip count.
 template <class Fn>
 __device__ __forceinline__ void team_rows(int nrows, int T, Fn&& fn)

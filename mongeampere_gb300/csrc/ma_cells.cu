@@ -7,16 +7,19 @@
 // produced cell by cell in two kernels:
 //
 //   stage 1, k_cells_stage1 (one thread per site): branch and bound over the site
-//     tree; Sutherland-Hodgman clips of the mesh's bounding box give the cell and
-//     its neighbour list, written out with the cell's bounding box;
-//   stage 2, k_pieces (a warp per eight consecutive cells): the lanes clip the
-//     mesh triangles under the cells' boxes by the cells' neighbours into a list of
-//     pieces in shared memory, then integrate the listed pieces one per lane in
-//     FP64, and the per-cell sums (in list order, so results are reproducible)
-//     give the mass, the value part and the Hessian row.
+//     tree (the walk and the node test are in ma_stage.cuh); Sutherland-Hodgman
+//     clips of the mesh's bounding box give the cell and its neighbour list, written
+//     out in site order with the cell's bounding box;
+//   stage 2, k_pieces (a warp per eight consecutive cells): certified corner tests
+//     sort the mesh triangles under the cells' boxes into outside, inside and
+//     crossed; the crossed ones are clipped by the half-warps, a vertex per lane; the
+//     pieces are listed in shared memory, integrated one per lane in FP64, and the
+//     per-cell sums (in a fixed order, so results are reproducible) give the mass,
+//     the value part and the Hessian row.
 //
 // Cells that outgrow the 48 slots of stage 1, or whose pieces need exact arithmetic
-// or more than 12 vertices, are redone end to end by k_cells_large, one thread per cell with a 256-slot workspace in global scratch.
+// or more than 12 vertices, are redone end to end by k_cells_large, one thread per
+// cell with a 256-slot workspace in global scratch.
 #include <climits>
 
 #include "ma_internal.h"
