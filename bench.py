@@ -504,7 +504,9 @@ def main():
     achieved = bytes_eval / (pieces_ms * 1e-3) / 1e9
     # DRAM bytes (read + write) of one k_pieces launch from the ncu capture summarised
     # in profiles/k_pieces_c2_full.md, for this workload
+    # and the kernel's binding resource from the same capture: the FP64 pipe
     traffic = None
+    fp64_pct = None
     tfile = os.path.join(ROOT, "profiles", "traffic.txt")
     if os.path.exists(tfile):
         with open(tfile) as fh:
@@ -512,12 +514,17 @@ def main():
                 f = ln.split()
                 if len(f) == 2 and f[0] == "k_pieces_c2_dram_bytes_per_launch":
                     traffic = float(f[1])
+                if len(f) == 2 and f[0] == "k_pieces_c2_fp64_pipe_pct_active":
+                    fp64_pct = float(f[1])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic,
                 "kernel": "k_pieces (triangle clipping + FP64 integrals + Hessian rows of one evaluation)",
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_eval,
                 "avg_launch_ms": pieces_ms,
-                "other_eval_kernels_ms": {"k_cells_stage1": stage1_ms, "k_tree_bounds": bounds_ms}}
+                "other_eval_kernels_ms": {"k_cells_stage1": stage1_ms, "k_tree_bounds": bounds_ms},
+                "binding": {"resource": "FP64 pipe (GB300: ~2 FP64 FMA lanes per clock per SM)",
+                            "pct_of_peak_active": fp64_pct,
+                            "source": "ncu sm__pipe_fp64_cycles_active, profiles/k_pieces_c2_full.md"}}
 
     # ---- e2e through the C ABI with host buffers ----
     xh = torch.tensor(p.x).pin_memory().numpy()
