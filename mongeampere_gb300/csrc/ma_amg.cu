@@ -577,6 +577,7 @@ struct AmgPcgArgs {
     double* z;
     double* p;
     double* q;
+    double* ys;    // the fine level's pre-smoothed plus prolonged correction (levels >= 3)
     double* part;  // 3 * gridDim.x partial sums
     double* out;   // [iterations, |r|, |b|]
     double rtol;
@@ -746,11 +747,17 @@ __device__ __forceinline__ void prolong_level(const AmgPcgArgs& a, int l, double
                                                 : 0.0;
                     s -= A.va[k] * yK;
                 }
-                if (t == 0) yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, A.agg[I], xc);
+                yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, A.agg[I], xc);
             }
         }
         s = team_sum(s, T);
-        if (I >= 0 && t == 0) A.xp[I] = dI != 0.0 ? yI + kOmega * dI * (A.b[I] + s) : 0.0;
+        const double xI = dI != 0.0 ? yI + kOmega * dI * (A.b[I] + s) : 0.0;
+        if (I >= 0 && t == 0) A.xp[I] = xI;
+        if (l == 1 && I >= 0) {
+            // the fine rows of aggregate I take their share of the correction now
+            const AmgLevelDev& F = a.L[0];
+            for (int q = F.mp[I] + t; q < F.mp[I + 1]; q += T) a.ys[F.mem[q]] += kCoarseScale * xI;
+        }
     });
 }
 
@@ -803,6 +810,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                 l_rr += rk * rk;
                 const double dk = F.dinv[k];
                 double s = 0.0;
+                if (!jacobi) a.ys[k] = dk != 0.0 ? kOmega * dk * rk : 0.0;
                 if (!jacobi && dk != 0.0) {
                     s = rk;
                     const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
@@ -849,26 +857,44 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                 grid.sync();
             }
             if (a.nlev == 2) coarsest_solve(a, xc, sinv, sb);
-            for (int k = tid; k < n; k += stride) {
-                const double dk = F.dinv[k];
-                double zk = 0.0;
-                if (dk != 0.0) {
-                    const double yk = kOmega * dk * rc[k] + kCoarseScale * coarse_corr(a, 0, F.agg[k], xc);
-                    double s = rc[k];
-                    const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
+            if (a.nlev > 2) {
+                // y, complete since the level-1 prolongation: one gather per entry
+                for (int k = tid; k < n; k += stride) {
+                    const double dk = F.dinv[k];
+                    double zk = 0.0;
+                    if (dk != 0.0) {
+                        double s = rc[k];
+                        const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
 #pragma unroll 4
-                    for (int e = 0; e < w; e++) {
-                        const int j = F.eci[b0 + 32 * e];
-                        const double dj = F.dinv[j];
-                        const double yj =
-                            dj != 0.0 ? kOmega * dj * rc[j] + kCoarseScale * coarse_corr(a, 0, F.agg[j], xc)
-                                      : 0.0;
-                        s -= F.eva[b0 + 32 * e] * yj;
+                        for (int e = 0; e < w; e++) s -= F.eva[b0 + 32 * e] * a.ys[F.eci[b0 + 32 * e]];
+                        zk = a.ys[k] + kOmega * dk * s;
                     }
-                    zk = yk + kOmega * dk * s;
+                    a.z[k] = zk;
+                    l_rz += zk * rc[k];
                 }
-                a.z[k] = zk;
-                l_rz += zk * rc[k];
+            } else {
+                // two levels: the coarsest correction straight from xc
+                for (int k = tid; k < n; k += stride) {
+                    const double dk = F.dinv[k];
+                    double zk = 0.0;
+                    if (dk != 0.0) {
+                        const double yk = kOmega * dk * rc[k] + kCoarseScale * coarse_corr(a, 0, F.agg[k], xc);
+                        double s = rc[k];
+                        const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
+#pragma unroll 4
+                        for (int e = 0; e < w; e++) {
+                            const int j = F.eci[b0 + 32 * e];
+                            const double dj = F.dinv[j];
+                            const double yj =
+                                dj != 0.0 ? kOmega * dj * rc[j] + kCoarseScale * coarse_corr(a, 0, F.agg[j], xc)
+                                          : 0.0;
+                            s -= F.eva[b0 + 32 * e] * yj;
+                        }
+                        zk = yk + kOmega * dk * s;
+                    }
+                    a.z[k] = zk;
+                    l_rz += zk * rc[k];
+                }
             }
         }
         {
@@ -1111,6 +1137,8 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     a.z = c->cg_z.as<double>();
     a.p = c->cg_p.as<double>();
     a.q = c->cg_q.as<double>();
+    MA_CUDA(c, G.ys.ensure(sizeof(double) * n));
+    a.ys = G.ys.as<double>();
     a.part = c->cg_part.as<double>();
     a.out = c->cg_scal.as<double>();
     a.rtol = rtol;

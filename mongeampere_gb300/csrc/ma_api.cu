@@ -505,7 +505,7 @@ void ma_ctx_destroy(ma_ctx* c)
         DevBuf* lb[] = {&l.rp, &l.ci, &l.va, &l.dinv, &l.b, &l.xp, &l.agg, &l.mp, &l.mem};
         for (DevBuf* b : lb) b->release();
     }
-    DevBuf* ab[] = {&c->amg.r1, &c->amg.xs, &c->amg.inv, &c->amg.cnt, &c->amg.rp0, &c->amg.ci0, &c->amg.va0, &c->amg.sp, &c->amg.eci, &c->amg.eva,
+    DevBuf* ab[] = {&c->amg.ys, &c->amg.r1, &c->amg.xs, &c->amg.inv, &c->amg.cnt, &c->amg.rp0, &c->amg.ci0, &c->amg.va0, &c->amg.sp, &c->amg.eci, &c->amg.eva,
                     &c->amg.flag, &c->amg.cinv, &c->amg.mate, &c->amg.best, &c->amg.claim, &c->amg.mflag,
                     &c->amg.mid, &c->amg.join, &c->amg.agg1, &c->amg.agg2, &c->amg.mp1, &c->amg.mem1,
                     &c->amg.mfill, &c->amg.rp1, &c->amg.ci1, &c->amg.va1, &c->amg.dinv1, &c->amg.part,

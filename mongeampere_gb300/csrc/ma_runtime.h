@@ -69,7 +69,7 @@ struct AmgBuf {
 };
 struct Amg {
     AmgBuf lev[16];
-    DevBuf r1, xs, inv, cnt, rp0, ci0, va0, sp, eci, eva, flag, cinv;
+    DevBuf r1, xs, inv, cnt, rp0, ci0, va0, sp, eci, eva, flag, cinv, ys;
     // aggregation scratch: the matching state, the first pass's aggregates and
     // their Galerkin matrix
     DevBuf mate, best, claim, mflag, mid, join, agg1, agg2, mp1, mem1, mfill, rp1, ci1, va1, dinv1, part, counts;
