@@ -550,6 +550,7 @@ struct AmgLevelDev {
     const double* dinv;
     double* b;   // restricted residual
     double* xp;  // post-smoothed correction
+    double* y;   // pre-smoothed plus prolonged correction (levels 1 .. nlev-3)
     int tr;      // team size restricting this level into the next
     int tp;      // team size prolonging into this level
     const int* agg;  // row -> node of the next level (-1: inactive)
@@ -685,7 +686,10 @@ __device__ __forceinline__ void restrict_level(const AmgPcgArgs& a, int l)
             }
         }
         s = team_sum(s, T);
-        if (J >= 0 && t == 0) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
+        if (J >= 0 && t == 0) {
+            C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
+            if (C.y) C.y[J] = C.dinv[J] != 0.0 ? kOmega * C.dinv[J] * s : 0.0;
+        }
     });
 }
 
@@ -701,7 +705,10 @@ __device__ __forceinline__ void restrict_fine(const AmgPcgArgs& a, const double*
         if (J >= 0)
             for (int q = F.mp[J] + t; q < F.mp[J + 1]; q += T) s += s_fine[F.mem[q]];
         s = team_sum(s, T);
-        if (J >= 0 && t == 0) C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
+        if (J >= 0 && t == 0) {
+            C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
+            if (C.y) C.y[J] = C.dinv[J] != 0.0 ? kOmega * C.dinv[J] * s : 0.0;
+        }
     });
 }
 
@@ -740,23 +747,30 @@ __device__ __forceinline__ void prolong_level(const AmgPcgArgs& a, int l, double
         if (I >= 0) {
             dI = A.dinv[I];
             if (dI != 0.0) {
-                for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) {
-                    const int K = A.ci[k];
-                    const double dK = A.dinv[K];
-                    const double yK = dK != 0.0 ? kOmega * dK * A.b[K] + kCoarseScale * coarse_corr(a, l, A.agg[K], xc)
-                                                : 0.0;
-                    s -= A.va[k] * yK;
+                if (A.y) {
+                    // y complete since the prolongation of level l + 1: one gather
+                    for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) s -= A.va[k] * A.y[A.ci[k]];
+                    yI = A.y[I];
+                } else {
+                    for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) {
+                        const int K = A.ci[k];
+                        const double dK = A.dinv[K];
+                        const double yK =
+                            dK != 0.0 ? kOmega * dK * A.b[K] + kCoarseScale * coarse_corr(a, l, A.agg[K], xc) : 0.0;
+                        s -= A.va[k] * yK;
+                    }
+                    yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, A.agg[I], xc);
                 }
-                yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, A.agg[I], xc);
             }
         }
         s = team_sum(s, T);
         const double xI = dI != 0.0 ? yI + kOmega * dI * (A.b[I] + s) : 0.0;
         if (I >= 0 && t == 0) A.xp[I] = xI;
-        if (l == 1 && I >= 0) {
-            // the fine rows of aggregate I take their share of the correction now
-            const AmgLevelDev& F = a.L[0];
-            for (int q = F.mp[I] + t; q < F.mp[I + 1]; q += T) a.ys[F.mem[q]] += kCoarseScale * xI;
+        if (I >= 0) {
+            // the rows of aggregate I one level down take their share of the correction now
+            const AmgLevelDev& D = a.L[l - 1];
+            double* yd = l == 1 ? a.ys : D.y;
+            for (int q = D.mp[I] + t; q < D.mp[I + 1]; q += T) yd[D.mem[q]] += kCoarseScale * xI;
         }
     });
 }
@@ -1005,8 +1019,9 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
 
     AmgPcgArgs a{};
     a.L[0] = AmgLevelDev{n,       G.rp0.as<int>(), G.ci0.as<int>(), G.va0.as<double>(), c->cg_dinv.as<double>(),
-                         nullptr, nullptr,         1,               1,                 nullptr,
-                         nullptr, nullptr,         G.sp.as<int>(),  G.eci.as<int>(),   G.eva.as<double>()};
+                         nullptr, nullptr,         nullptr,         1,                 1,
+                         nullptr, nullptr,         nullptr,         G.sp.as<int>(),    G.eci.as<int>(),
+                         G.eva.as<double>()};
     // the level setup's cooperative grid: co-resident blocks, at most one row per thread
     int setup_max = 0, sms = 0;
     {
@@ -1078,7 +1093,7 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         A.mp = B.mp.as<int>();
         A.mem = B.mem.as<int>();
         a.L[l + 1] = AmgLevelDev{nc,      Cb.rp.as<int>(), Cb.ci.as<int>(), Cb.va.as<double>(), Cb.dinv.as<double>(),
-                                 Cb.b.as<double>(), Cb.xp.as<double>(), 1, 1, nullptr, nullptr, nullptr,
+                                 Cb.b.as<double>(), Cb.xp.as<double>(), nullptr, 1, 1, nullptr, nullptr, nullptr,
                                  nullptr, nullptr, nullptr};
         nlev++;
     }
@@ -1087,6 +1102,10 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         return fail(c, MA_ERR_CAPACITY, "multigrid coarsest level too large");
     }
     a.nlev = nlev;
+    for (int l = 1; l + 3 <= nlev; l++) {  // levels whose corrections are materialised
+        MA_CUDA(c, G.lev[l].y.ensure(sizeof(double) * (size_t)a.L[l].n));
+        a.L[l].y = G.lev[l].y.as<double>();
+    }
     if (!keep) {
         G.agg_epoch = c->index_epoch;
         G.agg_nlev = nlev;

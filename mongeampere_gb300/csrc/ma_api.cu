@@ -502,7 +502,7 @@ void ma_ctx_destroy(ma_ctx* c)
                       &c->ms_x, &c->ms_y, &c->ms_nu, &c->ms_w, &c->tune_w};
     for (DevBuf* b : bufs) b->release();
     for (AmgBuf& l : c->amg.lev) {
-        DevBuf* lb[] = {&l.rp, &l.ci, &l.va, &l.dinv, &l.b, &l.xp, &l.agg, &l.mp, &l.mem};
+        DevBuf* lb[] = {&l.rp, &l.ci, &l.va, &l.dinv, &l.b, &l.xp, &l.y, &l.agg, &l.mp, &l.mem};
         for (DevBuf* b : lb) b->release();
     }
     DevBuf* ab[] = {&c->amg.ys, &c->amg.r1, &c->amg.xs, &c->amg.inv, &c->amg.cnt, &c->amg.rp0, &c->amg.ci0, &c->amg.va0, &c->amg.sp, &c->amg.eci, &c->amg.eva,

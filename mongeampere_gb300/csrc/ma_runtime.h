@@ -64,7 +64,7 @@ struct Mesh {
 
 // aggregation multigrid hierarchy (levels 1.. of the Newton system)
 struct AmgBuf {
-    DevBuf rp, ci, va, dinv, b, xp;  // the level's matrix (levels >= 1) and work vectors
+    DevBuf rp, ci, va, dinv, b, xp, y;  // the level's matrix (levels >= 1) and work vectors
     DevBuf agg, mp, mem;             // its aggregates: row -> node of the next level, member lists
 };
 struct Amg {
