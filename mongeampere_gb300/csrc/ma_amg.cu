@@ -1079,7 +1079,11 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         sa.overflow = G.flag.as<int>();
         sa.reuse = keep ? 1 : 0;
         sa.nc = keep ? G.agg_n[l + 1] : 0;
-        const int nbs = std::max(1, std::min(setup_max, (A.n + kSetupThreads - 1) / kSetupThreads));
+        // a thread per row for the matching; when only the Galerkin matrix is rebuilt, a
+        // warp per coarse row instead (its grid has four barriers, not ~50)
+        const int rows_blocks = (A.n + kSetupThreads - 1) / kSetupThreads;
+        const int gal_blocks = keep ? (G.agg_n[l + 1] + kRowWarps - 1) / kRowWarps : 0;
+        const int nbs = std::max(1, std::min(setup_max, std::max(rows_blocks, gal_blocks)));
         void* sargs[] = {&sa};
         MA_CUDA(c, cudaLaunchCooperativeKernel((void*)k_level_setup, dim3(nbs), dim3(kSetupThreads), sargs, 0, s));
         c->launches += 1;
