@@ -389,7 +389,7 @@ __device__ void process_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>&
 // ---------------------------------------------------------------------------
 constexpr int kCapLarge = 256;
 
-__global__ void __launch_bounds__(128) k_cells_stage1(CellArgs A)
+__global__ void __launch_bounds__(128, 6) k_cells_stage1(CellArgs A)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= A.n) return;

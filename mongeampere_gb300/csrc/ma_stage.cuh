@@ -216,48 +216,58 @@ __device__ CellOut cell_stage(const CellArgs& A, int k, const SiteD& S, const Ow
         for (int s = 0; s < nseed && !r.empty && !r.overflow; s++)
             if (!visit(seeds[s])) r.empty = true;
     }
-    while (sp > 0 && !r.empty && !r.overflow) {
-        if (A.abort_flag && (r.popped & 7) == 0 && *(volatile const int*)A.abort_flag) {
-            r.aborted = true;
-            break;
-        }
-        int nd = stack[--sp];
-        r.popped++;
-        if (nd < 0) {
-            int q = nd & 0x7fffffff;
-            if (!is_seed(q) && !visit(q)) r.empty = true;
-            continue;
-        }
-        // everything the node may need, loaded at once (one round trip, not three)
-        const int2 rg = T.range[nd];
-        const int2 ch = T.child[nd];
-        const float4 nbf = T.boxf[nd];
-        const float4 nnk = T.nk[nd];
-        bool contains = rg.x <= k && k <= rg.y;
-        if (!contains) {
-            r.tested++;
-            if (node_harmless(*P, ox, oy, owh, oxa, nbf, nnk)) {
-                r.pruned++;
-                continue;
+    // Two phases per round, so that the lanes of a warp clip together: every lane
+    // walks until it reaches sites to clip against (a leaf or a small node: the range
+    // [vlo, vhi]) or its stack runs out, and the lanes that found sites then clip
+    // against them side by side.  Sites are met in the same depth-first order as in a
+    // single loop, so the cell and its slots do not depend on the phases.
+    for (;;) {
+        int vlo = 0, vhi = -1;
+        while (sp > 0 && !r.empty && !r.overflow) {
+            if (A.abort_flag && (r.popped & 7) == 0 && *(volatile const int*)A.abort_flag) {
+                r.aborted = true;
+                break;
+            }
+            int nd = stack[--sp];
+            r.popped++;
+            if (nd < 0) {
+                vlo = vhi = nd & 0x7fffffff;
+                break;
+            }
+            // everything the node may need, loaded at once (one round trip, not three)
+            const int2 rg = T.range[nd];
+            const int2 ch = T.child[nd];
+            const float4 nbf = T.boxf[nd];
+            const float4 nnk = T.nk[nd];
+            bool contains = rg.x <= k && k <= rg.y;
+            if (!contains) {
+                r.tested++;
+                if (node_harmless(*P, ox, oy, owh, oxa, nbf, nnk)) {
+                    r.pruned++;
+                    continue;
+                }
+            }
+            if (rg.y - rg.x < kBucket) {
+                vlo = rg.x;
+                vhi = rg.y;
+                break;
+            }
+            if (sp > kStack - 2) {
+                r.overflow = true;
+                break;
+            }
+            // nearer child on top
+            if (dist2(ch.x) <= dist2(ch.y)) {
+                stack[sp++] = ch.y;
+                stack[sp++] = ch.x;
+            } else {
+                stack[sp++] = ch.x;
+                stack[sp++] = ch.y;
             }
         }
-        if (rg.y - rg.x < kBucket) {
-            for (int q = rg.x; q <= rg.y && !r.empty && !r.overflow; q++)
-                if (!is_seed(q) && !visit(q)) r.empty = true;
-            continue;
-        }
-        if (sp > kStack - 2) {
-            r.overflow = true;
-            break;
-        }
-        // nearer child on top
-        if (dist2(ch.x) <= dist2(ch.y)) {
-            stack[sp++] = ch.y;
-            stack[sp++] = ch.x;
-        } else {
-            stack[sp++] = ch.x;
-            stack[sp++] = ch.y;
-        }
+        if (vlo > vhi || r.aborted) break;
+        for (int q = vlo; q <= vhi && !r.empty && !r.overflow; q++)
+            if (!is_seed(q) && !visit(q)) r.empty = true;
     }
     if (r.empty) {
         P->n = 0;
