@@ -1008,7 +1008,7 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     {
         int total = 0;
         MA_CUDA(c, cudaMemcpyAsync(&total, G.sp.as<int>() + nslice, sizeof(int), cudaMemcpyDeviceToHost, s));
-        MA_CUDA(c, cudaStreamSynchronize(s));
+        MA_CUDA(c, ctx_sync(c));
         if ((size_t)total > ell_cap) ell_cap = (size_t)total;
     }
     MA_CUDA(c, G.eci.ensure(sizeof(int) * ell_cap));
@@ -1090,7 +1090,7 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         int nc = sa.nc;
         if (!keep) {  // the next level's size decides the next iteration
             MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 7, G.counts.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
-            MA_CUDA(c, cudaStreamSynchronize(s));
+            MA_CUDA(c, ctx_sync(c));
             nc = c->hinfo[7];
         }
         A.agg = B.agg.as<int>();
@@ -1175,7 +1175,7 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     c->launches += 1;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat + 8, c->cg_scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 6, G.flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MA_CUDA(c, cudaStreamSynchronize(s));
+    MA_CUDA(c, ctx_sync(c));
     if (iters) *iters = (int)c->hstat[8];
     c->profile.pcg_iters += (int64_t)c->hstat[8];
     if (c->hinfo[6]) c->profile.amg_fallbacks++;

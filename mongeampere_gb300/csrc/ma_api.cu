@@ -84,7 +84,7 @@ ma_status build_site_index_box(Ctx* c, double X0, double Y0, double X1, double Y
     launch_key_to_double(c->keys.as<unsigned long long>(), c->bboxd.as<double>(), 4, s);
     c->launches += 2;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->bboxd.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    MA_CUDA(c, cudaStreamSynchronize(s));
+    MA_CUDA(c, ctx_sync(c));
     double xmin = c->hstat[0], xmax = c->hstat[1], ymin = c->hstat[2], ymax = c->hstat[3];
     if (!(std::isfinite(xmin) && std::isfinite(xmax) && std::isfinite(ymin) && std::isfinite(ymax)))
         return fail(c, MA_ERR_INVALID_ARGUMENT, "non-finite site coordinates");
@@ -296,7 +296,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     c->hinfo[3] = 0;
     if (a.abort_flag)
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 3, a.abort_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MA_CUDA(c, cudaStreamSynchronize(s));
+    MA_CUDA(c, ctx_sync(c));
     if (c->hinfo[3]) {
         // a line-search trial with an empty cell: nothing else is computed
         c->aborted = true;
@@ -317,7 +317,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         launch_scan(c->pv_cnt.as<int>(), c->pv_base.as<int>(), n, c->scan_scratch.as<int>(), s);
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 4, c->pc_base.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 5, c->pv_base.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
-        MA_CUDA(c, cudaStreamSynchronize(s));
+        MA_CUDA(c, ctx_sync(c));
         const int64_t np = c->hinfo[4], nv = c->hinfo[5];
         MA_CUDA(c, c->pc_site.ensure(sizeof(int) * (size_t)(np + 1)));
         MA_CUDA(c, c->pc_tri.ensure(sizeof(int) * (size_t)(np + 1)));
@@ -337,7 +337,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
             launch_pieces_tri(a, m->tri_dev(), 4, s);
         c->launches += 5;
         MA_CUDA(c, cudaMemcpyAsync(c->pc_off.as<int64_t>() + np, &nv, sizeof(int64_t), cudaMemcpyHostToDevice, s));
-        MA_CUDA(c, cudaStreamSynchronize(s));
+        MA_CUDA(c, ctx_sync(c));
         c->npieces = np;
         c->npverts = nv;
         c->have_pieces = true;
@@ -374,7 +374,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         c->profile.large_sites += nredo;
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        MA_CUDA(c, cudaStreamSynchronize(s));
+        MA_CUDA(c, ctx_sync(c));
         if (c->hinfo[0] > 0)
             return fail(c, MA_ERR_CAPACITY, "a Laguerre cell has more vertices than the largest kernel capacity");
     }
@@ -394,7 +394,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         launch_scan(c->rowcnt.as<int>(), c->rowptr.as<int>(), n, c->scan_scratch.as<int>(), s);
         c->launches += 2;
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 2, c->rowptr.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
-        MA_CUDA(c, cudaStreamSynchronize(s));
+        MA_CUDA(c, ctx_sync(c));
         int64_t nnz = c->hinfo[2];
         MA_CUDA(c, c->col.ensure(sizeof(int) * (size_t)(nnz + 1)));
         MA_CUDA(c, c->val.ensure(sizeof(double) * (size_t)(nnz + 1)));
@@ -511,6 +511,7 @@ void ma_ctx_destroy(ma_ctx* c)
                     &c->amg.mfill, &c->amg.rp1, &c->amg.ci1, &c->amg.va1, &c->amg.dinv1, &c->amg.part,
                     &c->amg.counts};
     for (DevBuf* b : ab) b->release();
+    if (c->sync_event) cudaEventDestroy(c->sync_event);
     if (c->pev[0]) cudaEventDestroy(c->pev[0]);
     if (c->pev[1]) cudaEventDestroy(c->pev[1]);
     if (c->hstat) cudaFreeHost(c->hstat);

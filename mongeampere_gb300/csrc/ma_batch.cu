@@ -14,7 +14,7 @@
 // K is autotuned when the caller passes 0 and the context has no earlier choice: the
 // batch's median-sized problem is solved once on every candidate worker (their
 // buffers reach that size), then K copies of it are solved concurrently for each
-// candidate K = 4, 8, 16, 32, and the K with the most problems per second is kept in
+// candidate K = 4, 8, 16, 32, 64, and the K with the most problems per second is kept in
 // the context.  The batch then runs largest problem first: every worker's buffers
 // reach their size early (device allocations synchronise the whole GPU), and the
 // longest solves do not end up last.
@@ -38,7 +38,10 @@ static ma_status ensure_workers(Ctx* c, int k)
         c->workers.push_back(w);
     }
     // k problems share the GPU: each cooperative solve takes 1 / k of it
-    for (int t = 0; t < k; t++) c->workers[(size_t)t]->grid_share = k;
+    for (int t = 0; t < k; t++) {
+        c->workers[(size_t)t]->grid_share = k;
+        c->workers[(size_t)t]->blocking_sync = true;
+    }
     return MA_OK;
 }
 
@@ -106,8 +109,8 @@ static ma_status solve_copies(Ctx* c, const ma_problem& p, ma_mem mem, const ma_
 
 static ma_status autotune(Ctx* c, const ma_problem* pb, int64_t count, ma_mem mem, const ma_solve_opts* o, int* best)
 {
-    const int cand[] = {4, 8, 16, 32};
-    const int kmax = 32;
+    const int cand[] = {4, 8, 16, 32, 64};
+    const int kmax = 64;
     std::vector<int64_t> idx((size_t)count);
     for (int64_t i = 0; i < count; i++) idx[(size_t)i] = i;
     std::nth_element(idx.begin(), idx.begin() + count / 2, idx.end(),

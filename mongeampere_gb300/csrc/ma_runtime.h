@@ -123,6 +123,10 @@ struct Ctx {
     std::vector<ma_ctx*> workers;
     int batch_workers = 0;
     int grid_share = 1;  // a batch worker's cooperative grids use 1 / grid_share of the GPU
+    // a batch worker waits for its stream asleep (an event with cudaEventBlockingSync)
+    // rather than spinning, so that more workers than host cores can share the cores
+    bool blocking_sync = false;
+    cudaEvent_t sync_event = nullptr;
     DevBuf tune_w;                // weight copies of the batch autotuner (device callers)
     std::vector<double> tune_wh;  //                                       (host callers)
     Amg amg;
@@ -134,6 +138,20 @@ struct Ctx {
     double* hstat = nullptr;  // 16 doubles
     int* hinfo = nullptr;     // 8 ints
 };
+
+// wait for the context's stream: cudaStreamSynchronize, or asleep on an event for a
+// context with blocking_sync
+inline cudaError_t ctx_sync(Ctx* c)
+{
+    if (!c->blocking_sync) return cudaStreamSynchronize(c->stream);
+    if (!c->sync_event) {
+        cudaError_t e = cudaEventCreateWithFlags(&c->sync_event, cudaEventBlockingSync | cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaEventRecord(c->sync_event, c->stream);
+    if (e != cudaSuccess) return e;
+    return cudaEventSynchronize(c->sync_event);
+}
 
 // error helpers
 ma_status fail(Ctx* c, ma_status s, const std::string& msg);

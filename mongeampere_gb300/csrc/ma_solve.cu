@@ -249,7 +249,7 @@ static ma_status pcg_solve(Ctx* c, int n, const double* b, double* x, double rto
     }
     c->launches += 2;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat + 8, c->cg_scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    MA_CUDA(c, cudaStreamSynchronize(s));
+    MA_CUDA(c, ctx_sync(c));
     if (iters) *iters = (int)c->hstat[8];
     c->profile.pcg_iters += (int64_t)c->hstat[8];
     if (relres) *relres = c->hstat[10] > 0 ? c->hstat[9] / c->hstat[10] : 0.0;
@@ -360,7 +360,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
         } else {
             MA_CUDA(c, cudaMemcpyAsync(c->hstat, c->stat_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
         }
-        MA_CUDA(c, cudaStreamSynchronize(s));
+        MA_CUDA(c, ctx_sync(c));
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         S.t_eval_ms += ms;
@@ -560,7 +560,7 @@ static ma_status multiscale_solve(Ctx* c, const Mesh* m, int n, const double* dx
     MA_CUDA(c, cudaMemcpyAsync(L[0].x.data(), dx, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(L[0].y.data(), dy, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(L[0].nu.data(), dnu, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-    MA_CUDA(c, cudaStreamSynchronize(s));
+    MA_CUDA(c, ctx_sync(c));
     while ((int)L.back().x.size() > kMsCoarse) {
         MsLevel& f = L.back();
         const size_t nf = f.x.size();
@@ -618,7 +618,7 @@ static ma_status multiscale_solve(Ctx* c, const Mesh* m, int n, const double* dx
         for (int tries = 0;; tries++) {
             for (int i = 0; i < nl; i++) wt[i] = t * wl[i];
             MA_CUDA(c, cudaMemcpyAsync(lw, wt.data(), sizeof(double) * nl, cudaMemcpyHostToDevice, s));
-            MA_CUDA(c, cudaStreamSynchronize(s));
+            MA_CUDA(c, ctx_sync(c));
             if (t == 0.0) break;
             ma_status st = build_site_index(c, m, nl, lx, ly, lw);
             if (st != MA_OK) return st;
@@ -661,7 +661,7 @@ static ma_status multiscale_solve(Ctx* c, const Mesh* m, int n, const double* dx
         }
         MA_CUDA(c, cudaMemcpyAsync(wc.data(), lw, sizeof(double) * nl, cudaMemcpyDeviceToHost, s));
         MA_CUDA(c, cudaMemcpyAsync(mo.data(), c->mom.p, sizeof(double) * 6 * nl, cudaMemcpyDeviceToHost, s));
-        MA_CUDA(c, cudaStreamSynchronize(s));
+        MA_CUDA(c, ctx_sync(c));
         const MsLevel& F = L[l - 1];
         const MsLevel& Cl = L[l];
         const std::vector<int>& par = F.parent;
@@ -817,7 +817,7 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     if (result == MA_OK || result == MA_MAXITER || result == MA_LINESEARCH_FAIL) {
         cudaMemcpyAsync(w_inout, w, sizeof(double) * n,
                         mem == MA_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s);
-        cudaStreamSynchronize(s);
+        ctx_sync(c);
     }
     if (stats) *stats = S;
     return result;
