@@ -112,6 +112,22 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(t, dist, device="cpu"):
+    """The slowest rank's time: every rank solves its own problem (weak scaling, no
+    exchange between ranks), so the job takes as long as its slowest rank."""
+    if dist is None:
+        return t
+    import torch
+    tt = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_rate(steps, world, t):
+    """Whole-job throughput: each of the `world` ranks completed `steps` solves in t."""
+    return steps * world / t
+
+
 def cpu_sample(problem, threads=None):
     """One Laguerre evaluation in the reference's FP64 arithmetic + one sparse LU
     Newton solve, on the host cores (the oracle)."""
@@ -462,11 +478,8 @@ def main():
     launches = ctx.launch_count - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_dev = sum(step_ms) / 1e3
-    if dist:
-        tt = torch.tensor([t_dev], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
-    value = args.steps * world / t_dev
+    t_dev = max_over_ranks(t_dev, dist, dev)
+    value = job_rate(args.steps, world, t_dev)
     ms_per_step = 1e3 * t_dev / args.steps
     for s in stats:
         assert s.max_rel_err <= p.tol_rel, "solve did not converge"
@@ -546,7 +559,8 @@ def main():
                             precision=args.precision, ctx=ctx2)
         e2e_t += time.perf_counter() - t1
     assert np.isfinite(wres).all()
-    e2e = {"value": args.steps * world / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * p.n,
+    e2e_t = max_over_ranks(e2e_t, dist, dev)
+    e2e = {"value": job_rate(args.steps, world, e2e_t), "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * p.n,
            "d2h_bytes_per_step": 8 * p.n}
 
     line = {
