@@ -381,6 +381,10 @@ def main():
                          "1M-site / 2048^2 workload, and a 1M-uniform-site solve); c5: 512 independent "
                          "problems, batched against sequential solves; one JSON line each")
     args = ap.parse_args()
+    if args.workload == "c5":
+        # the batch's 64 worker streams get 32 hardware queues instead of the default
+        # 8 (read when the process creates its CUDA context, so set before any CUDA call)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -205,12 +205,16 @@ ma_status ma_ot_solve(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double*
  * same device), sites, target masses and weights (initial guess in, solution out);
  * every array of the batch is in `mem`.  The problems are solved by `workers`
  * contexts (one CUDA stream and one host thread each) taking them in order; kernels of
- * different problems run concurrently.  workers = 0 autotunes the count (4 to 32) on the
- * first chunks of the batch (kept in the context for later calls); *workers_used (nullable)
- * receives the count used.  Each problem is solved by ma_ot_solve (status and
- * statistics are its); a worker's CG uses a share of the GPU, so results agree with
- * separate calls to the solver's tolerance, not to the last bit.  The call returns
- * MA_OK unless a CUDA or argument error stopped a worker. */
+ * different problems run concurrently.  workers = 0 autotunes the count (4 to 64) by
+ * solving copies of the batch's median problem (kept in the context for later calls);
+ * *workers_used (nullable) receives the count used.  Each problem is solved by
+ * ma_ot_solve (status and statistics are its); a worker's CG uses a share of the GPU,
+ * so results agree with separate calls to the solver's tolerance, not to the last bit.
+ * The call returns MA_OK unless a CUDA or argument error stopped a worker.  The
+ * workers' streams share the device's hardware work queues: a process that batches
+ * should set CUDA_DEVICE_MAX_CONNECTIONS=32 before it creates its CUDA context (the
+ * default, 8, serialises the streams onto 8 queues; 512 mixed problems of 500-50,000
+ * sites went from 188 to 236 problems/s with 32). */
 typedef struct ma_problem {
     const ma_mesh* mesh;
     int64_t n;
