@@ -519,9 +519,9 @@ def main():
     bytes_eval = eval_bytes(p.n, nnz, p.mesh.nv)
     peak, peak_kind = measured_peaks()
     achieved = bytes_eval / (pieces_ms * 1e-3) / 1e9
-    # DRAM bytes (read + write) of one k_pieces launch from the ncu capture summarised
-    # in profiles/k_pieces_c2_full.md, for this workload
-    # and the kernel's binding resource from the same capture: the FP64 pipe
+    # DRAM bytes (read + write) of one k_pieces launch on this workload, from a full ncu
+    # capture of the kernel (dram__bytes_read.sum + dram__bytes_write.sum), and the
+    # kernel's binding resource from the same capture: the FP64 pipe
     traffic = None
     fp64_pct = None
     tfile = os.path.join(ROOT, "profiles", "traffic.txt")
