@@ -89,6 +89,20 @@ public:
               d.ctx_, "ma_mesh_create_triangles");
         return d;
     }
+    // image_to_pl_function (functions.hpp:82-120): the density of a grey image,
+    // pixels[y * width + x] with rows top first and values 0..255 (CImg's image(x, y)),
+    // on a width x height vertex grid of [-1, 1]^2 with vertex values pixel / 255 + 1e-3.
+    // total_mass() is the value the reference returns.
+    static Density image(const std::vector<double>& pixels, int width, int height,
+                         Engine& e = Engine::instance())
+    {
+        if (width < 2 || height < 2 || (int64_t)pixels.size() != (int64_t)width * height)
+            throw Error(MA_ERR_INVALID_ARGUMENT, "image_to_pl_function: pixels.size() must be width * height");
+        Density d;
+        d.ctx_ = e.get();
+        check(ma_mesh_create_image(d.ctx_, width, height, pixels.data(), &d.mesh_), d.ctx_, "ma_mesh_create_image");
+        return d;
+    }
     Density(Density&& o) noexcept : ctx_(o.ctx_), mesh_(o.mesh_) { o.mesh_ = nullptr; }
     ~Density() { ma_mesh_destroy(mesh_); }
     ma_mesh* get() const { return mesh_; }
@@ -343,6 +357,46 @@ std::vector<Polygon> voronoi_polygon_intersection(const Polygon& P, const Matrix
     for (int64_t i = 0; i < n; i++)
         for (int64_t v = off[i]; v < off[i + 1]; v++) r[(size_t)i].emplace_back(xy[2 * v], xy[2 * v + 1]);
     return r;
+}
+
+// MA::draw_laguerre_diagram (rasterization.hpp:516-547): every piece of every Laguerre
+// cell rasterised with exact pixel coverage into a height x width x channels image
+// (row-major, row 0 first), pixel (i, j) covering [x0 + i dx, x0 + (i+1) dx] x
+// [y0 + j dy, y0 + (j+1) dy] with dx = (x1 - x0) / w, dy = (y1 - y0) / h; each piece adds
+// cover * (mean density at its vertices) * colors[site][channel].  colors holds n *
+// channels values, site-major.
+template <class Matrix, class Vector>
+std::vector<double> draw_laguerre_diagram(const Density& density, const Matrix& X, const Vector& weights,
+                                          const std::vector<double>& colors, int channels, double x0, double y0,
+                                          double x1, double y1, size_t w, size_t h)
+{
+    std::vector<double> x, y;
+    detail::split_sites(X, x, y);
+    const int64_t n = (int64_t)x.size();
+    if (channels < 1 || (int64_t)colors.size() != n * channels)
+        throw Error(MA_ERR_INVALID_ARGUMENT, "draw_laguerre_diagram: colors.size() must be n * channels");
+    std::vector<double> wv = detail::to_vec(weights, n), image(w * h * (size_t)channels, 0.0);
+    check(ma_draw_laguerre(density.ctx(), density.get(), n, x.data(), y.data(), wv.data(), colors.data(), channels,
+                           x0, y0, x1, y1, (int)w, (int)h, image.data(), MA_MEM_HOST),
+          density.ctx(), "ma_draw_laguerre");
+    return image;
+}
+
+// The reference's form, with one scalar colour per site and a put_pixel(x, y, value)
+// callback: the image is computed as above and put_pixel is called once per pixel
+// with the sum of the pieces' contributions to it (the reference calls it once per
+// piece and pixel, so a put_pixel that adds gives the same image); pixels that no
+// piece covers are not visited.
+template <class Matrix, class Vector, class ColorVector, class PutPixel>
+void draw_laguerre_diagram(const Density& density, const Matrix& X, const Vector& weights, const ColorVector& colors,
+                           double x0, double y0, double x1, double y1, size_t w, size_t h, PutPixel put_pixel)
+{
+    const int64_t n = (int64_t)X.rows();
+    const std::vector<double> img =
+        draw_laguerre_diagram(density, X, weights, detail::to_vec(colors, n), 1, x0, y0, x1, y1, w, h);
+    for (size_t j = 0; j < h; j++)
+        for (size_t i = 0; i < w; i++)
+            if (img[j * w + i] != 0.0) put_pixel((int)i, (int)j, img[j * w + i]);
 }
 
 // MA::solve_laplacian_matrix (optimal_transport.hpp:41-87) for the Hessian of the

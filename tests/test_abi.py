@@ -44,7 +44,7 @@ def test_python_api_fails_loudly_without_device():
         api.Context(0)
 
 
-def _build_wrapper_example(tmp_path):
+def _build_wrapper_example(tmp_path, name="wrapper_example"):
     import shutil
     import subprocess
     from mongeampere_gb300 import build as B
@@ -52,10 +52,10 @@ def _build_wrapper_example(tmp_path):
     gxx = shutil.which("g++")
     if not gxx:
         pytest.skip("no g++")
-    exe = str(tmp_path / "wrapper_example")
+    exe = str(tmp_path / name)
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    subprocess.check_call([gxx, "-std=c++17", "-O1", "-I", os.path.join(root, "include"),
-                           os.path.join(root, "tests", "cpp", "wrapper_example.cpp"), "-o", exe,
+    subprocess.check_call([gxx, "-std=c++17", "-O1", "-Wall", "-I", os.path.join(root, "include"),
+                           os.path.join(root, "tests", "cpp", name + ".cpp"), "-o", exe,
                            "-L", os.path.dirname(lib), "-lma_gb300", "-Wl,-rpath," + os.path.dirname(lib)])
     return exe
 
@@ -78,3 +78,15 @@ def test_cpp_wrapper_runs(tmp_path):
     exe = _build_wrapper_example(tmp_path)
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_cpp_image_and_drawing_wrappers_build(tmp_path):
+    # MA::Density::image and MA::draw_laguerre_diagram link against the library;
+    # without a GPU the error surfaces as MA::Error (exit status 3)
+    import subprocess
+    exe = _build_wrapper_example(tmp_path, "wrapper_image_raster")
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 3 and "no usable CUDA device" in r.stdout
