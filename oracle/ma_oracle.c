@@ -1668,6 +1668,16 @@ void ora_free(ora_result *r)
     free(r);
 }
 
+/* quadrature.hpp:24-42 on one triangle tri = (ax, ay, bx, by, cx, cy), for the tests
+ * that check the rule (tests/test_quadrature_triangle.cpp:10-21 integrates x y^2): the
+ * seven integrands of `integrand` for the linear function a x + b y + c and the site
+ * (sx, sy), added to out[0..6] */
+void ora_albrecht_collatz(double a, double b, double c, double sx, double sy, const double *tri, double *out)
+{
+    const linfn L = {a, b, c};
+    albrecht_collatz(&L, sx, sy, tri[0], tri[1], tri[2], tri[3], tri[4], tri[5], out);
+}
+
 /* exact predicate entry points, for the tests that check the filters */
 int ora_side1(const double *v, const double *w, double ex, double ey)
 {

@@ -66,6 +66,7 @@ def lib():
         L.ora_set_threads.argtypes = [ctypes.c_int]
         L.ora_max_threads.restype = ctypes.c_int
         L.ora_set_precision.argtypes = [ctypes.c_int]
+        L.ora_albrecht_collatz.argtypes = [ctypes.c_double] * 5 + [_dp, _dp]
         L.ora_side1.restype = ctypes.c_int
         L.ora_side1.argtypes = [_dp, _dp, ctypes.c_double, ctypes.c_double]
         L.ora_side2.restype = ctypes.c_int
@@ -282,6 +283,18 @@ def polygon_cells(x, y, w, qx, qy):
         off.append(off[-1] + m)
     return (np.array(off, np.int64), np.concatenate(xs) if xs else np.zeros((0, 2)),
             np.concatenate(labs) if labs else np.zeros(0, np.int32))
+
+
+def albrecht_collatz(lin, site, tri):
+    """quadrature.hpp:24-42 (integrate_albrecht_collatz) over one triangle
+    ``tri`` (3 x 2) for the linear function ``lin`` = (a, b, c), rho = a x + b y + c:
+    the integrals of rho |x - site|^2, rho, rho x, rho y, rho x^2, rho y^2, rho x y."""
+    L = lib()
+    t, tp = _d(np.asarray(tri, dtype=np.float64).reshape(6))
+    out = np.zeros(7)
+    L.ora_albrecht_collatz(float(lin[0]), float(lin[1]), float(lin[2]), float(site[0]), float(site[1]), tp,
+                           out.ctypes.data_as(_dp))
+    return out
 
 
 def side1(v, w, e):

@@ -329,3 +329,68 @@ def test_polygon_cells_candidates_change_nothing(oracle):
             a = xy[off[i]:off[i + 1]]
             s = int(np.argmin(np.abs(out[:m] - a[0]).max(1)))
             np.testing.assert_array_equal(np.roll(out[:m], -s, axis=0), a)
+
+
+def _exact_triangle_integrals(lin, site, tri):
+    """Exact integrals over a triangle with rational corners of rho |x - s|^2, rho,
+    rho x, rho y, rho x^2, rho y^2, rho x y (rho = a x + b y + c): the integrand as a
+    polynomial in the reference coordinates (u, v), x = A + u (B - A) + v (C - A), and
+    int_ref u^i v^j = i! j! / (i + j + 2)!."""
+    from fractions import Fraction as Fr
+    from math import factorial
+
+    def mul(p, q):
+        r = {}
+        for (i, j), a in p.items():
+            for (k, l), b in q.items():
+                r[(i + k, j + l)] = r.get((i + k, j + l), 0) + a * b
+        return r
+
+    def add(*ps):
+        r = {}
+        for p in ps:
+            for k, a in p.items():
+                r[k] = r.get(k, 0) + a
+        return r
+
+    def const(c):
+        return {(0, 0): Fr(c)}
+
+    (ax, ay), (bx, by), (cx, cy) = [(Fr(p[0]), Fr(p[1])) for p in tri]
+    X = {(0, 0): ax, (1, 0): bx - ax, (0, 1): cx - ax}
+    Y = {(0, 0): ay, (1, 0): by - ay, (0, 1): cy - ay}
+    a, b, c = (Fr(t) for t in lin)
+    rho = add(mul(const(a), X), mul(const(b), Y), const(c))
+    dx, dy = add(X, const(-Fr(site[0]))), add(Y, const(-Fr(site[1])))
+    polys = [mul(rho, add(mul(dx, dx), mul(dy, dy))), rho, mul(rho, X), mul(rho, Y), mul(rho, mul(X, X)),
+             mul(rho, mul(Y, Y)), mul(rho, mul(X, Y))]
+    jac = abs((bx - ax) * (cy - ay) - (cx - ax) * (by - ay))
+    return [float(jac * sum(v * Fr(factorial(i) * factorial(j), factorial(i + j + 2)) for (i, j), v in p.items()))
+            for p in polys]
+
+
+def test_albrecht_collatz_is_exact_for_cubics(oracle):
+    # tests/test_quadrature_triangle.cpp:10-21: the 6-point rule integrates x y^2 (and
+    # every integrand of degree <= 3) exactly; here on random triangles with dyadic
+    # corners (exact in binary) against rational arithmetic
+    from fractions import Fraction as Fr
+    rng = np.random.default_rng(12)
+    for _ in range(50):
+        tri = rng.integers(-64, 64, size=(3, 2)) / 32.0
+        cr = (tri[1, 0] - tri[0, 0]) * (tri[2, 1] - tri[0, 1]) - (tri[2, 0] - tri[0, 0]) * (tri[1, 1] - tri[0, 1])
+        if abs(cr) < 1e-3:
+            continue
+        if cr < 0:  # the rule weighs by CGAL's signed area: counter-clockwise corners
+            tri = tri[[0, 2, 1]]
+        lin = rng.integers(-16, 16, size=3) / 8.0
+        site = rng.integers(-32, 32, size=2) / 16.0
+        got = oracle.albrecht_collatz(lin, site, tri)
+        want = _exact_triangle_integrals([Fr(t) for t in lin], [Fr(t) for t in site], tri.tolist())
+        scale = max(1e-300, max(abs(v) for v in want))
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-14 * scale)
+        # clockwise corners give the negated integrals (signed area)
+        np.testing.assert_allclose(oracle.albrecht_collatz(lin, site, tri[[0, 2, 1]]), -got, rtol=0,
+                                   atol=1e-14 * scale)
+    # the reference test's own integrand: x y^2 is rho = x times the y^2 moment
+    got = oracle.albrecht_collatz((1.0, 0.0, 0.0), (0.0, 0.0), [[0, 0], [1, 0], [0, 1]])
+    assert got[5] == pytest.approx(1.0 / 60.0, rel=1e-15)
