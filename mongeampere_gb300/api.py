@@ -477,7 +477,9 @@ def ot_solve_batch(problems, eps_g: float = 1e-6, stop: str = "rel", precision: 
     """Many independent problems (``ma_ot_solve_batch``): ``problems`` is a list of
     ``(mesh, X, nu)`` or ``(mesh, X, nu, w0)``.  Returns ``(weights, stats, workers)``:
     the solved weights and a :class:`Statistics` per problem (``status`` set), and
-    the number of concurrent workers used (``workers=0``: autotuned)."""
+    the number of concurrent workers used (``workers=0``: autotuned).  The workers'
+    streams share the device's hardware queues: set ``CUDA_DEVICE_MAX_CONNECTIONS=32``
+    in the environment before the process first uses CUDA (the default is 8)."""
     ctx = ctx or default_context()
     n = len(problems)
     arr = (L.MaProblem * n)()
