@@ -90,3 +90,23 @@ def test_cpp_image_and_drawing_wrappers_build(tmp_path):
         pytest.skip("a GPU is present")
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 3 and "no usable CUDA device" in r.stdout
+
+
+def test_static_solve_checks_arguments_before_the_device():
+    # ma_laplacian_solve_static (the Newton solve that allocates nothing) rejects a
+    # system beyond its fixed scratch and null pointers on the host, before any CUDA
+    # call; with valid arguments and no GPU it reports the missing device
+    if has_gpu():
+        pytest.skip("a GPU is present: covered by the GPU test")
+    import ctypes
+    from mongeampere_gb300 import _lib
+    lib = _lib.load()
+    buf = (ctypes.c_double * 4)()
+    ibuf = (ctypes.c_int32 * 4)()
+    it = ctypes.c_int64(0)
+    args = (ibuf, ibuf, buf, buf, buf, 1e-10, 0, ctypes.byref(it), None)
+    assert lib.ma_laplacian_solve_static((1 << 18) + 1, *args) == _lib.MA_ERR_BUFFER_TOO_SMALL
+    assert lib.ma_laplacian_solve_static(0, *args) == _lib.MA_ERR_INVALID_ARGUMENT
+    assert lib.ma_laplacian_solve_static(3, None, ibuf, buf, buf, buf, 1e-10, 0, ctypes.byref(it),
+                                         None) == _lib.MA_ERR_INVALID_ARGUMENT
+    assert lib.ma_laplacian_solve_static(3, *args) == _lib.MA_ERR_NO_DEVICE
