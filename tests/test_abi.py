@@ -110,3 +110,18 @@ def test_static_solve_checks_arguments_before_the_device():
     assert lib.ma_laplacian_solve_static(3, None, ibuf, buf, buf, buf, 1e-10, 0, ctypes.byref(it),
                                          None) == _lib.MA_ERR_INVALID_ARGUMENT
     assert lib.ma_laplacian_solve_static(3, *args) == _lib.MA_ERR_NO_DEVICE
+
+
+def test_solve_defaults_are_the_references():
+    # MA::ot_solve(..., double eps_g = 1e-7, size_t maxiter = 100, ...)
+    # (optimal_transport.hpp:89-99) with its stop rule |m - nu|_2 < eps_g (:150), FP64
+    # and the caller's initial weights; host-only, no device needed
+    from mongeampere_gb300 import _lib
+    lib = _lib.load()
+    o = _lib.MaSolveOpts()
+    lib.ma_solve_opts_default(o)
+    assert o.eps_g == 1e-7 and o.maxiter == 100
+    assert o.stop_rule == 0 and o.precision == 0 and o.init == 0 and o.verbose == 0
+    # every status has a message
+    for s in range(11):
+        assert lib.ma_status_string(s).decode()
