@@ -125,3 +125,24 @@ def test_solve_defaults_are_the_references():
     # every status has a message
     for s in range(11):
         assert lib.ma_status_string(s).decode()
+
+
+def test_header_is_plain_c(tmp_path):
+    # include/ma.h is a C ABI: a C11 caller compiles against it with -pedantic, links
+    # the library and calls a host-only entry point
+    import shutil
+    import subprocess
+    from mongeampere_gb300 import build as B
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no gcc")
+    lib = B.build()
+    src = tmp_path / "caller.c"
+    src.write_text('#include "ma.h"\n'
+                   "int main(void)\n{\n    ma_solve_opts o;\n    ma_solve_opts_default(&o);\n"
+                   "    return o.maxiter == 100 && o.eps_g == 1e-7 ? 0 : 1;\n}\n")
+    exe = str(tmp_path / "caller")
+    subprocess.check_call([gcc, "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                           os.path.join(ROOT, "include"), str(src), "-o", exe, "-L", os.path.dirname(lib),
+                           "-lma_gb300", "-Wl,-rpath," + os.path.dirname(lib)])
+    assert subprocess.run([exe]).returncode == 0
