@@ -14,10 +14,13 @@ copy of sites, masses and initial weights, device->host copy of the weights insi
 the timed region).  L2 is flushed (a 512 MB write) before every timed step.
 
 ``--impl reference`` times the reference algorithm's CPU restatement (oracle/) on
-the host cores instead: each step is a bounded sample -- one Laguerre evaluation
-in the reference's FP64 arithmetic plus one sparse direct Newton solve -- scaled to
-a full solve by the number of evaluations and Newton iterations the reference
-algorithm takes on this workload.
+the host cores instead.  It first solves the workload once with it (FP64 evaluations,
+sparse LU Newton directions, the reference's backtracking), timed as a whole, which
+gives the Newton iterations and evaluations the algorithm takes; each step is then a
+bounded sample -- one Laguerre evaluation at one of that solve's Newton iterates plus
+one sparse LU Newton direction -- and ``value`` scales the samples to a full solve by
+those counts (the line says ``"extrapolated": true`` and carries the measured full
+solve beside it).
 """
 from __future__ import annotations
 
@@ -35,19 +38,19 @@ sys.path.insert(0, ROOT)
 METRIC = "Laguerre evals/s & OT solves/s at mass err≤1e-6, mixed vs FP64, 1 GB300"
 UNIT = "OT solves/s"
 WORKLOAD = "plain FP64 OT: 512x512 grid, 0.1 + 5 Gaussians, N=100,000 uniform sites, masses ~U[0.5,1.5], stop max rel mass err 1e-6"
-
-# The reference algorithm (oracle.ot_solve: flood-filled Laguerre evaluations, sparse
-# direct Newton solves, KMT backtracking) on this workload, seed 0: Newton
-# iterations and Laguerre evaluations to reach max relative mass error 1e-6
-# (oracle.ot_solve(p.mesh, p.x, p.y, p.nu, tol_rel=1e-6, arith="fp64", ring=1) with
-# p = workloads.c2(0): 15 iterations, 45 evaluations, max rel error 5.1e-9).
-REF_NITER = 15
-REF_NEVAL = 45
+WORKLOAD_C1 = "plain FP64 OT: 64x64 grid U[0.5,1.5], N=1,000 uniform sites, equal masses, stop max rel mass err 1e-9"
 
 # algorithmic bytes of one Laguerre evaluation on an implicit grid mesh:
 # X 16N + w 8N + g 8N + CSR Hessian (12 nnz + 4 (N+1)) + value 8 + vertex values 8V
 def eval_bytes(n, nnz, nv):
     return 16 * n + 8 * n + 8 * n + 12 * nnz + 4 * (n + 1) + 8 + 8 * nv
+
+
+# algorithmic bytes of one conjugate-gradient iteration of a Newton step: the sparse
+# product reads the CSR matrix (12 nnz + 4N), the vector updates read and write six
+# vectors of N doubles (48N)
+def cg_iter_bytes(n, nnz):
+    return 12 * nnz + 4 * n + 48 * n
 
 
 def measured_peaks():
@@ -128,16 +131,19 @@ def job_rate(steps, world, t):
     return steps * world / t
 
 
-def cpu_sample(problem, threads=None):
-    """One Laguerre evaluation in the reference's FP64 arithmetic + one sparse LU
-    Newton solve, on the host cores (the oracle)."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
     import oracle
-    if threads:
-        oracle.set_threads(threads)
+    return oracle
+
+
+def cpu_sample(problem, w):
+    """One Laguerre evaluation at weights w in the reference's FP64 arithmetic + one
+    sparse LU Newton direction of its Hessian, on all host threads (the oracle)."""
+    import numpy as np
+    oracle = _oracle()
     t0 = time.perf_counter()
-    r = oracle.kantorovich(problem.mesh, problem.x, problem.y, problem.w0, arith="fp64", ring=1)
+    r = oracle.kantorovich(problem.mesh, problem.x, problem.y, w, arith="fp64", ring=1)
     t1 = time.perf_counter()
     d = oracle.solve_laplacian_matrix(r.hessian(), r.g - problem.nu)
     t2 = time.perf_counter()
@@ -145,34 +151,53 @@ def cpu_sample(problem, threads=None):
     return t1 - t0, t2 - t1, oracle.max_threads()
 
 
+def reference_full_solve(problem):
+    """The reference algorithm's complete solve of the workload (oracle.ot_solve: FP64
+    evaluations, sparse LU directions, KMT backtracking from w = 0 to the stopping
+    rule), timed as a whole: (result with its Newton iterates, seconds)."""
+    oracle = _oracle()
+    t0 = time.perf_counter()
+    r = oracle.ot_solve(problem.mesh, problem.x, problem.y, problem.nu, tol_rel=problem.tol_rel, arith="fp64",
+                        ring=1, keep_iterates=True)
+    return r, time.perf_counter() - t0
+
+
 def run_reference(args, rank):
+    import numpy as np
+
     from mongeampere_gb300 import workloads as W
     if rank != 0:
         return
-    problem = W.c2(0)
-    for _ in range(args.warmup):
-        cpu_sample(problem)
-    te, tl = 0.0, 0.0
-    for _ in range(args.steps):
-        a, b, cores = cpu_sample(problem)
-        te += a
-        tl += b
-    te /= args.steps
-    tl /= args.steps
-    niter = REF_NITER
-    neval = REF_NEVAL
-    solve_s = neval * te + niter * tl
+    problem = W.c1(0) if args.workload == "c1" else W.c2(0)
+    ref, full_s = reference_full_solve(problem)
+    iterates = [np.zeros(problem.n)] + [h[5] for h in ref.history]
+    for k in range(args.warmup):
+        cpu_sample(problem, iterates[k % len(iterates)])
+    te, tl = [], []
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        a, b, cores = cpu_sample(problem, iterates[k % len(iterates)])
+        te.append(a)
+        tl.append(b)
+    t_steps = time.perf_counter() - t0
+    te_m, tl_m = float(np.mean(te)), float(np.mean(tl))
+    solve_s = ref.neval * te_m + ref.niter * tl_m
     value = 1.0 / solve_s
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": solve_s * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "seed": 0},
-        "laguerre_evals_per_s": 1.0 / te,
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"per step: 1 Laguerre evaluation ({te:.2f} s) + 1 sparse LU Newton solve "
-                                   f"({tl:.2f} s) of the CPU restatement on all {cores} threads; a full "
-                                   f"solve = {neval} evaluations + {niter} Newton solves"},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_steps / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD_C1 if args.workload == "c1" else WORKLOAD, "seed": 0},
+        "extrapolated": True,
+        "laguerre_evals_per_s": 1.0 / te_m,
+        "full_solve_measured": {"seconds": full_s, "solves_per_s": 1.0 / full_s, "newton_iters": ref.niter,
+                                "evals": ref.neval, "max_rel_err": ref.max_rel_err},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "extrapolated": True,
+                         "sample": f"per step: 1 Laguerre evaluation at one of the Newton iterates ({te_m:.2f} s "
+                                   f"mean) + 1 sparse LU Newton direction ({tl_m:.2f} s mean) of the CPU "
+                                   f"restatement on all {cores} threads; a full solve = {ref.neval} evaluations + "
+                                   f"{ref.niter} Newton directions, the counts of the complete reference-algorithm "
+                                   f"solve run first in this process ({full_s:.1f} s measured)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -376,11 +401,14 @@ def main():
                          "solution weights and print per-kernel device times (no benchmark line)")
     ap.add_argument("--profile-solve", action="store_true",
                     help="profiling driver: one solve with per-kernel device times (no benchmark line)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c3: the 1M-site mixed-precision comparison (evaluations of the clustered "
                          "1M-site / 2048^2 workload, and a 1M-uniform-site solve); c5: 512 independent "
-                         "problems, batched against sequential solves; one JSON line each")
+                         "problems, batched against sequential solves; one JSON line each; c1 (the "
+                         "reference's own 64^2 / 1,000-site case): the reference arm only")
     args = ap.parse_args()
+    if args.workload == "c1" and args.impl != "reference":
+        ap.error("--workload c1 (the reference's own CPU case) is for --impl reference")
     if args.workload == "c5":
         # the batch's 64 worker streams get 32 hardware queues instead of the default
         # 8 (read when the process creates its CUDA context, so set before any CUDA call)
@@ -516,32 +544,40 @@ def main():
     pieces_ms = prof["pieces_ms"] / max(prof["pieces_launches"], 1)
     stage1_ms = prof["cells_ms"] / max(prof["cells_launches"], 1)
     bounds_ms = prof["bounds_ms"] / max(prof["bounds_launches"], 1)
+    # and of the CG kernel over one complete solve
+    ctx.profile(True)
+    _, st_prof = solve_device()
+    torch.cuda.synchronize()
+    sprof = ctx.profile_read()
+    ctx.profile(False)
     bytes_eval = eval_bytes(p.n, nnz, p.mesh.nv)
+    bytes_cg = cg_iter_bytes(p.n, nnz)
     peak, peak_kind = measured_peaks()
-    achieved = bytes_eval / (pieces_ms * 1e-3) / 1e9
-    # DRAM bytes (read + write) of one k_pieces launch on this workload, from a full ncu
-    # capture of the kernel (dram__bytes_read.sum + dram__bytes_write.sum), and the
-    # kernel's binding resource from the same capture: the FP64 pipe
-    traffic = None
-    fp64_pct = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.txt")
-    if os.path.exists(tfile):
-        with open(tfile) as fh:
-            for ln in fh:
-                f = ln.split()
-                if len(f) == 2 and f[0] == "k_pieces_c2_dram_bytes_per_launch":
-                    traffic = float(f[1])
-                if len(f) == 2 and f[0] == "k_pieces_c2_fp64_pipe_pct_active":
-                    fp64_pct = float(f[1])
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic,
-                "kernel": "k_pieces (triangle clipping + FP64 integrals + Hessian rows of one evaluation)",
-                "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_eval,
-                "avg_launch_ms": pieces_ms,
-                "other_eval_kernels_ms": {"k_cells_stage1": stage1_ms, "k_tree_bounds": bounds_ms},
-                "binding": {"resource": "FP64 pipe (GB300: ~2 FP64 FMA lanes per clock per SM)",
-                            "pct_of_peak_active": fp64_pct,
-                            "source": "ncu sm__pipe_fp64_cycles_active, profiles/k_pieces_c2_full.md"}}
+    cg_iter_ms = sprof["pcg_ms"] / max(sprof["pcg_iters"], 1)
+
+    def leg(ms, nbytes):
+        a = nbytes / (ms * 1e-3) / 1e9
+        return {"avg_ms": ms, "algorithmic_bytes": nbytes, "achieved_gbs": a, "frac": a / peak}
+
+    kernels = {"k_cells_stage1": leg(stage1_ms, bytes_eval), "k_pieces": leg(pieces_ms, bytes_eval),
+               "k_pcg_amg (per CG iteration)": leg(cg_iter_ms, bytes_cg)}
+    # the dominant evaluation kernel: the larger share of one evaluation
+    dom = "k_cells_stage1" if stage1_ms >= pieces_ms else "k_pieces"
+    what = {"k_cells_stage1": "k_cells_stage1 (site-tree search and clipping of every Laguerre cell)",
+            "k_pieces": "k_pieces (cell-triangle clipping, integrals and Hessian rows)"}[dom]
+    roofline = {"bound": "hbm", "achieved": kernels[dom]["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                "frac": kernels[dom]["frac"],
+                # DRAM bytes need an ncu capture, which the benchmark does not run: the
+                # capture of this kernel is kept with the profiles as evidence
+                "traffic": None,
+                "kernel": what, "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_eval,
+                "avg_launch_ms": kernels[dom]["avg_ms"],
+                "per_kernel": kernels, "k_tree_bounds_ms": bounds_ms}
+    # the whole solve: every evaluation and every CG iteration over the solve's time
+    solve_bytes = st_prof.neval * bytes_eval + st_prof.cg_iters * bytes_cg
+    solve_gbs = solve_bytes / (ms_per_step * 1e-3) / 1e9
+    solve_roofline = {"algorithmic_bytes": solve_bytes, "evals": st_prof.neval, "cg_iters": st_prof.cg_iters,
+                      "achieved_gbs": solve_gbs, "frac": solve_gbs / peak}
 
     # ---- e2e through the C ABI with host buffers ----
     xh = torch.tensor(p.x).pin_memory().numpy()
@@ -580,19 +616,25 @@ def main():
                         "max_rel_err": stats[0].max_rel_err, "wall_s_per_step": t_wall / args.steps},
         "e2e": e2e,
         "roofline": roofline,
+        "solve_roofline": solve_roofline,
         "clocks": clk,
         "gpu_launches": launches,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        te, tl, cores = cpu_sample(W.c2(0))
-        niter = REF_NITER
-        neval = REF_NEVAL
+        # the oracle at w = 0 and at the solution (the two ends of the Newton path), one
+        # sparse LU direction each, scaled by this run's own solve counts
+        pc = W.c2(0)
+        te0, tl0, cores = cpu_sample(pc, pc.w0)
+        te1, tl1, _ = cpu_sample(pc, wsol.cpu().numpy())
+        te, tl = 0.5 * (te0 + te1), 0.5 * (tl0 + tl1)
+        neval, niter = stats[0].neval, stats[0].niter
         cpu_solve = neval * te + niter * tl
         line["cpu_baseline"] = {
-            "value": 1.0 / cpu_solve, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"1 Laguerre evaluation ({te:.2f} s) + 1 sparse LU Newton solve ({tl:.2f} s) of the CPU "
-                      f"restatement (reference FP64 arithmetic) on {cores} threads, scaled to {neval} "
-                      f"evaluations + {niter} Newton solves"}
+            "value": 1.0 / cpu_solve, "unit": UNIT, "cores": cores, "kind": "port", "extrapolated": True,
+            "sample": f"2 Laguerre evaluations (w = 0 and the solution; {te:.2f} s mean) + 2 sparse LU Newton "
+                      f"directions ({tl:.2f} s mean) of the CPU restatement (reference FP64 arithmetic) on "
+                      f"{cores} threads, scaled to this run's solve: {neval} evaluations + {niter} Newton "
+                      f"directions"}
     if rank == 0:
         print(json.dumps(line))
     if dist:

@@ -19,6 +19,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdio>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -407,8 +408,13 @@ Vector solve_laplacian_matrix(const Density& density, const Vector& g)
     const int64_t n = (int64_t)g.size();
     std::vector<double> gg = detail::to_vec(g, n), d(n);
     int64_t it = 0;
-    check(ma_laplacian_solve(density.ctx(), gg.data(), d.data(), MA_MEM_HOST, 1e-12, 0, &it), density.ctx(),
-          "ma_laplacian_solve");
+    const ma_status s = ma_laplacian_solve(density.ctx(), gg.data(), d.data(), MA_MEM_HOST, 1e-12, 0, &it);
+    // the reference warns and goes on when its Cholesky residual is large
+    // (optimal_transport.hpp:67-79); so does this wrapper when the CG stops early
+    if (s == MA_CG_NOCONV)
+        std::fprintf(stderr, "WARNING: in solve_laplacian_matrix: %s\n", ma_status_string(s));
+    else
+        check(s, density.ctx(), "ma_laplacian_solve");
     Vector r;
     detail::from_vec(r, d);
     return r;

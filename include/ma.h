@@ -58,7 +58,11 @@ typedef enum ma_status {
                                    (optimal_transport.hpp:137-148) */
     MA_LINESEARCH_FAIL = 8,     /* ot_solve: the step fell below 2^-40 */
     MA_MAXITER = 9,             /* ot_solve: maxiter reached before the stop rule held */
-    MA_ERR_BUFFER_TOO_SMALL = 10
+    MA_ERR_BUFFER_TOO_SMALL = 10,
+    MA_CG_NOCONV = 11           /* a linear solve stopped at its iteration cap, or broke down (p.Hp <= 0),
+                                   before its relative residual reached rtol; the output holds the
+                                   last iterate (the reference's SimplicialLLT has no such state; its
+                                   residual check, optimal_transport.hpp:67-79, falls back to SPQR) */
 } ma_status;
 
 typedef enum ma_mem { MA_MEM_HOST = 0, MA_MEM_DEVICE = 1 } ma_mem;
@@ -190,6 +194,9 @@ typedef struct ma_stats {
     double t_linsolve_ms;        /* device time spent in linear solves */
     size_t neval_fp64;           /* evaluations with FP64 integrals (all of them unless precision
                                     is MA_MIXED) */
+    size_t cg_noconv;            /* Newton steps whose CG stopped at cg_maxiter (or broke down) before
+                                    its residual met the forcing term: the step went on with the
+                                    unconverged direction, checked by the line search as usual */
 } ma_stats;
 
 void ma_solve_opts_default(ma_solve_opts* o);
@@ -241,7 +248,9 @@ ma_status ma_w2_flow(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, double* x, dou
                      ma_stats* stats);
 
 /* Newton direction of solve_laplacian_matrix: solve H[:n-1,:n-1] d = g[:n-1], d[n-1] = 0,
- * for the Hessian of the last ma_kantorovich call.  Returns the CG iteration count in *iters. */
+ * for the Hessian of the last ma_kantorovich call.  Returns the CG iteration count in *iters;
+ * MA_CG_NOCONV (with d the last iterate) when the CG stopped before |r| <= rtol |g|.
+ * rtol <= 0 means 1e-10; maxiter <= 0 means 20000 (larger values are capped at INT_MAX). */
 ma_status ma_laplacian_solve(ma_ctx* ctx, const double* g, double* d, ma_mem mem, double rtol,
                              int64_t maxiter, int64_t* iters);
 
@@ -252,12 +261,14 @@ ma_status ma_laplacian_solve(ma_ctx* ctx, const double* g, double* d, ma_mem mem
  * H[:n-1,:n-1] d = g[:n-1], d[n-1] = 0 (the system of ma_laplacian_solve) for a CSR
  * Hessian the caller passes in; rowptr, col, val, g and d are device memory of the
  * current device, `stream` is a cudaStream_t (NULL: the default stream), *iters (host)
- * receives the CG iteration count.
+ * receives the CG iteration count.  rtol <= 0 means 1e-10; maxiter <= 0 means 20000 and
+ * larger values are capped at INT_MAX.  The call returns MA_CG_NOCONV, with d holding the
+ * last iterate, when the CG stopped at maxiter (or broke down) before |r| <= rtol |g|.
  *  - The CG work vectors live in one fixed device array of the library (10.1 MB, held
  *    by every GPU that loads the library until the process exits); n is limited to
  *    262,144 and larger systems return MA_ERR_BUFFER_TOO_SMALL.
- *  - The first call on a device looks up that array's address; make it before any
- *    stream capture.
+ *  - The first call on a device looks up that array's address, so make that first call
+ *    before any stream capture begins.
  *  - Every call shares the array: calls that overlap on the GPU (from several threads
  *    or streams) race and corrupt each other's result. */
 ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,

@@ -27,7 +27,8 @@ class MaStats(ctypes.Structure):
     _fields_ = [("niter", ctypes.c_size_t), ("neval", ctypes.c_size_t), ("cg_iters", ctypes.c_size_t),
                 ("linesearch_halvings", ctypes.c_size_t), ("grad_norm", ctypes.c_double),
                 ("max_rel_err", ctypes.c_double), ("value", ctypes.c_double), ("t_eval_ms", ctypes.c_double),
-                ("t_linsolve_ms", ctypes.c_double), ("neval_fp64", ctypes.c_size_t)]
+                ("t_linsolve_ms", ctypes.c_double), ("neval_fp64", ctypes.c_size_t),
+                ("cg_noconv", ctypes.c_size_t)]
 
 
 class MaProblem(ctypes.Structure):
@@ -132,6 +133,7 @@ MA_EMPTY_CELL = 7
 MA_LINESEARCH_FAIL = 8
 MA_MAXITER = 9
 MA_ERR_BUFFER_TOO_SMALL = 10
+MA_CG_NOCONV = 11
 
 MA_MEM_HOST = 0
 MA_MEM_DEVICE = 1

@@ -418,6 +418,7 @@ class Statistics:
     t_eval_ms: float = 0.0
     t_linsolve_ms: float = 0.0
     neval_fp64: int = 0
+    cg_noconv: int = 0
     status: int = 0
 
 

@@ -447,6 +447,7 @@ const char* ma_status_string(ma_status s)
     case MA_LINESEARCH_FAIL: return "line search failed";
     case MA_MAXITER: return "maximum number of iterations reached";
     case MA_ERR_BUFFER_TOO_SMALL: return "buffer too small";
+    case MA_CG_NOCONV: return "conjugate gradients stopped before reaching the requested residual";
     }
     return "unknown status";
 }

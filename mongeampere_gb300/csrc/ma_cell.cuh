@@ -616,72 +616,103 @@ MA_HD void integrate_labels(int n, const Lab& lab_of, const Nb64* nb, const Fixe
 // ---------------------------------------------------------------------------
 // the mixed-precision integrals (FP32)
 // ---------------------------------------------------------------------------
-// FP32 vertex between edges prev and cur from the FP32 slot data (the values of
-// vtx_fixed_bis / vtx_bis_bis without their error radii)
-MA_HD void vtx32(int prev, int cur, const Slot* slots, const Fixed& fx, float& X, float& Y)
+// FP32 vertex between edges prev and cur from the FP32 slot data, with its certified
+// per-component error radius R (the positions and radii of the clip: a fixed corner,
+// vtx_fixed_bis or vtx_bis_bis)
+MA_HD void vtx32r(int prev, int cur, const Slot* slots, const Fixed& fx, float& X, float& Y, float& R)
 {
     if (prev < 0 && cur < 0) {
         const int e = -1 - cur;
         X = fx.ux[e];
         Y = fx.uy[e];
+        R = fx.ur[e];
         return;
     }
     if (prev >= 0 && cur >= 0) {
-        const Slot a = slots[prev], b = slots[cur];
-        const float inv = 1.0f / (2.0f * (a.dx * b.dy - a.dy * b.dx));
-        X = (a.z * b.dy - b.z * a.dy) * inv;
-        Y = (a.dx * b.z - b.dx * a.z) * inv;
+        vtx_bis_bis(slots[prev], slots[cur], X, Y, R);
         return;
     }
-    const int e = (prev < 0) ? -1 - prev : -1 - cur;
-    const Slot a = slots[(prev < 0) ? cur : prev];
-    const int e1 = (e + 1 == fx.n) ? 0 : e + 1;
-    const float px = fx.ux[e], py = fx.uy[e];
-    const float ex = fx.ux[e1] - px, ey = fx.uy[e1] - py;
-    const float t = -(2.0f * (px * a.dx + py * a.dy) - a.z) / (2.0f * (ex * a.dx + ey * a.dy));
-    X = px + t * ex;
-    Y = py + t * ey;
+    if (prev < 0)
+        vtx_fixed_bis(fx, -1 - prev, slots[cur], X, Y, R);
+    else
+        vtx_fixed_bis(fx, -1 - cur, slots[prev], X, Y, R);
 }
 
+// FP32 sum with a running compensation (Neumaier's variant of Kahan summation): the
+// rounding error of every addition is carried in c, so the sum's error does not grow
+// with the number of terms
+struct CompF {
+    float s, c;
+    MA_HD void add(float x)
+    {
+        const float t = s + x;
+        c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
+    MA_HD float val() const { return s + c; }
+};
+
+// An FP32 radical-axis edge integral is kept when the error radii of its two ends are
+// below kEdgeTol32 / 2 of its length |dx| + |dy|; otherwise the edge is redone in FP64.
+// With crs = |e x d| = |e| |d| and |e| >= (|dx| + |dy|) / sqrt 2, the edge's relative
+// error is then below kEdgeTol32 plus a few FP32 roundings: every Hessian entry is a sum
+// of such edges of one sign, so each entry is within ~2.5e-4 of the FP64 one.
+constexpr float kEdgeTol32 = 0x1p-12f;
+
 // integrate_labels (mass, value part, Hessian edges; no moments) in FP32 from the
-// FP32 vertices; the caller sums the pieces of a cell in FP64.  Relative error of a
-// piece's integrals: a few FP32 roundings of the cell-relative coordinates.
+// FP32 vertices, with compensated fan sums; the caller sums the pieces of a cell in
+// FP64.  The Hessian part of an edge comes from FP32 vertices when their certified
+// radii allow (kEdgeTol32), else from the FP64 vertices of vtx64 (nb, fx.rx / ry): short
+// edges, whose FP32 ends cancel, are the ones that need it.
 template <class Lab, class Edge>
-MA_HD void integrate_labels32(int n, const Lab& lab_of, const Slot* slots, const Fixed& fx, float c0, float gx,
-                              float gy, float& mass, float& second, const Edge& edge)
+MA_HD void integrate_labels32(int n, const Lab& lab_of, const Slot* slots, const Nb64* nb, const Fixed& fx, double c0,
+                              double gx, double gy, float& mass, float& second, const Edge& edge)
 {
-    float x0, y0;
-    vtx32(lab_of(n - 1), lab_of(0), slots, fx, x0, y0);
-    float ax = x0, ay = y0;
-    float m0 = 0, m1x = 0, m1y = 0, q2 = 0, c3x = 0, c3y = 0;
+    const float c0f = (float)c0, gxf = (float)gx, gyf = (float)gy;
+    float x0, y0, r0;
+    vtx32r(lab_of(n - 1), lab_of(0), slots, fx, x0, y0, r0);
+    float ax = x0, ay = y0, ar = r0;
+    CompF m0{0, 0}, m1x{0, 0}, m1y{0, 0}, q2{0, 0}, c3x{0, 0}, c3y{0, 0};
     for (int k = 0; k < n; k++) {
         const int lab = lab_of(k);
-        float bx, by;
+        float bx, by, br;
         if (k + 1 < n)
-            vtx32(lab, lab_of(k + 1), slots, fx, bx, by);
+            vtx32r(lab, lab_of(k + 1), slots, fx, bx, by, br);
         else {
             bx = x0;
             by = y0;
+            br = r0;
         }
         const float cr = ax * by - ay * bx;
         const float aa = ax * ax + ay * ay, ab = ax * bx + ay * by, bb = bx * bx + by * by;
-        m0 += cr;
-        m1x += cr * (ax + bx);
-        m1y += cr * (ay + by);
-        q2 += cr * (aa + ab + bb);
+        m0.add(cr);
+        m1x.add(cr * (ax + bx));
+        m1y.add(cr * (ay + by));
+        q2.add(cr * (aa + ab + bb));
         const float ka = 3.0f * aa + 2.0f * ab + bb, kb = aa + 2.0f * ab + 3.0f * bb;
-        c3x += cr * (ax * ka + bx * kb);
-        c3y += cr * (ay * ka + by * kb);
+        c3x.add(cr * (ax * ka + bx * kb));
+        c3y.add(cr * (ay * ka + by * kb));
         if (lab >= 0) {
-            const Slot d = slots[lab];
-            const float crs = fabsf((bx - ax) * d.dy - (by - ay) * d.dx);
-            edge(k, lab, crs * (c0 + gx * 0.5f * (ax + bx) + gy * 0.5f * (ay + by)));
+            const float ex = bx - ax, ey = by - ay;
+            if (2.0f * (ar + br) <= kEdgeTol32 * (fabsf(ex) + fabsf(ey))) {
+                const Slot d = slots[lab];
+                const float crs = fabsf(ex * d.dy - ey * d.dx);
+                edge(k, lab, (double)(crs * (c0f + gxf * 0.5f * (ax + bx) + gyf * 0.5f * (ay + by))));
+            } else {
+                double px, py, qx, qy;
+                vtx64(lab_of(k == 0 ? n - 1 : k - 1), lab, nb, fx, px, py);
+                vtx64(lab, lab_of(k + 1 < n ? k + 1 : 0), nb, fx, qx, qy);
+                const Nb64 d = nb[lab];
+                const double crs = fabs((qx - px) * d.dy - (qy - py) * d.dx);
+                edge(k, lab, crs * (c0 + gx * 0.5 * (px + qx) + gy * 0.5 * (py + qy)));
+            }
         }
         ax = bx;
         ay = by;
+        ar = br;
     }
-    mass = c0 * (m0 * 0.5f) + gx * (m1x * (1.0f / 6.0f)) + gy * (m1y * (1.0f / 6.0f));
-    second = c0 * (q2 * (1.0f / 12.0f)) + gx * (c3x * (1.0f / 60.0f)) + gy * (c3y * (1.0f / 60.0f));
+    mass = c0f * (m0.val() * 0.5f) + gxf * (m1x.val() * (1.0f / 6.0f)) + gyf * (m1y.val() * (1.0f / 6.0f));
+    second = c0f * (q2.val() * (1.0f / 12.0f)) + gxf * (c3x.val() * (1.0f / 60.0f)) + gyf * (c3y.val() * (1.0f / 60.0f));
 }
 
 // ---------------------------------------------------------------------------

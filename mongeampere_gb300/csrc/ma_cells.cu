@@ -1043,8 +1043,8 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                     // FP32 integrals of the piece; the cell sums below are FP64
                     float pm, ps;
                     integrate_labels32(
-                        (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.slot + C.soff, T, (float)c0, (float)gx,
-                        (float)gy, pm, ps, [&](int e, int, float v) { W.hvc[e][p] = (double)v; });
+                        (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.slot + C.soff, W.nb + C.soff, T, c0, gx, gy,
+                        pm, ps, [&](int e, int, double v) { W.hvc[e][p] = v; });
                     W.out[0][p] = (double)pm;
                     W.out[1][p] = (double)ps;
                     continue;

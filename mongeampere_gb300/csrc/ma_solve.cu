@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <climits>
 #include <cstdio>
 #include <mutex>
 #include <utility>
@@ -408,7 +409,10 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
                 continue;
             }
             if (niter > o.maxiter) {
+                // the reference's loop test `niter++ <= maxiter` (optimal_transport.hpp:150-151)
+                // counts this last, failed test too: Statistics::niter = maxiter + 2
                 result = MA_MAXITER;
+                niter++;
                 break;
             }
             niter++;
@@ -437,6 +441,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
             cudaEventElapsedTime(&ms, e0, e1);
             S.t_linsolve_ms += ms;
             S.cg_iters += it;
+            if (!(rr <= rtol * (1.0 + 1e-12))) S.cg_noconv++;  // rr = |r| / |g| of the direction
             MA_CUDA(c, cudaMemcpyAsync(c->w0.p, w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
             double alpha = 1.0, n0 = gn;
             bool ok = false;
@@ -641,6 +646,7 @@ static ma_status multiscale_solve(Ctx* c, const Mesh* m, int n, const double* dx
         S.niter += Sl.niter;
         S.neval += Sl.neval;
         S.neval_fp64 += Sl.neval_fp64;
+        S.cg_noconv += Sl.cg_noconv;
         S.cg_iters += Sl.cg_iters;
         S.linesearch_halvings += Sl.linesearch_halvings;
         S.t_eval_ms += Sl.t_eval_ms;
@@ -722,7 +728,7 @@ ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int3
     a.part = part;
     a.out = out;
     a.rtol = rtol > 0 ? rtol : 1e-10;
-    a.maxiter = maxiter > 0 ? (int)maxiter : 20000;
+    a.maxiter = maxiter <= 0 ? 20000 : (maxiter > INT_MAX ? INT_MAX : (int)maxiter);
     void* args[] = {&a};
     if (cudaLaunchCooperativeKernel((void*)k_pcg, dim3(nb), dim3(kPcgThreads), args, 0, s) != cudaSuccess) {
         cudaGetLastError();
@@ -735,6 +741,9 @@ ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int3
         return MA_ERR_CUDA;
     }
     if (iters) *iters = (int64_t)res[0];
+    // res[1] = |r|, res[2] = |g| of the last iterate: the CG stopped at maxiter or broke
+    // down (p.Hp <= 0) unless the residual met the tolerance
+    if (!(res[1] <= a.rtol * res[2])) return MA_CG_NOCONV;
     return MA_OK;
 }
 
@@ -770,14 +779,17 @@ ma_status ma_laplacian_solve(ma_ctx* cp, const double* g, double* d, ma_mem mem,
     double* dd = (mem == MA_MEM_HOST) ? c->dirn.as<double>() : d;
     int it = 0;
     double rr = 0;
-    ma_status st = pcg_solve(c, n, dg, dd, rtol > 0 ? rtol : 1e-10, maxiter > 0 ? (int)maxiter : 20000, &it, &rr,
-                             MA_PRECOND_MULTIGRID);
+    const double tol = rtol > 0 ? rtol : 1e-10;
+    const int mit = maxiter <= 0 ? 20000 : (maxiter > INT_MAX ? INT_MAX : (int)maxiter);
+    ma_status st = pcg_solve(c, n, dg, dd, tol, mit, &it, &rr, MA_PRECOND_MULTIGRID);
     if (st != MA_OK) return st;
     if (mem == MA_MEM_HOST) {
         MA_CUDA(c, cudaMemcpyAsync(d, dd, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
         MA_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     if (iters) *iters = it;
+    if (!(rr <= tol * (1.0 + 1e-12)))
+        return fail(c, MA_CG_NOCONV, "CG stopped at its iteration cap before reaching rtol");
     return MA_OK;
 }
 
@@ -850,6 +862,7 @@ ma_status ma_w2_flow(ma_ctx* cp, const ma_mesh* mp, int64_t n64, double* x, doub
         total.niter += st.niter;
         total.neval += st.neval;
         total.neval_fp64 += st.neval_fp64;
+        total.cg_noconv += st.cg_noconv;
         total.cg_iters += st.cg_iters;
         total.linesearch_halvings += st.linesearch_halvings;
         total.t_eval_ms += st.t_eval_ms;

@@ -350,10 +350,11 @@ def solve_laplacian_matrix(h, g):
 
 def ot_solve(mesh, x, y, nu, w=None, eps_g: float = 1e-7, maxiter: int = 100,
              tol_rel: float | None = None, mode: int = 1, verbose: bool = False, arith: str = "dd",
-             ring: int = 2) -> SolveResult:
+             ring: int = 2, keep_iterates: bool = False) -> SolveResult:
     """``MA::ot_solve`` restated.  The stop rule is the reference's
     ``|m - nu|_2 < eps_g`` unless ``tol_rel`` is given, in which case it is
-    ``max_i |m_i - nu_i| / nu_i <= tol_rel``."""
+    ``max_i |m_i - nu_i| / nu_i <= tol_rel``.  ``keep_iterates`` adds each accepted
+    Newton iterate's weights to the history entries."""
     nu = np.asarray(nu, dtype=np.float64)
     n = nu.shape[0]
     w = np.zeros(n) if w is None or len(w) != n else np.array(w, dtype=np.float64)
@@ -393,7 +394,8 @@ def ot_solve(mesh, x, y, nu, w=None, eps_g: float = 1e-7, maxiter: int = 100,
             alpha *= 0.5
             if alpha < 2.0 ** -40:
                 raise RuntimeError("line search failed")
-        history.append((niter, fx, float(np.linalg.norm(g)), alpha, stats["neval"]))
+        history.append((niter, fx, float(np.linalg.norm(g)), alpha, stats["neval"]) +
+                       ((w.copy(),) if keep_iterates else ()))
         if verbose:
             print(f"it {niter}: f={fx} |df|={np.linalg.norm(g)} tau={alpha} eval={stats['neval']}")
     return SolveResult(w, m, niter, stats["neval"], fx, float(np.linalg.norm(g)),

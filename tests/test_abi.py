@@ -123,8 +123,8 @@ def test_solve_defaults_are_the_references():
     assert o.eps_g == 1e-7 and o.maxiter == 100
     assert o.stop_rule == 0 and o.precision == 0 and o.init == 0 and o.verbose == 0
     # every status has a message
-    for s in range(11):
-        assert lib.ma_status_string(s).decode()
+    for s in range(_lib.MA_CG_NOCONV + 1):
+        assert lib.ma_status_string(s).decode() != "unknown status"
 
 
 def test_header_is_plain_c(tmp_path):

@@ -68,7 +68,7 @@ def test_reference_arm_under_torchrun_prints_one_line():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0"]
+           "--impl", "reference", "--gpus", "2", "--steps", "2", "--warmup", "0", "--workload", "c1"]
     env = dict(os.environ, OMP_NUM_THREADS="2")
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
@@ -77,3 +77,7 @@ def test_reference_arm_under_torchrun_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    # the counts come from the complete solve run in the same process, and the line
+    # says that its value is scaled from samples
+    assert d["extrapolated"] is True and d["full_solve_measured"]["newton_iters"] > 0
+    assert d["full_solve_measured"]["max_rel_err"] <= 1e-9

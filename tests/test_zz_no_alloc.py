@@ -57,3 +57,33 @@ def test_static_solve_rejects_oversized_systems():
     st = lib.ma_laplacian_solve_static((1 << 18) + 1, _ptr(i), _ptr(i), _ptr(x), _ptr(x), _ptr(x), 1e-10, 0,
                                        ctypes.byref(it), None)
     assert st == _lib.MA_ERR_BUFFER_TOO_SMALL
+
+
+def test_static_solve_reports_a_capped_iteration():
+    # maxiter = 1 cannot reach rtol 1e-13: the call says so (MA_CG_NOCONV) and leaves the
+    # first CG iterate in d; a maxiter beyond INT_MAX is capped, not wrapped to zero
+    import torch
+    from mongeampere_gb300 import _lib, api
+
+    ctx = api.Context(0)
+    lib = ctx.lib
+    p = W.make_problem(48, 2000, seed=2)
+    v, g, h = api.kantorovich(p.mesh, np.c_[p.x, p.y], np.zeros(p.n), ctx=ctx)
+    rhs = np.asarray(g) - p.nu
+    rp = torch.tensor(h.rowptr, dtype=torch.int32, device="cuda")
+    col = torch.tensor(h.col, dtype=torch.int32, device="cuda")
+    val = torch.tensor(h.val, dtype=torch.float64, device="cuda")
+    b = torch.tensor(rhs, dtype=torch.float64, device="cuda")
+    d = torch.zeros(p.n, dtype=torch.float64, device="cuda")
+    it = ctypes.c_int64(-1)
+    st = lib.ma_laplacian_solve_static(p.n, _ptr(rp), _ptr(col), _ptr(val), _ptr(b), _ptr(d), 1e-13, 1,
+                                       ctypes.byref(it), None)
+    assert st == _lib.MA_CG_NOCONV
+    assert it.value == 1
+    assert np.isfinite(d.cpu().numpy()).all()
+    d_ref, _ = api.solve_laplacian_matrix(rhs, rtol=1e-13, ctx=ctx)
+    it = ctypes.c_int64(-1)
+    st = lib.ma_laplacian_solve_static(p.n, _ptr(rp), _ptr(col), _ptr(val), _ptr(b), _ptr(d), 1e-13, 1 << 40,
+                                       ctypes.byref(it), None)
+    assert st == _lib.MA_OK and it.value > 1
+    np.testing.assert_allclose(d.cpu().numpy(), d_ref, rtol=0, atol=1e-9 * np.abs(d_ref).max())
