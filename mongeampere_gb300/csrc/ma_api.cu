@@ -223,6 +223,8 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     a.tree.ab = c->t_ab.as<double4>();
     a.tree.nk = c->t_nk.as<float4>();
     a.tree.posf = c->posf.as<float2>();
+    a.tree.parent = c->t_parent.as<int>();
+    a.tree.leaf_parent = c->t_leaf_parent.as<int>();
     a.X0 = m->X0;
     a.Y0 = m->Y0;
     a.X1 = m->X1;

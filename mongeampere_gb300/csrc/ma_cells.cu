@@ -385,55 +385,485 @@ __device__ void process_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>&
 }
 
 // ---------------------------------------------------------------------------
-// stage 1: one thread per cell
+// stage 1: a warp per cell
 // ---------------------------------------------------------------------------
+// The cell's polygon is held a vertex per lane (its labels, FP32 positions and error
+// radii in registers, mirrored in shared memory for the tests that read every vertex);
+// the neighbour slots live in shared memory.  Candidate sites are tested 32 at a time
+// ("can this site cut the polygon?", certified FP32, every vertex) and the ones that
+// may cut are clipped one after another by the whole warp: a side test per vertex, a
+// ballot of the vertices outside, a scan of the Sutherland-Hodgman outputs
+// (vti.hpp:168-198) and a pass through shared memory.  The candidates are
+//   1. the seeds: the previous evaluation's neighbours (same sites, nearby weights),
+//      or else the 16 sites around the site in Morton order;
+//   2. the site tree, walked in batches of up to 32 nodes from the top of a stack: it
+//      starts from the siblings of the site's own root-to-leaf path (every other
+//      subtree); a node that no site of can cut the polygon (node_harmless_v) is
+//      dropped, a small node's sites become candidates, a larger one is replaced by
+//      its two children.
+// The cell is exact whatever order the candidates come in (every decision is certified
+// or symbolic); the neighbour list is written sorted by site index.
 constexpr int kCapLarge = 256;
+constexpr int kS1Warps = 4;     // warps per block
+constexpr int kS1Stack = 512;   // tree nodes waiting per warp
+constexpr int kS1Cand = 128;    // candidate sites of one batch (32 nodes of < 4 sites)
+constexpr int kS1Bucket = 4;    // nodes of fewer sites are visited site by site
+constexpr int kS1Window = 8;    // Morton-order seeds on either side without a previous list
 
-__global__ void __launch_bounds__(128, 6) k_cells_stage1(CellArgs A)
+struct Stage1Warp {
+    float pux[32], puy[32], pur[32];  // the polygon, a vertex per lane
+    int plab[32];
+    Slot slot[kCapSmall];
+    int seed[kSeedCap + 1];
+    int stack[kS1Stack];
+    int cand[kS1Cand];
+    Fixed box;
+};
+
+__global__ void __launch_bounds__(32 * kS1Warps, 6) k_cells_stage1(CellArgs A)
 {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    constexpr unsigned kFull = 0xffffffffu;
+    __shared__ Stage1Warp shw[kS1Warps];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Stage1Warp& W = shw[wib];
+    const int k = blockIdx.x * kS1Warps + wib;
     if (k >= A.n) return;
     const SiteD S = A.sites[k];
-    Owner o{S.x, S.y, S.w, k};
-    Work1<kCapSmall> W;
-    Poly<kCapSmall>* P = &W.PA;
-    Poly<kCapSmall>* Q = &W.PB;
-    CellOut c = cell_stage<kCapSmall, false>(A, k, S, o, domain_box(A, o), W.slots, W.map, P, Q);
-    if (c.aborted) return;
-    if (c.st) atomicOr(A.status, c.st & ~ST_NEED_EXACT);
-    if (A.counters) {
-        atomicAdd(&A.counters[0], (unsigned long long)c.popped);
-        atomicAdd(&A.counters[1], (unsigned long long)c.tested);
-        atomicAdd(&A.counters[2], (unsigned long long)c.pruned);
-        atomicAdd(&A.counters[3], (unsigned long long)c.visited);
-        atomicAdd(&A.counters[4], (unsigned long long)c.cuts);
-        atomicAdd(&A.counters[5], (unsigned long long)c.ns);
-    }
-    if (c.overflow) {
-        A.nb_cnt[k] = -2;  // finished by the large-capacity pass
-        A.redo[atomicAdd(A.nredo, 1)] = k;
-        atomicOr(A.status, ST_POLY_OVERFLOW);
-        return;
-    }
-    if (c.empty || P->n == 0) {
-        A.nb_cnt[k] = -1;
-        return;
-    }
-    // the neighbour list by site index (the seeds of the next evaluation set the
-    // order the walk meets them in; the pieces are clipped in list order, so a fixed
-    // order keeps their sums independent of the seeds)
-    int* lab = A.nb_lab + (size_t)k * kCapSmall;
-    for (int s = 0; s < c.ns; s++) {
-        const int v = W.slots[s].site;
-        int r = s - 1;
-        while (r >= 0 && lab[r] > v) {
-            lab[r + 1] = lab[r];
-            r--;
+    const Owner o{S.x, S.y, S.w, k};
+    const int gi = A.perm[k];
+    if (!(isfinite(S.x) && isfinite(S.y) && isfinite(S.w))) {
+        if (lane == 0) {
+            A.nb_cnt[k] = -1;
+            atomicOr(A.status, ST_BAD_INPUT);
+            if (A.abort_flag) atomicExch(A.abort_flag, 1);
         }
-        lab[r + 1] = v;
+        return;
     }
-    A.nb_cnt[k] = c.ns;
-    A.cell_box[k] = cell_box(*P, S, A);
+    // the mesh's bounding box (domain_box's corners), lanes 0..3
+    if (lane < 4) {
+        const double bx = (lane == 0 || lane == 3) ? A.X0 : A.X1;
+        const double by = lane < 2 ? A.Y0 : A.Y1;
+        set_fixed(W.box, lane, bx, by, o);
+    }
+    if (lane == 0) W.box.n = 4;
+    __syncwarp();
+    int n = 4;  // polygon vertices
+    float vx = 0.0f, vy = 0.0f, vr = 0.0f;
+    int vl = 0;
+    if (lane < 4) {
+        vx = W.box.ux[lane];
+        vy = W.box.uy[lane];
+        vr = W.box.ur[lane];
+        vl = -1 - lane;
+        W.pux[lane] = vx;
+        W.puy[lane] = vy;
+        W.pur[lane] = vr;
+        W.plab[lane] = vl;
+    }
+    const float ox = (float)S.x, oy = (float)S.y;
+    const float owh = (float)(0.5 * S.w), oxa = fabsf(ox) + fabsf(oy);
+    int ns = 0;  // slots in use
+    uint32_t st = 0;
+    bool empty = false, overflow = false, aborted = false;
+    int popped = 0, tested = 0, pruned = 0, visited = 0, cuts = 0;
+    __syncwarp();
+
+    // clip the polygon by slot cs: 0 no vertex outside, 1 clipped, 2 nothing left,
+    // 3 beyond capacity or undecided (the cell goes to the large-capacity pass)
+    auto clip = [&](int cs) -> int {
+        const Slot c = W.slot[cs];
+        const bool act = lane < n;
+        const int prevlab = __shfl_sync(kFull, vl, lane == 0 ? n - 1 : lane - 1);
+        bool vout = false, und = false;
+        if (act) {
+            const int t = test32(vx, vy, vr, c);
+            if (t != 0)
+                vout = t > 0;
+            else
+                vout = !sym_inside<kCapSmall, false>(prevlab, vl, W.slot, W.box, o, A.sites, c.site, st, und);
+        }
+        if (__any_sync(kFull, und)) {
+            st |= ST_NEED_EXACT;
+            return 3;
+        }
+        const unsigned om = __ballot_sync(kFull, act && vout);
+        if (om == 0u) return 0;
+        if (__popc(om) == n) return 2;
+        const int v1 = lane + 1 == n ? 0 : lane + 1;
+        const bool in0 = act && !vout, in1 = !((om >> v1) & 1u);
+        const int cnt = act ? (in0 ? (in1 ? 1 : 2) : (in1 ? 1 : 0)) : 0;
+        int pos = cnt;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(kFull, pos, d);
+            if (lane >= d) pos += y;
+        }
+        const int m = __shfl_sync(kFull, pos, 31);
+        pos -= cnt;
+        if (m > 32) return 3;
+        __syncwarp();
+        if (act) {
+            int q = pos;
+            if (in0) {
+                W.pux[q] = vx;
+                W.puy[q] = vy;
+                W.pur[q] = vr;
+                W.plab[q] = vl;
+                q++;
+            }
+            if (in0 != in1) {
+                float nx, ny, nr;
+                new_vertex<kCapSmall>(vl, cs, W.slot, W.box, nx, ny, nr);
+                W.pux[q] = nx;
+                W.puy[q] = ny;
+                W.pur[q] = nr;
+                W.plab[q] = in0 ? cs : vl;
+            }
+        }
+        __syncwarp();
+        n = m;
+        if (lane < n) {
+            vx = W.pux[lane];
+            vy = W.puy[lane];
+            vr = W.pur[lane];
+            vl = W.plab[lane];
+        }
+        __syncwarp();
+        return 1;
+    };
+
+    // keep only the slots the polygon's edges use (compact_slots, a warp at a time)
+    auto compact = [&]() {
+        const unsigned lo = __reduce_or_sync(kFull, (lane < n && vl >= 0 && vl < 32) ? (1u << vl) : 0u);
+        const unsigned hi = __reduce_or_sync(kFull, (lane < n && vl >= 32) ? (1u << (vl - 32)) : 0u);
+        const bool u0 = lane < ns && ((lo >> lane) & 1u), u1 = lane + 32 < ns && ((hi >> lane) & 1u);
+        Slot a0, a1;
+        if (u0) a0 = W.slot[lane];
+        if (u1) a1 = W.slot[lane + 32];
+        __syncwarp();
+        const unsigned below = (1u << lane) - 1u;
+        if (u0) W.slot[__popc(lo & below)] = a0;
+        if (u1) W.slot[__popc(lo) + __popc(hi & below)] = a1;
+        if (lane < n && vl >= 0)
+            vl = vl < 32 ? __popc(lo & ((1u << vl) - 1u)) : __popc(lo) + __popc(hi & ((1u << (vl - 32)) - 1u));
+        if (lane < n) W.plab[lane] = vl;
+        ns = __popc(lo) + __popc(hi);
+        __syncwarp();
+    };
+
+    // clip by the sites list[0..cnt): 32 at a time, the ones that may cut in list order
+    auto try_sites = [&](const int* list, int cnt) {
+        for (int c0 = 0; c0 < cnt && !empty && !overflow; c0 += 32) {
+            const int j = c0 + lane;
+            bool cut = false, kill = false;
+            Slot sl;
+            int q = j < cnt ? list[j] : -1;
+            // a site already clipped against (a seed met again): its radical axis carries
+            // polygon vertices, where the side tests would be exactly tied
+            for (int t = 0; t < ns && q >= 0; t++)
+                if (W.slot[t].site == q) q = -1;
+            if (q >= 0) {
+                const SiteD C = A.sites[q];
+                if (C.x == S.x && C.y == S.y) {
+                    // coincident sites: the larger weight, then the lower index, keeps the cell
+                    const int gj = A.perm[q];
+                    kill = C.w > S.w || (C.w == S.w && gj < gi);
+                } else {
+                    sl = make_slot(q, C, o);
+                    for (int v = 0; v < n && !cut; v++) cut = test32(W.pux[v], W.puy[v], W.pur[v], sl) >= 0;
+                }
+            }
+            if (__any_sync(kFull, kill)) {
+                empty = true;
+                break;
+            }
+            unsigned cm = __ballot_sync(kFull, cut);
+            visited += __popc(cm);
+            while (cm) {
+                const int src = __ffs(cm) - 1;
+                cm &= cm - 1;
+                if (ns == kCapSmall) {
+                    compact();
+                    if (ns == kCapSmall) {
+                        overflow = true;
+                        break;
+                    }
+                }
+                if (lane == src) W.slot[ns] = sl;
+                __syncwarp();
+                const int r = clip(ns);
+                if (r == 1) {
+                    ns++;
+                    cuts++;
+                } else if (r == 2) {
+                    empty = true;
+                    break;
+                } else if (r == 3) {
+                    overflow = true;
+                    break;
+                }
+            }
+        }
+    };
+
+    // 1. seeds
+    int nseed = 0;
+    if (A.prev_valid) {
+        const int c = A.nb_cnt[k];
+        if (c > 0 && c <= kSeedCap) nseed = c;
+    }
+    const bool windowed = nseed == 0;
+    int wlo = 0, whi = -1;
+    int ccount;  // candidates waiting in the list (the seeds first, then W.cand)
+    if (windowed) {
+        wlo = max(k - kS1Window, 0);
+        whi = min(k + kS1Window, A.n - 1);
+        for (int q = wlo + lane; q <= whi; q += 32)
+            if (q != k) W.seed[q - wlo - (q > k ? 1 : 0)] = q;
+        ccount = whi - wlo;  // the window without k
+    } else {
+        for (int j = lane; j < nseed; j += 32) W.seed[j] = A.nb_lab[(size_t)k * kSeedCap + j];
+        ccount = nseed;
+    }
+    __syncwarp();
+    auto is_seed = [&](int q) -> bool {
+        if (windowed) return q >= wlo && q <= whi;
+        int lo = 0, hi = nseed - 1;  // the previous list is sorted by site index
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (W.seed[mid] < q)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        return W.seed[lo] == q;
+    };
+
+    // 2. the site tree, a batch of up to 32 nodes after each list of candidates
+    int sp = -1;  // -1: the walk has not started
+    const int* clist = W.seed;
+    for (;;) {
+        if (ccount) try_sites(clist, ccount);
+        if (empty || overflow) break;
+        clist = W.cand;
+        ccount = 0;
+        if (sp < 0) {
+            sp = 0;
+            if (A.tree.n >= 2) {
+                if (lane == 0) {
+                    int cur = (int)(0x80000000u | (unsigned)k);
+                    int p = A.tree.leaf_parent[k];
+                    while (p >= 0 && sp < kS1Stack) {
+                        const int2 ch = A.tree.child[p];
+                        W.stack[sp++] = ch.x == cur ? ch.y : ch.x;
+                        cur = p;
+                        p = A.tree.parent[p];
+                    }
+                    if (p >= 0) sp = -1;
+                }
+                sp = __shfl_sync(kFull, sp, 0);
+                __syncwarp();
+                if (sp < 0) {
+                    overflow = true;
+                    break;
+                }
+                if (windowed) {
+                    // Without a previous list the window leaves the polygon far from the
+                    // cell; before the walk, every sibling subtree of the path gives the
+                    // sites it holds nearest the site: a lane descends it, taking the child
+                    // whose box is nearer each time, down to a leaf or a small node.  The
+                    // walk visits these sites again and finds them harmless.
+                    int clo = 0, ccnt = 0;
+                    if (lane < min(sp, 32)) {
+                        int c = W.stack[sp - 1 - lane];
+                        for (;;) {
+                            if (c < 0) {
+                                clo = c & 0x7fffffff;
+                                ccnt = 1;
+                                break;
+                            }
+                            const int2 rg = A.tree.range[c];
+                            if (rg.y - rg.x < kS1Bucket) {
+                                clo = rg.x;
+                                ccnt = rg.y - rg.x + 1;
+                                break;
+                            }
+                            const int2 ch = A.tree.child[c];
+                            float d0, d1;
+                            if (ch.x < 0) {
+                                const float2 q = A.tree.posf[ch.x & 0x7fffffff];
+                                d0 = (q.x - ox) * (q.x - ox) + (q.y - oy) * (q.y - oy);
+                            } else {
+                                const float4 b = A.tree.boxf[ch.x];
+                                const float dx = fmaxf(fmaxf(b.x - ox, ox - b.z), 0.0f);
+                                const float dy = fmaxf(fmaxf(b.y - oy, oy - b.w), 0.0f);
+                                d0 = dx * dx + dy * dy;
+                            }
+                            if (ch.y < 0) {
+                                const float2 q = A.tree.posf[ch.y & 0x7fffffff];
+                                d1 = (q.x - ox) * (q.x - ox) + (q.y - oy) * (q.y - oy);
+                            } else {
+                                const float4 b = A.tree.boxf[ch.y];
+                                const float dx = fmaxf(fmaxf(b.x - ox, ox - b.z), 0.0f);
+                                const float dy = fmaxf(fmaxf(b.y - oy, oy - b.w), 0.0f);
+                                d1 = dx * dx + dy * dy;
+                            }
+                            c = d0 <= d1 ? ch.x : ch.y;
+                        }
+                    }
+                    int cpos = ccnt;
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const int y = __shfl_up_sync(kFull, cpos, d);
+                        if (lane >= d) cpos += y;
+                    }
+                    ccount = __shfl_sync(kFull, cpos, 31);
+                    cpos -= ccnt;
+                    for (int q = 0; q < ccnt; q++) W.cand[cpos + q] = clo + q;
+                    __syncwarp();
+                    continue;
+                }
+            }
+        }
+        if (sp == 0) break;
+        if (A.abort_flag) {
+            const int f = lane == 0 ? *(volatile const int*)A.abort_flag : 0;
+            if (__shfl_sync(kFull, f, 0)) {
+                aborted = true;
+                break;
+            }
+        }
+        const int nb = min(sp, 32);
+        sp -= nb;
+        const bool have = lane < nb;
+        const int nd = have ? W.stack[sp + lane] : 0;
+        __syncwarp();
+        popped += nb;
+        int npush = 0, c0 = 0, c1 = 0, clo = 0, ccnt = 0;
+        bool test = false, prune = false;
+        if (have) {
+            if (nd < 0) {
+                clo = nd & 0x7fffffff;
+                ccnt = 1;
+            } else {
+                // every node here lies outside the path to site k
+                const int2 rg = A.tree.range[nd];
+                const int2 ch = A.tree.child[nd];
+                const float4 nbf = A.tree.boxf[nd];
+                const float4 nnk = A.tree.nk[nd];
+                test = true;
+                prune = node_harmless_v(W.pux, W.puy, W.pur, n, ox, oy, owh, oxa, nbf, nnk);
+                if (!prune) {
+                    if (rg.y - rg.x < kS1Bucket) {
+                        clo = rg.x;
+                        ccnt = rg.y - rg.x + 1;
+                    } else {
+                        npush = 2;
+                        c0 = ch.x;
+                        c1 = ch.y;
+                    }
+                }
+            }
+        }
+        tested += __popc(__ballot_sync(kFull, test));
+        pruned += __popc(__ballot_sync(kFull, prune));
+        // children onto the stack
+        int pos = npush;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(kFull, pos, d);
+            if (lane >= d) pos += y;
+        }
+        const int tot = __shfl_sync(kFull, pos, 31);
+        pos -= npush;
+        if (sp + tot > kS1Stack) {
+            overflow = true;
+            break;
+        }
+        if (npush) {
+            W.stack[sp + pos] = c1;
+            W.stack[sp + pos + 1] = c0;
+        }
+        sp += tot;
+        // the candidate sites, without the seeds already clipped
+        unsigned cmask = 0;
+        for (int q = 0; q < ccnt; q++)
+            if (!is_seed(clo + q)) cmask |= 1u << q;
+        const int cn = __popc(cmask);
+        int cpos = cn;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(kFull, cpos, d);
+            if (lane >= d) cpos += y;
+        }
+        ccount = __shfl_sync(kFull, cpos, 31);
+        cpos -= cn;
+        for (int q = 0; q < ccnt; q++)
+            if ((cmask >> q) & 1u) W.cand[cpos++] = clo + q;
+        __syncwarp();
+    }
+
+    if (aborted) return;
+    if (A.counters && lane == 0) {
+        atomicAdd(&A.counters[0], (unsigned long long)popped);
+        atomicAdd(&A.counters[1], (unsigned long long)tested);
+        atomicAdd(&A.counters[2], (unsigned long long)pruned);
+        atomicAdd(&A.counters[3], (unsigned long long)visited);
+        atomicAdd(&A.counters[4], (unsigned long long)cuts);
+    }
+    const uint32_t sto = st & ~(uint32_t)ST_NEED_EXACT;
+    if (sto && lane == 0) atomicOr(A.status, sto);
+    if (empty) {
+        if (lane == 0) {
+            A.nb_cnt[k] = -1;
+            if (A.abort_flag) atomicExch(A.abort_flag, 1);
+        }
+        return;
+    }
+    if (overflow) {
+        if (lane == 0) {
+            A.nb_cnt[k] = -2;  // finished by the large-capacity pass
+            A.redo[atomicAdd(A.nredo, 1)] = k;
+            atomicOr(A.status, ST_POLY_OVERFLOW);
+        }
+        return;
+    }
+    compact();
+    if (A.counters && lane == 0) atomicAdd(&A.counters[5], (unsigned long long)ns);
+    // the neighbour list by site index (the pieces are clipped in list order, so a
+    // fixed order keeps their sums independent of the order of the walk)
+    const int s0 = lane < ns ? W.slot[lane].site : INT_MAX;
+    const int s1 = lane + 32 < ns ? W.slot[lane + 32].site : INT_MAX;
+    int r0 = 0, r1 = 0;
+    for (int j = 0; j < 32; j++) {
+        const int a = __shfl_sync(kFull, s0, j), b = __shfl_sync(kFull, s1, j);
+        r0 += (a < s0) + (b < s0);
+        r1 += (a < s1) + (b < s1);
+    }
+    int* lab = A.nb_lab + (size_t)k * kCapSmall;
+    if (lane < ns) lab[r0] = s0;
+    if (lane + 32 < ns) lab[r1] = s1;
+    // the cell's conservative absolute bounding box (cell_box)
+    float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+    if (lane < n) {
+        const float r = vr * 1.0001f;
+        mnx = vx - r;
+        mxx = vx + r;
+        mny = vy - r;
+        mxy = vy + r;
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(kFull, mnx, d));
+        mny = fminf(mny, __shfl_xor_sync(kFull, mny, d));
+        mxx = fmaxf(mxx, __shfl_xor_sync(kFull, mxx, d));
+        mxy = fmaxf(mxy, __shfl_xor_sync(kFull, mxy, d));
+    }
+    if (lane == 0) {
+        A.nb_cnt[k] = ns;
+        if (!(mxx - mnx < INFINITY && mxy - mny < INFINITY)) {
+            A.cell_box[k] = make_double4(A.X0, A.Y0, A.X1, A.Y1);
+        } else {
+            const double sx = fmax(fabs((double)mnx), fabs((double)mxx)), sy = fmax(fabs((double)mny), fabs((double)mxy));
+            A.cell_box[k] = make_double4(S.x + (double)mnx - 1e-6 * sx - 1e-300, S.y + (double)mny - 1e-6 * sy - 1e-300,
+                                         S.x + (double)mxx + 1e-6 * sx + 1e-300, S.y + (double)mxy + 1e-6 * sy + 1e-300);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1210,7 +1640,7 @@ int stage1_cap() { return kCapSmall; }
 void launch_cells_stage1(const CellArgs& a, cudaStream_t s)
 {
     if (a.n <= 0) return;
-    k_cells_stage1<<<(a.n + 127) / 128, 128, 0, s>>>(a);
+    k_cells_stage1<<<(a.n + kS1Warps - 1) / kS1Warps, 32 * kS1Warps, 0, s>>>(a);
 }
 
 static unsigned pieces_blocks(int n)

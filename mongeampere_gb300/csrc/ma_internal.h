@@ -21,6 +21,8 @@ struct SiteTree {
     const float4* nk;     // the same about the FP32 box centre c: A = alpha + beta.c - |c|^2/2
                           // (rounded down), beta_x - c_x, beta_y - c_y, 0
     const float2* posf;   // sorted site positions (FP32)
+    const int* parent;      // parent of each internal node (-1 at the root)
+    const int* leaf_parent; // parent of each leaf
 };
 
 // implicit grid mesh: vertex (i, j) at (gx[i], gy[j]) with value val[j * nx + i];

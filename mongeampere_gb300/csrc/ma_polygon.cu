@@ -204,6 +204,8 @@ ma_status ma_polygon_cells(ma_ctx* cp, int64_t n, const double* x, const double*
     a.tree.ab = c->t_ab.as<double4>();
     a.tree.nk = c->t_nk.as<float4>();
     a.tree.posf = c->posf.as<float2>();
+    a.tree.parent = c->t_parent.as<int>();
+    a.tree.leaf_parent = c->t_leaf_parent.as<int>();
     a.X0 = X0;
     a.Y0 = Y0;
     a.X1 = X1;

@@ -63,9 +63,9 @@ __device__ __forceinline__ void compact_slots(Poly<CAP>& P, Slot* slots, int* ma
 // whose terms are all small where the test is close; x_i - beta = d - g.  The box enters
 // relative to the FP32 site position, with the conversion errors absorbed into a wider
 // box.
-template <int CAP>
-__device__ __forceinline__ bool node_harmless(const Poly<CAP>& P, float ox, float oy, float owh, float oxa,
-                                              const float4 bf, const float4 nk)
+__device__ __forceinline__ bool node_harmless_v(const float* pux, const float* puy, const float* pur, int pn,
+                                                float ox, float oy, float owh, float oxa, const float4 bf,
+                                                const float4 nk)
 {
     if (!(nk.x > -INFINITY)) return false;
     const float ccx = 0.5f * (bf.x + bf.z), ccy = 0.5f * (bf.y + bf.w);
@@ -84,14 +84,21 @@ __device__ __forceinline__ bool node_harmless(const Poly<CAP>& P, float ox, floa
     hy = hy * 1.000001f + wy;
     const float L = fabsf(cx) + fabsf(cy) + hx + hy;
     const float e0 = 1.2e-7f * (fabsf(fex) + fabsf(fey) + sd + sg + 2.0f * oxa);
-    for (int v = 0; v < P.n; v++) {
-        float qx = fex + P.ux[v], qy = fey + P.uy[v];
+    for (int v = 0; v < pn; v++) {
+        float qx = fex + pux[v], qy = fey + puy[v];
         float T = qx * cx + qy * cy + fabsf(qx) * hx + fabsf(qy) * hy - fK;
         float S = fabsf(qx * cx) + fabsf(qy * cy) + fabsf(qx) * hx + fabsf(qy) * hy + fabsf(fK);
-        float err = 1e-6f * S + (P.ur[v] + e0) * L * 1.0001f + fke + 1e-36f;
+        float err = 1e-6f * S + (pur[v] + e0) * L * 1.0001f + fke + 1e-36f;
         if (!(T + err < 0.0f)) return false;
     }
     return true;
+}
+
+template <int CAP>
+__device__ __forceinline__ bool node_harmless(const Poly<CAP>& P, float ox, float oy, float owh, float oxa,
+                                              const float4 bf, const float4 nk)
+{
+    return node_harmless_v(P.ux, P.uy, P.ur, P.n, ox, oy, owh, oxa, bf, nk);
 }
 
 // ---------------------------------------------------------------------------
