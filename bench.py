@@ -204,70 +204,78 @@ def run_reference(args, rank):
 
 
 def run_c3(args, ctx, dev, rank):
-    """Mixed precision against FP64 at 1M sites: (a) complete Laguerre evaluations of the
-    clustered 1M-site / 2048^2 workload (workloads.c3) at w = 0 -- evaluations/s and the
-    mixed form's mass and Hessian errors against the FP64 form; (b) one OT solve to max
-    relative mass error 1e-6 of 1M uniform sites on the same density (the clustered
-    sites stall the reference's damped Newton from w = 0: every step is cut to 2^-11 to
-    keep all cells non-empty), wall clock of each form and the FP64-evaluated error."""
+    """Mixed precision against FP64 on the clustered 1M-site workload (workloads.c3:
+    2048^2 grid U[0.5,1.5], 1,000,000 sites, 70% in 20 Gaussian blobs, equal masses):
+    (a) complete Laguerre evaluations at w = 0, evaluations/s of each form; (b) one
+    complete OT solve of each form from w = 0 to max relative mass error 1e-6, by the
+    continuation in the target masses (MA_INIT_CONTINUATION: the reference's damped
+    Newton from w = 0 cuts every step to a few 2^-11 on these sites), each timed with its
+    own clock record; (c) the mixed solution's errors against the FP64 evaluation (which
+    the tests pin to the oracle at this size): weights, masses and every Hessian entry."""
     import numpy as np
     import torch
 
     from mongeampere_gb300 import api
     from mongeampere_gb300 import workloads as W
-    out = {"metric": METRIC, "workload": "c3", "n_gpus": 1}
+    out = {"metric": METRIC, "workload": "c3", "n_gpus": 1,
+           "config": "1,000,000 sites (70% in 20 Gaussian blobs), 2048^2 grid U[0.5,1.5], equal masses, "
+                     "inputs in device memory"}
     p = W.c3(0)
     dm = ctx.mesh(p.mesh)
     X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
-    w = torch.zeros(p.n, dtype=torch.float64, device=dev)
-    res = {}
+    nu = torch.tensor(p.nu, device=dev)
+    w0 = torch.zeros(p.n, dtype=torch.float64, device=dev)
+    ev = {}
     for prec in ("fp64", "mixed"):
-        for _ in range(args.warmup):
-            api.kantorovich(dm, X, w, precision=prec, ctx=ctx)
+        for _ in range(max(args.warmup, 1)):
+            api.kantorovich(dm, X, w0, precision=prec, ctx=ctx)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record()
         for _ in range(args.steps):
-            v, g, h = api.kantorovich(dm, X, w, precision=prec, ctx=ctx)
+            api.kantorovich(dm, X, w0, precision=prec, ctx=ctx)
         e1.record()
         torch.cuda.synchronize()
-        res[prec] = (args.steps / (e0.elapsed_time(e1) * 1e-3), v, g.cpu().numpy(), h)
-    g64, g32 = res["fp64"][2], res["mixed"][2]
-    rel = np.abs(g32 - g64) / np.maximum(g64, 1e-300)
-    h64, h32 = res["fp64"][3], res["mixed"][3]
-    hrel = np.abs(h32.val - h64.val) / np.maximum(np.abs(h64.val), 1e-300)
-    out["evaluations"] = {
-        "config": "1,000,000 sites (70% in 20 Gaussian blobs), 2048^2 grid U[0.5,1.5], w = 0, masses + value + CSR Hessian",
-        "fp64_evals_per_s": res["fp64"][0], "mixed_evals_per_s": res["mixed"][0],
-        "mixed_mass_rel_err_max": float(rel.max()), "mixed_mass_rel_err_median": float(np.median(rel)),
-        "mixed_value_rel_err": float(abs(res["mixed"][1] - res["fp64"][1]) / abs(res["fp64"][1])),
-        "mixed_hessian_rel_err_max": float(hrel.max()), "same_sparsity": bool(np.array_equal(h32.col, h64.col))}
-    q = W.make_problem(2048, 1_000_000, "uniform", "uniform", "equal", seed=0)
-    dq = ctx.mesh(q.mesh)
-    xq = torch.tensor(q.x, device=dev)
-    yq = torch.tensor(q.y, device=dev)
-    nq = torch.tensor(q.nu, device=dev)
-    solves = {}
+        ev[prec] = args.steps / (e0.elapsed_time(e1) * 1e-3)
+    out["evaluations_at_w0"] = {"fp64_evals_per_s": ev["fp64"], "mixed_evals_per_s": ev["mixed"],
+                                "mixed_speedup": ev["mixed"] / ev["fp64"]}
+    solves, wsol = {}, {}
     for prec in ("fp64", "mixed"):
-        times = []
-        for k in range(max(1, args.steps // 2) + 1):
-            wq = torch.zeros(q.n, dtype=torch.float64, device=dev)
-            st = api.Statistics()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record()
-            api.ot_solve(dq, xq, nq, x=wq, y=yq, eps_g=1e-6, stop="rel", precision=prec, stats=st, ctx=ctx)
-            e1.record()
-            torch.cuda.synchronize()
-            if k > 0:
-                times.append(e0.elapsed_time(e1) * 1e-3)
-        v, g, _ = api.kantorovich(dq, torch.stack([xq, yq], 1), wq, ctx=ctx)
-        err = float(np.max(np.abs(g.cpu().numpy() - q.nu) / q.nu))
-        solves[prec] = {"s_per_solve": float(np.median(times)), "newton_iters": st.niter, "evals": st.neval,
-                        "fp64_evals": st.neval_fp64, "cg_iters": st.cg_iters, "max_rel_err_fp64": err}
-    out["solve_1M_uniform"] = {
-        "config": "1,000,000 uniform sites, 2048^2 grid U[0.5,1.5], equal masses, from w = 0 to max rel mass err 1e-6",
-        **solves, "mixed_speedup": solves["fp64"]["s_per_solve"] / solves["mixed"]["s_per_solve"]}
+        w = torch.zeros(p.n, dtype=torch.float64, device=dev)
+        st = api.Statistics()
+        clocks = ClockSampler(0)
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record()
+        api.ot_solve(dm, X, nu, x=w, eps_g=1e-6, stop="rel", precision=prec, init="continuation", maxiter=300,
+                     stats=st, ctx=ctx)
+        e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        clk = clocks.stop()
+        secs = e0.elapsed_time(e1) * 1e-3
+        wsol[prec] = w
+        solves[prec] = {"seconds": secs, "solves_per_s": 1.0 / secs, "wall_s": wall, "newton_iters": st.niter,
+                        "evals": st.neval, "fp64_evals": st.neval_fp64, "cg_iters": st.cg_iters,
+                        "linesearch_halvings": st.linesearch_halvings, "max_rel_err": st.max_rel_err,
+                        "eval_ms": st.t_eval_ms, "linsolve_ms": st.t_linsolve_ms, "clocks": clk}
+    # the mixed solution, evaluated in FP64
+    v64, g64, h64 = api.kantorovich(dm, X, wsol["mixed"], ctx=ctx)
+    v32, g32, h32 = api.kantorovich(dm, X, wsol["mixed"], precision="mixed", ctx=ctx)
+    g64n, g32n = g64.cpu().numpy(), g32.cpu().numpy()
+    wm, wd = wsol["mixed"].cpu().numpy(), wsol["fp64"].cpu().numpy()
+    same = bool(np.array_equal(h32.col, h64.col))
+    hrel = float(np.max(np.abs(h32.val - h64.val) / np.abs(h64.val))) if same else None
+    out["solve"] = {"fp64": solves["fp64"], "mixed": solves["mixed"],
+                    "mixed_speedup": solves["fp64"]["seconds"] / solves["mixed"]["seconds"],
+                    "mixed_solution_fp64_mass_rel_err_max": float(np.max(np.abs(g64n - p.nu) / p.nu)),
+                    "mixed_vs_fp64_weights_max_abs_diff": float(np.max(np.abs(wm - wd))),
+                    "weights_scale": float(np.max(np.abs(wd))),
+                    "mixed_eval_mass_rel_err_max": float(np.max(np.abs(g32n - g64n) / g64n)),
+                    "mixed_eval_value_rel_err": float(abs(v32 - v64) / abs(v64)),
+                    "mixed_eval_hessian_entry_rel_err_max": hrel, "same_sparsity": same}
     if rank == 0:
         print(json.dumps(out))
 
@@ -402,8 +410,8 @@ def main():
     ap.add_argument("--profile-solve", action="store_true",
                     help="profiling driver: one solve with per-kernel device times (no benchmark line)")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
-                    help="c3: the 1M-site mixed-precision comparison (evaluations of the clustered "
-                         "1M-site / 2048^2 workload, and a 1M-uniform-site solve); c5: 512 independent "
+                    help="c3: the 1M-site mixed-precision comparison on the clustered 1M-site / 2048^2 "
+                         "workload (evaluations, and complete solves of each form); c5: 512 independent "
                          "problems, batched against sequential solves; one JSON line each; c1 (the "
                          "reference's own 64^2 / 1,000-site case): the reference arm only")
     args = ap.parse_args()

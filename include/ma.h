@@ -114,6 +114,9 @@ typedef struct ma_profile {
                                  capacity and ran with the diagonal preconditioner */
     double amg_setup_ms;      /* multigrid hierarchy: fine matrix, aggregation, Galerkin levels */
     int64_t amg_levels;       /* levels of the last hierarchy */
+    int64_t mixed[4];         /* mixed-precision evaluations: pieces integrated, cells redone in
+                                 FP64 (their certified FP32 mass error above 2^-14), radical-axis
+                                 edges, edges integrated in FP64 */
 } ma_profile;
 /* enable != 0: reset the profile and start recording; 0: stop. */
 ma_status ma_ctx_profile(ma_ctx* ctx, int enable);
@@ -163,10 +166,16 @@ typedef enum ma_precond {
 
 typedef enum ma_init {
     MA_INIT_GIVEN = 0,      /* start from w_inout (the reference's behaviour; zeros = its empty start) */
-    MA_INIT_MULTISCALE = 1  /* coarse-to-fine initial guess: sites aggregated by 8 in Morton order
+    MA_INIT_MULTISCALE = 1, /* coarse-to-fine initial guess: sites aggregated by 8 in Morton order
                                down to ~4,000, each level solved to 1e-2 relative from its parent's
                                weights (no counterpart in the reference, whose ot_solve takes the
-                               initial guess as an argument); for clustered sites far from equilibrium */
+                               initial guess as an argument); for sites near a uniform spread */
+    MA_INIT_CONTINUATION = 2 /* continuation in the target masses from those of w_inout: stages
+                               nu_t = m(w_in) + t (nu - m(w_in)), no cell's target changing by more
+                               than 2x between stages, each the reference's damped Newton to 1e-2
+                               relative (at most 5 * maxiter steps), the last one to the caller's
+                               rule; no counterpart in the reference.  For sites far from equilibrium
+                               (clustered sites), where the damped Newton from w_inout stalls */
 } ma_init;
 
 typedef struct ma_solve_opts {

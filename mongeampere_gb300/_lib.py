@@ -44,7 +44,7 @@ class MaProfile(ctypes.Structure):
                 ("pcg_ms", ctypes.c_double), ("pcg_launches", ctypes.c_int64), ("pcg_iters", ctypes.c_int64),
                 ("large_sites", ctypes.c_int64), ("search", ctypes.c_int64 * 6),
                 ("amg_fallbacks", ctypes.c_int64), ("amg_setup_ms", ctypes.c_double),
-                ("amg_levels", ctypes.c_int64)]
+                ("amg_levels", ctypes.c_int64), ("mixed", ctypes.c_int64 * 4)]
 
 
 # every symbol include/ma.h declares, with its ctypes signature
@@ -145,3 +145,4 @@ MA_PRECOND_MULTIGRID = 0
 MA_PRECOND_JACOBI = 1
 MA_INIT_GIVEN = 0
 MA_INIT_MULTISCALE = 1
+MA_INIT_CONTINUATION = 2

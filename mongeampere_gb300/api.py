@@ -88,6 +88,7 @@ class Context:
         _check(self.lib, self.h, self.lib.ma_ctx_profile_read(self.h, ctypes.byref(p)), "ma_ctx_profile_read")
         out = {f: getattr(p, f) for f, _ in L.MaProfile._fields_}
         out["search"] = list(out["search"])
+        out["mixed"] = list(out["mixed"])
         return out
 
     def mesh(self, mesh) -> "DeviceMesh":
@@ -430,7 +431,8 @@ def ot_solve(mesh, X, masses, x=None, eps_g: float = 1e-7, maxiter: int = 100, v
     or a wrong-sized array starts from zero like the reference).  ``stop="rel"``
     uses ``max_i |m_i - nu_i| / nu_i <= eps_g`` instead of ``|m - nu|_2 < eps_g``.
     ``precond`` is the CG preconditioner of the Newton step: "multigrid" or "jacobi".
-    ``init="multiscale"`` replaces the initial guess by a coarse-to-fine one."""
+    ``init="multiscale"`` replaces the initial guess by a coarse-to-fine one;
+    ``init="continuation"`` reaches the targets in stages from the masses of ``x``."""
     ctx = ctx or default_context()
     dm = _dmesh(ctx, mesh)
     xs, ys = _split_xy(X, y)
@@ -458,9 +460,10 @@ def ot_solve(mesh, X, masses, x=None, eps_g: float = 1e-7, maxiter: int = 100, v
     if precond not in ("multigrid", "jacobi"):
         raise ValueError("precond must be 'multigrid' or 'jacobi'")
     o.precond = L.MA_PRECOND_JACOBI if precond == "jacobi" else L.MA_PRECOND_MULTIGRID
-    if init not in ("given", "multiscale"):
-        raise ValueError("init must be 'given' or 'multiscale'")
-    o.init = L.MA_INIT_MULTISCALE if init == "multiscale" else L.MA_INIT_GIVEN
+    inits = {"given": L.MA_INIT_GIVEN, "multiscale": L.MA_INIT_MULTISCALE, "continuation": L.MA_INIT_CONTINUATION}
+    if init not in inits:
+        raise ValueError("init must be 'given', 'multiscale' or 'continuation'")
+    o.init = inits[init]
     s = L.MaStats()
     st = ctx.lib.ma_ot_solve(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], wp, a.mem, ctypes.byref(o),
                              ctypes.byref(s))

@@ -252,8 +252,8 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         a.abort_flag = c->abortf.as<int>();
     }
     if (c->prof) {
-        MA_CUDA(c, c->counters.ensure(8 * sizeof(unsigned long long)));
-        MA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), s));
+        MA_CUDA(c, c->counters.ensure(12 * sizeof(unsigned long long)));
+        MA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 12 * sizeof(unsigned long long), s));
         a.counters = c->counters.as<unsigned long long>();
     }
     a.nb_cnt = c->nb_cnt.as<int>();
@@ -381,9 +381,10 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
             return fail(c, MA_ERR_CAPACITY, "a Laguerre cell has more vertices than the largest kernel capacity");
     }
     if (a.counters) {
-        unsigned long long cnt[8];
+        unsigned long long cnt[12];
         MA_CUDA(c, cudaMemcpy(cnt, a.counters, sizeof(cnt), cudaMemcpyDeviceToHost));
         for (int q = 0; q < 6; q++) c->profile.search[q] += (int64_t)cnt[q];
+        for (int q = 0; q < 4; q++) c->profile.mixed[q] += (int64_t)cnt[6 + q];
     }
     uint32_t stbits = (uint32_t)c->hinfo[1];
     c->prev_valid = true;

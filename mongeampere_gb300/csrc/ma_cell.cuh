@@ -616,28 +616,6 @@ MA_HD void integrate_labels(int n, const Lab& lab_of, const Nb64* nb, const Fixe
 // ---------------------------------------------------------------------------
 // the mixed-precision integrals (FP32)
 // ---------------------------------------------------------------------------
-// FP32 vertex between edges prev and cur from the FP32 slot data, with its certified
-// per-component error radius R (the positions and radii of the clip: a fixed corner,
-// vtx_fixed_bis or vtx_bis_bis)
-MA_HD void vtx32r(int prev, int cur, const Slot* slots, const Fixed& fx, float& X, float& Y, float& R)
-{
-    if (prev < 0 && cur < 0) {
-        const int e = -1 - cur;
-        X = fx.ux[e];
-        Y = fx.uy[e];
-        R = fx.ur[e];
-        return;
-    }
-    if (prev >= 0 && cur >= 0) {
-        vtx_bis_bis(slots[prev], slots[cur], X, Y, R);
-        return;
-    }
-    if (prev < 0)
-        vtx_fixed_bis(fx, -1 - prev, slots[cur], X, Y, R);
-    else
-        vtx_fixed_bis(fx, -1 - cur, slots[prev], X, Y, R);
-}
-
 // FP32 sum with a running compensation (Neumaier's variant of Kahan summation): the
 // rounding error of every addition is carried in c, so the sum's error does not grow
 // with the number of terms
@@ -652,67 +630,145 @@ struct CompF {
     MA_HD float val() const { return s + c; }
 };
 
-// An FP32 radical-axis edge integral is kept when the error radii of its two ends are
-// below kEdgeTol32 / 2 of its length |dx| + |dy|; otherwise the edge is redone in FP64.
-// With crs = |e x d| = |e| |d| and |e| >= (|dx| + |dy|) / sqrt 2, the edge's relative
-// error is then below kEdgeTol32 plus a few FP32 roundings: every Hessian entry is a sum
-// of such edges of one sign, so each entry is within ~2.5e-4 of the FP64 one.
+// The mixed-precision integrals of one piece.  Every position is taken about an anchor
+// a near the cell (the centre of its bounding box, site-relative FP64): a cell can lie
+// many cell sizes away from its site, and FP32 positions relative to the site would
+// carry errors of 1e-7 of that distance.  The FP64 work is the triangle's corners minus
+// the anchor, per piece, and each radical axis's offset about the anchor, once per cell
+// and neighbour (zc): the axis {u : 2 u.d = z} becomes {v : 2 v.d = z - 2 a.d}.  The vertices come from the
+// certified FP32 constructions (vtx_fixed_bis, vtx_bis_bis: a value and an error radius
+// R), the fan sums are compensated FP32 sums.  The certified radii give two bounds:
+//   err_mass: the piece's mass moves by at most 1/2 sum over its edges of
+//   (R_a + R_b) |e|_1 times the largest density on it; the caller sums these per cell and
+//   redoes in FP64 a cell whose total exceeds kMassTol32 of its mass;
+//   a radical-axis edge is integrated in FP64 (vtx64, site-relative) when 2 (R_a + R_b)
+//   exceeds kEdgeTol32 of its length |e|_1: crs = |e x d| = |e| |d| with
+//   |e| >= |e|_1 / sqrt 2, so a kept edge is within kEdgeTol32 plus a few FP32 roundings,
+//   and every Hessian entry, a sum of edges of one sign, within ~2.5e-4 of the FP64 one.
+constexpr float kMassTol32 = 0x1p-14f;
 constexpr float kEdgeTol32 = 0x1p-12f;
 
-// integrate_labels (mass, value part, Hessian edges; no moments) in FP32 from the
-// FP32 vertices, with compensated fan sums; the caller sums the pieces of a cell in
-// FP64.  The Hessian part of an edge comes from FP32 vertices when their certified
-// radii allow (kEdgeTol32), else from the FP64 vertices of vtx64 (nb, fx.rx / ry): short
-// edges, whose FP32 ends cancel, are the ones that need it.
-template <class Lab, class Edge>
-MA_HD void integrate_labels32(int n, const Lab& lab_of, const Slot* slots, const Nb64* nb, const Fixed& fx, double c0,
-                              double gx, double gy, float& mass, float& second, const Edge& edge)
+// a triangle's corners about the anchor (FP32 values and error radii)
+struct FixedA {
+    int n;
+    float ux[3], uy[3], ur[3];
+};
+
+// the vertex between edges prev and cur about the anchor, with its error radius
+MA_HD void vtx_anchor(int prev, int cur, const Slot* slots, const float* zc, const FixedA& fa, float& X, float& Y,
+                      float& R)
 {
-    const float c0f = (float)c0, gxf = (float)gx, gyf = (float)gy;
-    float x0, y0, r0;
-    vtx32r(lab_of(n - 1), lab_of(0), slots, fx, x0, y0, r0);
-    float ax = x0, ay = y0, ar = r0;
-    CompF m0{0, 0}, m1x{0, 0}, m1y{0, 0}, q2{0, 0}, c3x{0, 0}, c3y{0, 0};
-    for (int k = 0; k < n; k++) {
-        const int lab = lab_of(k);
+    auto slot_at = [&](int lab) -> Slot {
+        Slot t = slots[lab];
+        t.z = zc[lab];
+        t.ez = kU32 * fabsf(t.z) + 1e-37f;
+        return t;
+    };
+    if (prev < 0 && cur < 0) {
+        const int e = -1 - cur;
+        X = fa.ux[e];
+        Y = fa.uy[e];
+        R = fa.ur[e];
+    } else if (prev >= 0 && cur >= 0) {
+        vtx_bis_bis(slot_at(prev), slot_at(cur), X, Y, R);
+    } else {
+        const int e = prev < 0 ? -1 - prev : -1 - cur;
+        vtx_fixed_bis(fa, e, slot_at(prev < 0 ? cur : prev), X, Y, R);
+    }
+}
+
+// the Hessian part of the radical-axis edge from vertex (p0, lab) to (lab, p1) in FP64
+MA_HDNI double edge64(int p0, int lab, int p1, const Nb64* nb, const Fixed& fx, double c0, double gx, double gy)
+{
+    double px, py, qx, qy;
+    vtx64(p0, lab, nb, fx, px, py);
+    vtx64(lab, p1, nb, fx, qx, qy);
+    const Nb64 d = nb[lab];
+    const double crs = fabs((qx - px) * d.dy - (qy - py) * d.dx);
+    return crs * (c0 + gx * 0.5 * (px + qx) + gy * 0.5 * (py + qy));
+}
+
+template <class Lab, class Edge>
+MA_HD void integrate_piece32(int n, const Lab& lab_of, const Slot* slots, const Nb64* nb, const float* zc,
+                             double ax, double ay,
+                             const Fixed& fx, double c0, double gx, double gy, double& mass, double& second,
+                             double& err_mass, const Edge& edge, int& nedge, int& fb_edge)
+{
+    // the triangle's corners about the anchor
+    FixedA fa;
+    fa.n = fx.n;
+    for (int e = 0; e < fx.n; e++) {
+        fa.ux[e] = (float)(fx.rx[e] - ax);
+        fa.uy[e] = (float)(fx.ry[e] - ay);
+        fa.ur[e] = kU32 * fmaxf(fabsf(fa.ux[e]), fabsf(fa.uy[e])) + 1e-37f;
+    }
+    // rho about the anchor: rho(v) = ca + g . v
+    const float caf = (float)(c0 + gx * ax + gy * ay), gxf = (float)gx, gyf = (float)gy;
+    float x0 = 0.0f, y0 = 0.0f, r0 = 0.0f;
+    float vx = 0.0f, vy = 0.0f, vr = 0.0f;
+    CompF m0{0, 0}, m1x{0, 0}, m1y{0, 0}, q2{0, 0}, c3x{0, 0}, c3y{0, 0}, sxx{0, 0}, syy{0, 0}, sxy{0, 0};
+    float errA = 0.0f, vmax = 0.0f;
+    // vertex k + 1 in iteration k; iteration -1 makes vertex 0 (one copy of the constructions)
+    for (int k = -1; k < n; k++) {
+        const int lab = k < 0 ? lab_of(n - 1) : lab_of(k);
         float bx, by, br;
         if (k + 1 < n)
-            vtx32r(lab, lab_of(k + 1), slots, fx, bx, by, br);
+            vtx_anchor(lab, lab_of(k + 1), slots, zc, fa, bx, by, br);
         else {
             bx = x0;
             by = y0;
             br = r0;
         }
-        const float cr = ax * by - ay * bx;
-        const float aa = ax * ax + ay * ay, ab = ax * bx + ay * by, bb = bx * bx + by * by;
+        if (k < 0) {
+            x0 = vx = bx;
+            y0 = vy = by;
+            r0 = vr = br;
+            vmax = fabsf(bx) + fabsf(by) + br;
+            continue;
+        }
+        const float ex = bx - vx, ey = by - vy, e1 = fabsf(ex) + fabsf(ey);
+        errA += (vr + br) * e1;
+        vmax = fmaxf(vmax, fabsf(bx) + fabsf(by) + br);
+        const float cr = vx * by - vy * bx;
+        const float aa = vx * vx + vy * vy, ab = vx * bx + vy * by, bb = bx * bx + by * by;
         m0.add(cr);
-        m1x.add(cr * (ax + bx));
-        m1y.add(cr * (ay + by));
+        m1x.add(cr * (vx + bx));
+        m1y.add(cr * (vy + by));
         q2.add(cr * (aa + ab + bb));
         const float ka = 3.0f * aa + 2.0f * ab + bb, kb = aa + 2.0f * ab + 3.0f * bb;
-        c3x.add(cr * (ax * ka + bx * kb));
-        c3y.add(cr * (ay * ka + by * kb));
+        c3x.add(cr * (vx * ka + bx * kb));
+        c3y.add(cr * (vy * ka + by * kb));
+        sxx.add(cr * (2.0f * (vx * vx + bx * bx) + 2.0f * vx * bx));
+        syy.add(cr * (2.0f * (vy * vy + by * by) + 2.0f * vy * by));
+        sxy.add(cr * (2.0f * (vx * vy + bx * by) + vx * by + bx * vy));
         if (lab >= 0) {
-            const float ex = bx - ax, ey = by - ay;
-            if (2.0f * (ar + br) <= kEdgeTol32 * (fabsf(ex) + fabsf(ey))) {
+            nedge++;
+            if (2.0f * (vr + br) <= kEdgeTol32 * e1) {
                 const Slot d = slots[lab];
                 const float crs = fabsf(ex * d.dy - ey * d.dx);
-                edge(k, lab, (double)(crs * (c0f + gxf * 0.5f * (ax + bx) + gyf * 0.5f * (ay + by))));
+                edge(k, lab, (double)(crs * (caf + gxf * 0.5f * (vx + bx) + gyf * 0.5f * (vy + by))));
             } else {
-                double px, py, qx, qy;
-                vtx64(lab_of(k == 0 ? n - 1 : k - 1), lab, nb, fx, px, py);
-                vtx64(lab, lab_of(k + 1 < n ? k + 1 : 0), nb, fx, qx, qy);
-                const Nb64 d = nb[lab];
-                const double crs = fabs((qx - px) * d.dy - (qy - py) * d.dx);
-                edge(k, lab, crs * (c0 + gx * 0.5 * (px + qx) + gy * 0.5 * (py + qy)));
+                fb_edge++;
+                edge(k, lab, edge64(lab_of(k == 0 ? n - 1 : k - 1), lab, lab_of(k + 1 < n ? k + 1 : 0), nb, fx, c0, gx, gy));
             }
         }
-        ax = bx;
-        ay = by;
-        ar = br;
+        vx = bx;
+        vy = by;
+        vr = br;
     }
-    mass = c0f * (m0.val() * 0.5f) + gxf * (m1x.val() * (1.0f / 6.0f)) + gyf * (m1y.val() * (1.0f / 6.0f));
-    second = c0f * (q2.val() * (1.0f / 12.0f)) + gxf * (c3x.val() * (1.0f / 60.0f)) + gyf * (c3y.val() * (1.0f / 60.0f));
+    const float A2 = m0.val();  // twice the area
+    // the vertices' radii, and the FP32 roundings of the sum (a few ulps of its terms)
+    err_mass = 0.5 * ((double)errA + 4.0 * (double)kU32 * (double)fabsf(A2)) *
+               ((double)fabsf(caf) + ((double)fabsf(gxf) + (double)fabsf(gyf)) * (double)vmax);
+    // int rho, int rho v, int rho |v|^2 about the anchor (fan from it, see integrate_labels)
+    const float I1 = A2 * 0.5f, Ivx = m1x.val() * (1.0f / 6.0f), Ivy = m1y.val() * (1.0f / 6.0f);
+    const float Sxx = sxx.val() * (1.0f / 24.0f), Syy = syy.val() * (1.0f / 24.0f), Sxy = sxy.val() * (1.0f / 24.0f);
+    const float rm = caf * I1 + gxf * Ivx + gyf * Ivy;
+    const float rvx = caf * Ivx + gxf * Sxx + gyf * Sxy, rvy = caf * Ivy + gxf * Sxy + gyf * Syy;
+    const float rq = caf * (q2.val() * (1.0f / 12.0f)) + gxf * (c3x.val() * (1.0f / 60.0f)) + gyf * (c3y.val() * (1.0f / 60.0f));
+    // int rho |u|^2 with u = v + a: int rho |v|^2 + 2 a . int rho v + |a|^2 int rho
+    mass = (double)rm;
+    second = (double)rq + 2.0 * (ax * (double)rvx + ay * (double)rvy) + (ax * ax + ay * ay) * (double)rm;
 }
 
 // ---------------------------------------------------------------------------

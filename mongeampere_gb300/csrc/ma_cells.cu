@@ -911,6 +911,7 @@ struct CellInfo {
     int pre;   // first flat triangle entry
     int4 box;  // mesh-specific range of triangles under the cell's box
     int np, nv;  // count / emit modes: pieces and vertices listed so far
+    double ax, ay;  // mixed mode: the centre of the cell's box, relative to the site
 };
 
 // modes of k_pieces: the evaluation, the evaluation with moments, the adjoint, and
@@ -928,10 +929,11 @@ struct ClipStage {
 
 template <int MODE>
 struct PieceWarp {
-    static constexpr int kAcc = MODE == kModeVjp ? 3 : (MODE == kModeMoments ? 7 : 2);
+    static constexpr int kAcc = MODE == kModeVjp || MODE == kModeMixed ? 3 : (MODE == kModeMoments ? 7 : 2);
     ClipStage cs;
     Slot slot[kSlotPool];
     Nb64 nb[kSlotPool];
+    float zc[MODE == kModeMixed ? kSlotPool : 1];  // mixed: each radical axis about its cell's anchor
     PieceRec rec[kList];
     double out[kAcc][kList];
     double hvc[kPV][kList];
@@ -1162,6 +1164,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
     // lane c sets up cell c
     int my_m = -2, my_cnt = 0;
     int4 my_box = make_int4(0, 0, 0, 0);
+    double my_ax = 0.0, my_ay = 0.0;
     if (lane < ncell) {
         const int k = kbase + lane;
         my_m = A.nb_cnt[k];
@@ -1180,10 +1183,19 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                 write_empty(A, gi, MOM);
             }
         }
-        if (my_m >= 0) my_cnt = mesh.setup(A.cell_box[k], my_box);
+        if (my_m >= 0) {
+            const double4 cb = A.cell_box[k];
+            my_cnt = mesh.setup(cb, my_box);
+            if (MIXED) {
+                const SiteD S = A.sites[k];
+                my_ax = 0.5 * (cb.x + cb.z) - S.x;
+                my_ay = 0.5 * (cb.y + cb.w) - S.y;
+            }
+        }
     }
     uint32_t st = 0;
     unsigned redo = 0;  // cells of the warp to redo (bit c)
+    int mx_np = 0, mx_fa = 0, mx_ne = 0, mx_fe = 0;  // mixed mode: pieces, cells redone in FP64, edges, FP64 edges
     for (int g0 = 0; g0 < ncell;) {
         // a group of cells whose neighbour slots fit in the pool
         int g1 = g0, soff = 0, pre = 0;
@@ -1193,7 +1205,8 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                                       __shfl_sync(kFull, my_box.z, g1), __shfl_sync(kFull, my_box.w, g1));
             const int used = max(mc, 0);
             if (soff + used > kSlotPool) break;
-            if (lane == 0) W.ci[g1 - g0] = CellInfo{kbase + g1, mc, soff, pre, bx, 0, 0};
+            const double cax = __shfl_sync(kFull, my_ax, g1), cay = __shfl_sync(kFull, my_ay, g1);
+            if (lane == 0) W.ci[g1 - g0] = CellInfo{kbase + g1, mc, soff, pre, bx, 0, 0, cax, cay};
             soff += used;
             pre += nc;
             g1++;
@@ -1210,7 +1223,10 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
             const Owner o{S.x, S.y, S.w, C.k};
             const SiteD Q = A.sites[q];
             W.slot[idx] = make_slot(q, Q, o);
-            W.nb[idx] = make_nb64(Q, o);
+            const Nb64 nbq = make_nb64(Q, o);
+            W.nb[idx] = nbq;
+            // mixed: the radical axis about the cell's anchor, 2 v.d = z - 2 a.d
+            if (MIXED) W.zc[idx] = (float)(nbq.z - 2.0 * (C.ax * nbq.dx + C.ay * nbq.dy));
         }
         __syncwarp();
         int f = 0;     // next flat entry
@@ -1471,12 +1487,15 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                 }
                 if (MIXED) {
                     // FP32 integrals of the piece; the cell sums below are FP64
-                    float pm, ps;
-                    integrate_labels32(
-                        (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.slot + C.soff, W.nb + C.soff, T, c0, gx, gy,
-                        pm, ps, [&](int e, int, double v) { W.hvc[e][p] = v; });
-                    W.out[0][p] = (double)pm;
-                    W.out[1][p] = (double)ps;
+                    double pm, ps, pe;
+                    integrate_piece32(
+                        (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.slot + C.soff, W.nb + C.soff,
+                        W.zc + (MIXED ? C.soff : 0), C.ax, C.ay, T, c0, gx, gy, pm, ps, pe,
+                        [&](int e, int, double v) { W.hvc[e][p] = v; }, mx_ne, mx_fe);
+                    mx_np++;
+                    W.out[0][p] = pm;
+                    W.out[1][p] = ps;
+                    W.out[2 % kAcc][p] = pe;
                     continue;
                 }
                 Acc acc{0, 0, 0, 0, 0, 0, 0};
@@ -1585,6 +1604,12 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                 p0 = p1;
                 if (!complete) break;
                 if (C.m >= 0) {
+                    // mixed: a cell whose certified FP32 mass error exceeds kMassTol32 of its
+                    // mass is redone in FP64 by the large-capacity pass
+                    if (MIXED && !(run[2 % kAcc] <= (double)kMassTol32 * fabs(run[0]))) {
+                        redo |= 1u << (g0 + cfin);
+                        if (lane == 0) mx_fa++;
+                    }
                     if ((redo >> (g0 + cfin)) & 1u) {
                         if (lane == 0) {
                             A.redo[atomicAdd(A.nredo, 1)] = C.k;
@@ -1618,6 +1643,16 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
     }
     st &= ~(uint32_t)ST_NEED_EXACT;
     if (st) atomicOr(A.status, st);
+    if (MIXED && A.counters) {
+        const int c0 = __reduce_add_sync(kFull, mx_np), c1 = __reduce_add_sync(kFull, mx_fa);
+        const int c2 = __reduce_add_sync(kFull, mx_ne), c3 = __reduce_add_sync(kFull, mx_fe);
+        if (lane == 0) {
+            atomicAdd(&A.counters[6], (unsigned long long)c0);
+            atomicAdd(&A.counters[7], (unsigned long long)c1);
+            atomicAdd(&A.counters[8], (unsigned long long)c2);
+            atomicAdd(&A.counters[9], (unsigned long long)c3);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------

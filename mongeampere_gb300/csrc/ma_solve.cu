@@ -315,8 +315,10 @@ constexpr double kForcing = 1e-2;  // relative CG residual of a Newton direction
 constexpr int kAggRefresh = 4;  // Newton steps per multigrid aggregation (the sites do not move; the
                                 // Hessian's strengths drift: +1 to 4 CG iterations by the fourth step)
 
+// fp64_finish = false: a mixed-precision solve may stop on its mixed residual (the
+// intermediate stages of the continuation, whose tolerance is far above the FP32 noise)
 static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, const double* dy, const double* dnu,
-                             double* w, const ma_solve_opts& o, ma_stats& S)
+                             double* w, const ma_solve_opts& o, ma_stats& S, bool fp64_finish = true)
 {
     cudaStream_t s = c->stream;
     const bool default_forcing = !(o.cg_rtol > 0);
@@ -337,10 +339,9 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
     // The FP32 integrals leave a noise of 1e-5 to 1e-4 of a cell's mass in the masses
     // (measured up to 3e-4 max-relative at 1M sites): from this relative residual on,
     // where only the quadratically convergent last steps remain, the evaluations are
-    // FP64; a mixed line search that has to cut the step below kMixedMinStep is also
-    // taken as the noise floor and redone in FP64.
+    // FP64.  Above it the noise cannot decide a line search; a mixed line search that
+    // fails all the same is redone in FP64.
     constexpr double kMixedFloor = 1e-2;
-    constexpr double kMixedMinStep = 1.0 / 64.0;
     auto timed_eval = [&](const double* wv, bool trial) -> ma_status {
         cudaEventRecord(e0, s);
         EvalFlags f;
@@ -395,7 +396,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
         int64_t niter = 0;
         for (;;) {
             if (converged(gn, mr) || (mixed_phase && mr <= kMixedFloor)) {
-                if (!mixed_phase) break;
+                if (!mixed_phase || (!fp64_finish && converged(gn, mr))) break;
                 // the mixed residual has converged: check (and finish) in FP64
                 mixed_phase = false;
                 if ((st = timed_eval(w, false)) != MA_OK) {
@@ -463,7 +464,6 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
                 }
                 alpha *= 0.5;
                 S.linesearch_halvings++;
-                if (mixed_phase && alpha < kMixedMinStep) break;
                 if (o.verbose)
                     fprintf(stderr, "subit %lld: min(masses)=%.17g\n", (long long)niter, minm);
                 if (alpha < 0x1p-40) break;
@@ -683,6 +683,87 @@ static ma_status multiscale_solve(Ctx* c, const Mesh* m, int n, const double* dx
     return MA_OK;
 }
 
+// ---------------------------------------------------------------------------
+// continuation in the target masses (no counterpart in the reference, whose ot_solve
+// takes the initial weights as an argument): from the masses m0 of the initial weights,
+// the targets nu_t = m0 + t (nu - m0) are reached stage by stage, each stage the
+// reference's damped Newton warm-started from the previous one, with t chosen so that no
+// cell's target changes by more than a factor kContFactor from one stage to the next.
+// At t = 0 the initial weights solve the problem exactly, so every stage starts from a
+// point with no empty cell, which the reference's Kitagawa-Merigot-Thibert rule needs
+// (its eps0 = min(m_start, nu_t) / 2 is taken per stage).  For sites far from
+// equilibrium (clustered sites on a spread-out density) the damped Newton from w = 0
+// cuts every step to a few 2^-11; here the stages are damped too, but converge.
+// ---------------------------------------------------------------------------
+constexpr double kContFactor = 2.0;
+constexpr double kContStageTol = 1e-2;  // max relative residual of an intermediate stage
+constexpr int64_t kContStageIters = 5;  // an intermediate stage may take this many times maxiter
+
+static ma_status continuation_solve(Ctx* c, const Mesh* m, int n, const double* dx, const double* dy,
+                                    const double* dnu, double* w, const ma_solve_opts& o, ma_stats& S)
+{
+    cudaStream_t s = c->stream;
+    ma_status st = build_site_index(c, m, n, dx, dy, w);
+    if (st != MA_OK) return st;
+    {
+        EvalFlags f;
+        f.hessian = false;
+        if ((st = run_eval(c, m, n, w, f)) != MA_OK) return st;
+        S.neval++;
+        S.neval_fp64++;
+    }
+    std::vector<double> m0(n), nu(n), nut(n);
+    MA_CUDA(c, cudaMemcpyAsync(m0.data(), c->mass.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, cudaMemcpyAsync(nu.data(), dnu, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    MA_CUDA(c, ctx_sync(c));
+    for (int i = 0; i < n; i++)
+        if (!(m0[i] > 0.0))
+            return fail(c, MA_EMPTY_CELL, "computed minimum mass is non-positive: a Laguerre cell is empty");
+    MA_CUDA(c, c->ms_nu.ensure(sizeof(double) * n));
+    double t = 0.0;
+    for (int stage = 0;; stage++) {
+        // the largest t' with m_t' / m_t in [1 / kContFactor, kContFactor] for every cell
+        double tn = 1.0;
+        for (int i = 0; i < n; i++) {
+            const double d = nu[i] - m0[i], mt = m0[i] + t * d;
+            if (d > 0.0)
+                tn = std::min(tn, (kContFactor * mt - m0[i]) / d);
+            else if (d < 0.0)
+                tn = std::min(tn, (m0[i] - mt / kContFactor) / -d);
+        }
+        tn = std::min(1.0, std::max(tn, t + 1e-6 * (1.0 - t)));
+        const bool last = tn >= 1.0;
+        const double* target = dnu;
+        ma_solve_opts os = o;
+        if (!last) {
+            for (int i = 0; i < n; i++) nut[i] = m0[i] + tn * (nu[i] - m0[i]);
+            MA_CUDA(c, cudaMemcpyAsync(c->ms_nu.p, nut.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+            target = c->ms_nu.as<double>();
+            os.stop_rule = MA_STOP_MAX_REL;
+            os.eps_g = kContStageTol;
+            os.maxiter = o.maxiter * kContStageIters;
+        }
+        ma_stats Sl{};
+        st = newton_core(c, m, n, dx, dy, target, w, os, Sl, last);
+        if (o.verbose)
+            fprintf(stderr, "continuation stage %d: t = %.6g, status %d, %zu Newton steps, %zu evaluations, max_rel %.3g\n",
+                    stage, tn, (int)st, Sl.niter, Sl.neval, Sl.max_rel_err);
+        S.niter += Sl.niter;
+        S.neval += Sl.neval;
+        S.neval_fp64 += Sl.neval_fp64;
+        S.cg_iters += Sl.cg_iters;
+        S.cg_noconv += Sl.cg_noconv;
+        S.linesearch_halvings += Sl.linesearch_halvings;
+        S.t_eval_ms += Sl.t_eval_ms;
+        S.t_linsolve_ms += Sl.t_linsolve_ms;
+        S.grad_norm = Sl.grad_norm;
+        S.max_rel_err = Sl.max_rel_err;
+        S.value = Sl.value;
+        if (last || st != MA_OK) return st;
+        t = tn;
+    }
+}
+
 extern "C" {
 
 ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
@@ -824,8 +905,9 @@ ma_status ma_ot_solve(ma_ctx* cp, const ma_mesh* mp, int64_t n64, const double* 
     double* w = c->wcur.as<double>();
     MA_CUDA(c, cudaMemcpyAsync(w, w_inout, sizeof(double) * n,
                                mem == MA_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
-    ma_status result = o.init == MA_INIT_MULTISCALE ? multiscale_solve(c, m, n, dx, dy, dnu, w, o, S)
-                                                    : newton_core(c, m, n, dx, dy, dnu, w, o, S);
+    ma_status result = o.init == MA_INIT_MULTISCALE     ? multiscale_solve(c, m, n, dx, dy, dnu, w, o, S)
+                       : o.init == MA_INIT_CONTINUATION ? continuation_solve(c, m, n, dx, dy, dnu, w, o, S)
+                                                        : newton_core(c, m, n, dx, dy, dnu, w, o, S);
     if (result == MA_OK || result == MA_MAXITER || result == MA_LINESEARCH_FAIL) {
         cudaMemcpyAsync(w_inout, w, sizeof(double) * n,
                         mem == MA_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s);

@@ -248,3 +248,47 @@ def test_solve_is_reproducible(ctx):
     for w, ni, ne, cg in runs[1:]:
         np.testing.assert_array_equal(w, runs[0][0])
         assert (ni, ne, cg) == runs[0][1:]
+
+
+def test_continuation_solves_clustered_sites(ctx, oracle):
+    # the clustered shape of the 1M-site workload, scaled down: the continuation in the
+    # target masses reaches 1e-6 (checked by the oracle) in stages of the reference's
+    # damped Newton; the plain solve from w = 0 reaches the same weights
+    from mongeampere_gb300 import api
+    p = W.make_problem(128, 20000, "uniform", "blobs", "equal", seed=0)
+    X = np.c_[p.x, p.y]
+    st = api.Statistics()
+    w = np.asarray(api.ot_solve(p.mesh, X, p.nu, eps_g=1e-6, stop="rel", init="continuation", maxiter=200,
+                                stats=st, ctx=ctx))
+    assert st.status == 0 and st.max_rel_err <= 1e-6
+    r = oracle.kantorovich(p.mesh, p.x, p.y, w, arith="fp64", ring=1)
+    assert np.max(np.abs(r.g - p.nu) / p.nu) <= 1.5e-6
+    st0 = api.Statistics()
+    w0 = np.asarray(api.ot_solve(p.mesh, X, p.nu, eps_g=1e-6, stop="rel", maxiter=200, stats=st0, ctx=ctx))
+    assert st0.status == 0
+    np.testing.assert_allclose(w, w0, rtol=0, atol=1e-5 * np.abs(w0).max())
+    # mixed precision: the stages run on FP32 integrals, the last one finishes in FP64
+    stm = api.Statistics()
+    api.ot_solve(p.mesh, X, p.nu, eps_g=1e-6, stop="rel", init="continuation", precision="mixed", maxiter=200,
+                 stats=stm, ctx=ctx)
+    assert stm.status == 0 and stm.max_rel_err <= 1e-6 and stm.neval_fp64 < stm.neval
+
+
+def test_mixed_precision_with_cells_far_from_their_sites(ctx):
+    # at the solution of a 20-fold density contrast the cells lie many cell sizes from
+    # their sites; the mixed integrals are taken about a point of the cell, so their
+    # error stays that of the FP32 certified bounds: masses within 2^-14, every Hessian
+    # entry within 2.5e-4 of the FP64 evaluation
+    from mongeampere_gb300 import api
+    p = W.make_problem(256, 20000, "gauss", "uniform", "random", seed=11)
+    X = np.c_[p.x, p.y]
+    w = np.asarray(api.ot_solve(p.mesh, X, p.nu, eps_g=1e-6, stop="rel", ctx=ctx))
+    v64, g64, h64 = api.kantorovich(p.mesh, X, w, ctx=ctx)
+    v32, g32, h32 = api.kantorovich(p.mesh, X, w, precision="mixed", ctx=ctx)
+    g64, g32 = np.asarray(g64), np.asarray(g32)
+    rel = np.abs(g32 - g64) / g64
+    assert rel.max() <= 2.0 ** -14, f"mixed mass off by {rel.max():.3e}"
+    assert abs(v32 - v64) <= 1e-6 * abs(v64)
+    np.testing.assert_array_equal(h32.col, h64.col)
+    hrel = np.abs(np.asarray(h32.val) - np.asarray(h64.val)) / np.abs(np.asarray(h64.val))
+    assert hrel.max() <= 2.5e-4, f"mixed Hessian entry off by {hrel.max():.3e}"
