@@ -203,6 +203,45 @@ def run_reference(args, rank):
     print(json.dumps(line))
 
 
+def c3_evaluations(ctx, dev, steps, warmup):
+    """Complete Laguerre evaluations (masses, value, CSR Hessian) of the clustered 1M-site
+    workload (workloads.c3) at w = 0, in FP64 and in the mixed form: evaluations/s of
+    each, and the mixed form's errors against FP64."""
+    import numpy as np
+    import torch
+
+    from mongeampere_gb300 import api
+    from mongeampere_gb300 import workloads as W
+    p = W.c3(0)
+    dm = ctx.mesh(p.mesh)
+    X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
+    out = {"config": "1,000,000 sites (70% in 20 Gaussian blobs), 2048^2 grid U[0.5,1.5]; masses, value and "
+                     "CSR Hessian per evaluation"}
+    w = torch.zeros(p.n, dtype=torch.float64, device=dev)
+    for name in ("w0",):
+        res = {}
+        for prec in ("fp64", "mixed"):
+            for _ in range(warmup):
+                api.kantorovich(dm, X, w, precision=prec, ctx=ctx)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(steps):
+                v, g, h = api.kantorovich(dm, X, w, precision=prec, ctx=ctx)
+            e1.record()
+            torch.cuda.synchronize()
+            res[prec] = (steps / (e0.elapsed_time(e1) * 1e-3), v, g.cpu().numpy(), h)
+        g64, g32 = res["fp64"][2], res["mixed"][2]
+        same = bool(np.array_equal(res["fp64"][3].col, res["mixed"][3].col))
+        hrel = (float(np.max(np.abs(res["mixed"][3].val - res["fp64"][3].val) / np.abs(res["fp64"][3].val)))
+                if same else None)
+        out[name] = {"fp64_evals_per_s": res["fp64"][0], "mixed_evals_per_s": res["mixed"][0],
+                     "mixed_mass_rel_err_max": float(np.max(np.abs(g32 - g64) / g64)),
+                     "mixed_value_rel_err": float(abs(res["mixed"][1] - res["fp64"][1]) / abs(res["fp64"][1])),
+                     "mixed_hessian_entry_rel_err_max": hrel, "same_sparsity": same}
+    return out
+
+
 def run_c3(args, ctx, dev, rank):
     """Mixed precision against FP64 on the clustered 1M-site workload (workloads.c3:
     2048^2 grid U[0.5,1.5], 1,000,000 sites, 70% in 20 Gaussian blobs, equal masses):
@@ -281,23 +320,32 @@ def run_c3(args, ctx, dev, rank):
 
 
 def run_c4(args, ctx, dev, rank):
-    """The adjoint and the W2 flow at 200,000 sites on a 256^2 density (workloads.c4):
-    (a) vector-Jacobian products of (value, masses, first moments) against forward
-    evaluations, per second, with cotangents N(0, 1), and the adjoint's directional
-    derivative against a central difference of the GPU forward pass (h = 1e-6 along a
-    random direction of the sites and weights); (b) 50 steps of the W2 flow
-    x <- x + tau (x - centroid) with tau = -0.5 (half of Lloyd's step towards the
-    centroids), each a warm-started solve to max relative mass error 1e-6."""
+    """The adjoint at 200,000 sites on a 256^2 density (workloads.c4), at the OT solution
+    (cells away from their sites): (a) vector-Jacobian products of (value, masses, first
+    moments), FP64 and FP32, per second, against forward evaluations, with cotangents
+    N(0, 1); (b) central differences of the FP64 forward pass on 1,000 random coordinates
+    of the sites, the weights and the density's vertex values, against both adjoints, with
+    h = 1e-6 in each coordinate's own scale (the mean cell size 1/sqrt(N) for sites, the
+    mean cell area 1/N for weights, 1 for vertex values: a weight step of 1e-6 would be a
+    fifth of a cell's weight scale at 200,000 sites, far from the difference's asymptotic
+    regime); (c) 50 steps of the W2 gradient flow whose direction is the backward pass:
+    after a warm-started solve to max relative mass error 1e-6, x <- x + tau dPhi/dx / (2 m)
+    = x + tau (c - x), with dPhi/dx = 2 (int rho x - m x) from the VJP of the value and c
+    the cell's centroid (tau = 0.5: half a Lloyd step, the W2 cost's gradient step)."""
     import numpy as np
     import torch
 
+    from mongeampere_gb300 import _lib
     from mongeampere_gb300 import api
     from mongeampere_gb300 import workloads as W
-    out = {"metric": METRIC, "workload": "c4", "n_gpus": 1}
+    out = {"metric": METRIC, "workload": "c4", "n_gpus": 1,
+           "config": "200,000 uniform sites, 256^2 grid U[0.5,1.5], equal masses, at the OT solution"}
     p = W.c4(0)
     dm = ctx.mesh(p.mesh)
     X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
+    nu = torch.tensor(p.nu, device=dev)
     w = torch.zeros(p.n, dtype=torch.float64, device=dev)
+    api.ot_solve(dm, X, nu, x=w, eps_g=1e-6, stop="rel", ctx=ctx)
     rng = np.random.default_rng(4)
     a = float(rng.normal())
     b = torch.tensor(rng.normal(size=p.n), device=dev)
@@ -316,33 +364,99 @@ def run_c4(args, ctx, dev, rank):
         return args.steps / (e0.elapsed_time(e1) * 1e-3)
 
     fwd = rate(lambda: api.kantorovich(dm, X, w, hessian=False, ctx=ctx))
-    vjp = rate(lambda: api.kantorovich_vjp(dm, X, w, a, b, e, ctx=ctx))
-    gX, gw, _ = api.kantorovich_vjp(dm, X, w, a, b, e, ctx=ctx)
-    vX = torch.tensor(rng.normal(size=(p.n, 2)) * 1e-3, device=dev)
-    vw = torch.tensor(rng.normal(size=p.n) * 1e-5, device=dev)
+    vjp64 = rate(lambda: api.kantorovich_vjp(dm, X, w, a, b, e, ctx=ctx))
+    vjp32 = rate(lambda: api.kantorovich_vjp(dm, X, w, a, b, e, precision="mixed", ctx=ctx))
+    g64 = [q.cpu().numpy() for q in api.kantorovich_vjp(dm, X, w, a, b, e, ctx=ctx)]
+    g32 = [q.cpu().numpy() for q in api.kantorovich_vjp(dm, X, w, a, b, e, precision="mixed", ctx=ctx)]
+    vals = np.asarray(p.mesh.values, dtype=np.float64).reshape(-1)
+    vals_dev = torch.tensor(vals, device=dev)
 
-    def f(t):
-        v, g, _ = api.kantorovich(dm, X + t * vX, w + t * vw, hessian=False, ctx=ctx)
-        _, first = api.first_moment(dm, X + t * vX, w + t * vw, ctx=ctx)
+    def objective(Xp, wp):
+        v, g, _ = api.kantorovich(dm, Xp, wp, hessian=False, ctx=ctx)
+        _, first = api.first_moment(dm, Xp, wp, ctx=ctx)
         return a * v + float((b * g).sum()) + float((e * first).sum())
 
     h = 1e-6
-    fd = (f(h) - f(-h)) / (2 * h)
-    ad = float((gX * vX).sum() + (gw * vw).sum())
-    out["adjoint"] = {"config": "200,000 uniform sites, 256^2 grid U[0.5,1.5], w = 0", "forward_evals_per_s": fwd,
-                      "vjp_per_s": vjp, "directional_derivative": ad, "central_difference": fd,
-                      "relative_difference": abs(ad - fd) / abs(fd)}
-    nu = torch.tensor(p.nu, device=dev)
-    st = api.Statistics()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ncoord = 1000
+    fd, ad64, ad32 = np.zeros(ncoord), np.zeros(ncoord), np.zeros(ncoord)
+    kinds = rng.integers(0, 4, ncoord)
+    t0 = time.perf_counter()
+    for q in range(ncoord):
+        kind = int(kinds[q])
+        if kind < 2:
+            i = int(rng.integers(p.n))
+            f = []
+            hs = h * p.n ** -0.5
+            for t in (hs, -hs):
+                Xp = X.clone()
+                Xp[i, kind] += t
+                f.append(objective(Xp, w))
+            ad64[q], ad32[q] = g64[0][i, kind], g32[0][i, kind]
+            f = [f[0] * p.n ** 0.5, f[1] * p.n ** 0.5]  # divided by 2h below: the step was h / sqrt(N)
+        elif kind == 2:
+            i = int(rng.integers(p.n))
+            f = []
+            for t in (h / p.n, -h / p.n):
+                wp = w.clone()
+                wp[i] += t
+                f.append(objective(X, wp))
+            ad64[q], ad32[q] = g64[1][i], g32[1][i]
+            f = [f[0] * p.n, f[1] * p.n]  # divided by 2h below: the step was h / N
+        else:
+            j = int(rng.integers(vals.size))
+            f = []
+            for t in (h, -h):
+                vp = vals_dev.clone()
+                vp[j] += t
+                dm.set_values(vp)
+                f.append(objective(X, w))
+            dm.set_values(vals_dev)
+            ad64[q], ad32[q] = g64[2][j], g32[2][j]
+        fd[q] = (f[0] - f[1]) / (2 * h)
+    fd_s = time.perf_counter() - t0
+    scale = float(np.abs(fd).max())
+    big = np.abs(fd) >= 1e-3 * scale
+
+    def agree(ad):
+        d = np.abs(ad - fd)
+        return {"max_abs_over_max_fd": float(d.max() / scale),
+                "max_rel_where_fd_above_1e-3_of_max": float(np.max(d[big] / np.abs(fd[big]))),
+                "median_rel": float(np.median(d[big] / np.abs(fd[big])))}
+
+    out["adjoint"] = {"forward_evals_per_s": fwd, "vjp_fp64_per_s": vjp64, "vjp_fp32_per_s": vjp32,
+                      "fd": {"h_sites": h * p.n ** -0.5, "h_weights": h / p.n, "h_vertex_values": h,
+                             "coordinates": ncoord,
+                             "kinds": {"site x": int((kinds == 0).sum()), "site y": int((kinds == 1).sum()),
+                                       "weight": int((kinds == 2).sum()), "vertex value": int((kinds == 3).sum())},
+                             "seconds": fd_s, "fp64_adjoint": agree(ad64), "fp32_adjoint": agree(ad32)},
+                      "fp32_vs_fp64_adjoint_rel_norm": [float(np.linalg.norm(q32 - q64) / np.linalg.norm(q64))
+                                                        for q64, q32 in zip(g64, g32)]}
+    # the W2 flow driven by the backward pass
+    Xf, wf = X.clone(), w.clone()
+    tau = 0.5
+    st_tot = [0, 0]
     torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    Xf, wf, st = api.w2_flow(dm, X, nu, steps=50, tau=-0.5, ctx=ctx)
+    for _ in range(50):
+        st = api.Statistics()
+        api.ot_solve(dm, Xf, nu, x=wf, eps_g=1e-6, stop="rel", stats=st, ctx=ctx, raise_on_error=False)
+        if st.status == _lib.MA_EMPTY_CELL:
+            # a moved site's cell is empty at the previous weights: restart from zero (as ma_w2_flow)
+            wf.zero_()
+            api.ot_solve(dm, Xf, nu, x=wf, eps_g=1e-6, stop="rel", stats=st, ctx=ctx)
+        assert st.status == 0, st.status
+        st_tot[0] += st.niter
+        st_tot[1] += st.neval
+        gX, _, _ = api.kantorovich_vjp(dm, Xf, wf, 1.0, None, None, grad_rho=False, ctx=ctx)
+        Xf = Xf + tau * gX / (2.0 * nu[:, None])
     e1.record()
     torch.cuda.synchronize()
     secs = e0.elapsed_time(e1) * 1e-3
-    out["w2_flow"] = {"config": "50 steps, tau = -0.5, each solve warm-started to max rel mass err 1e-6",
-                      "seconds": secs, "steps_per_s": 50 / secs, "newton_iters": st.niter, "evals": st.neval}
+    out["w2_flow"] = {"config": "50 steps, x <- x + tau dPhi/dx / (2 m), tau = 0.5, dPhi/dx from the VJP, each "
+                                "solve warm-started (from zero where a moved site's cell is empty at the previous "
+                                "weights) to max rel mass err 1e-6",
+                      "seconds": secs, "steps_per_s": 50 / secs, "newton_iters": st_tot[0], "evals": st_tot[1]}
     if rank == 0:
         print(json.dumps(out))
 
@@ -404,6 +518,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c3", action="store_true", help="leave out the 1M-site FP64 / mixed evaluations")
     ap.add_argument("--profile-evals", type=int, default=0,
                     help="profiling driver: solve once, then run this many Laguerre evaluations at the "
                          "solution weights and print per-kernel device times (no benchmark line)")
@@ -587,6 +702,11 @@ def main():
     solve_roofline = {"algorithmic_bytes": solve_bytes, "evals": st_prof.neval, "cg_iters": st_prof.cg_iters,
                       "achieved_gbs": solve_gbs, "frac": solve_gbs / peak}
 
+    # ---- the 1M-site clustered workload: FP64 against mixed evaluations ----------
+    c3 = None
+    if rank == 0 and not args.no_c3:
+        c3 = c3_evaluations(ctx, dev, max(args.steps, 3), 2)
+
     # ---- e2e through the C ABI with host buffers ----
     xh = torch.tensor(p.x).pin_memory().numpy()
     yh = torch.tensor(p.y).pin_memory().numpy()
@@ -625,6 +745,7 @@ def main():
         "e2e": e2e,
         "roofline": roofline,
         "solve_roofline": solve_roofline,
+        "c3_evaluations": c3,
         "clocks": clk,
         "gpu_launches": launches,
     }

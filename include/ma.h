@@ -352,11 +352,14 @@ ma_status ma_draw_laguerre(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const do
  *   grad_x, grad_y, grad_w [n]  receive the gradients with respect to the sites and weights
  *   grad_rho            receives the gradient with respect to the mesh's vertex values
  *                       (grid: nx * ny, row-major like the values; triangles: nv), or NULL
+ *   prec                MA_FP64, or MA_MIXED: the pieces' integrals in FP32 about a point of
+ *                       each cell (the mixed evaluation's), moved to the site-relative moments
+ *                       and summed per cell in FP64
  * Cells with more than 48 neighbours, or whose pieces need exact predicates, are not
  * handled (MA_ERR_CAPACITY).  grad_rho is accumulated with atomics: its last bits may
  * differ from run to run; the other gradients are reproducible. */
 ma_status ma_kantorovich_vjp(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
-                             const double* w, ma_mem mem, double cot_value, const double* cot_mass,
+                             const double* w, ma_mem mem, ma_precision prec, double cot_value, const double* cot_mass,
                              const double* cot_first, double* grad_x, double* grad_y, double* grad_w,
                              double* grad_rho);
 

@@ -85,7 +85,7 @@ SIGNATURES = {
     "ma_w2_flow": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int64,
                                   ctypes.c_double, _vp, _vp]),
     "ma_mesh_set_values": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
-    "ma_kantorovich_vjp": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, ctypes.c_double,
+    "ma_kantorovich_vjp": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                           _vp, _vp, _vp, _vp, _vp, _vp]),
     "ma_lloyd": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
 }

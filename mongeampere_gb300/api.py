@@ -365,11 +365,12 @@ def draw_laguerre_diagram(mesh, X, weights, colors, bbox, width: int, height: in
 
 
 def kantorovich_vjp(mesh, X, weights, cot_value: float = 0.0, cot_mass=None, cot_first=None, y=None, *,
-                    grad_rho: bool = True, ctx: Context | None = None):
+                    grad_rho: bool = True, precision: str = "fp64", ctx: Context | None = None):
     """Adjoint of ``(value, masses, first moments)`` (``ma_kantorovich_vjp``; no
     counterpart in the reference).  ``cot_first`` is ``(N, 2)``.  Returns
     ``(grad_X (N, 2), grad_w (N,), grad_rho (V,) or None)`` where ``grad_rho`` is per
-    mesh vertex (row-major ``ny x nx`` for a grid)."""
+    mesh vertex (row-major ``ny x nx`` for a grid).  ``precision="mixed"`` integrates
+    the pieces in FP32."""
     ctx = ctx or default_context()
     dm = _dmesh(ctx, mesh)
     x, yy = _split_xy(X, y)
@@ -384,7 +385,10 @@ def kantorovich_vjp(mesh, X, weights, cot_value: float = 0.0, cot_mass=None, cot
     src = dm.src
     nv = src.nx * src.ny if isinstance(src, GridMesh) else src.nv
     gr, grp = a.out(nv) if grad_rho else (None, None)
-    st = ctx.lib.ma_kantorovich_vjp(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.mem, float(cot_value),
+    if precision not in ("fp64", "mixed"):
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    prec = L.MA_MIXED if precision == "mixed" else L.MA_FP64
+    st = ctx.lib.ma_kantorovich_vjp(ctx.h, dm.h, n, a.ptrs[0], a.ptrs[1], a.ptrs[2], a.mem, prec, float(cot_value),
                                     a.ptrs[3], a.ptrs[4], gxp, gyp, gwp, grp)
     _check(ctx.lib, ctx.h, st, "ma_kantorovich_vjp")
     if a.device:

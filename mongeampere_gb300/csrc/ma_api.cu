@@ -291,7 +291,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         a.pc_cnt = c->pc_cnt.as<int>();
         a.pv_cnt = c->pv_cnt.as<int>();
     }
-    const int mode = f.pieces ? 3 : (f.vjp ? 2 : (f.moments > 0 ? 1 : (f.mixed ? 5 : 0)));
+    const int mode = f.pieces ? 3 : (f.vjp ? (f.mixed ? 6 : 2) : (f.moments > 0 ? 1 : (f.mixed ? 5 : 0)));
     launch_cells(c, m, a, 0, mode);
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -845,7 +845,7 @@ ma_status ma_kantorovich(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x
 }
 
 ma_status ma_kantorovich_vjp(ma_ctx* c, const ma_mesh* m, int64_t n, const double* x, const double* y,
-                             const double* w, ma_mem mem, double cot_value, const double* cot_mass,
+                             const double* w, ma_mem mem, ma_precision prec, double cot_value, const double* cot_mass,
                              const double* cot_first, double* grad_x, double* grad_y, double* grad_w,
                              double* grad_rho)
 {
@@ -886,6 +886,7 @@ ma_status ma_kantorovich_vjp(ma_ctx* c, const ma_mesh* m, int64_t n, const doubl
     EvalFlags f;
     f.hessian = false;
     f.vjp = &v;
+    f.mixed = prec == MA_MIXED;
     if ((st = run_eval(c, m, (int)n, dw, f)) != MA_OK) return st;
     if (mem == MA_MEM_HOST) {
         if ((st = copy_out(c, grad_x, v.grad_x, (size_t)n, mem)) != MA_OK) return st;

@@ -859,6 +859,102 @@ MA_HD void integrate_vjp(int n, const Lab& lab_of, const Nb64* nb, const Fixed& 
     M.Icy = c3y * (1.0 / 60.0);
 }
 
+// integrate_vjp in FP32 about the cell's anchor a (the mixed-precision adjoint): the
+// vertices of integrate_piece32 (their radii unused), the piece's moments and each
+// radical-axis edge's line integrals E0, Ev, Evv in compensated FP32 about a, then moved
+// to the site-relative moments integrate_vjp gives, u = v + a, in FP64:
+//   int u = Iv + a I1,  int u u^T = Svv + a Iv^T + Iv a^T + a a^T I1,
+//   int |u|^2 = Iqv + 2 a.Iv + |a|^2 I1,
+//   int u |u|^2 = Icv + 2 Svv a + |a|^2 Iv + a Iqv + 2 a (a.Iv) + a |a|^2 I1,
+// and likewise for the edge integrals; the gradients accumulate as in integrate_vjp.
+template <class Lab, class Cot>
+MA_HD void integrate_vjp32(int n, const Lab& lab_of, const Slot* slots, const float* zc, double ax, double ay,
+                           const Fixed& fx, double c0, double gx, double gy, double xi, double yi, double bi,
+                           double exi, double eyi, const Cot& cot, PieceMoments& M, double& gw, double& gpx,
+                           double& gpy)
+{
+    FixedA fa;
+    fa.n = fx.n;
+    for (int e = 0; e < fx.n; e++) {
+        fa.ux[e] = (float)(fx.rx[e] - ax);
+        fa.uy[e] = (float)(fx.ry[e] - ay);
+        fa.ur[e] = kU32 * fmaxf(fabsf(fa.ux[e]), fabsf(fa.uy[e])) + 1e-37f;
+    }
+    const float caf = (float)(c0 + gx * ax + gy * ay), gxf = (float)gx, gyf = (float)gy;
+    float x0 = 0.0f, y0 = 0.0f, vx = 0.0f, vy = 0.0f;
+    CompF m0{0, 0}, m1x{0, 0}, m1y{0, 0}, q2{0, 0}, c3x{0, 0}, c3y{0, 0}, sxx{0, 0}, syy{0, 0}, sxy{0, 0};
+    for (int k = -1; k < n; k++) {
+        const int lab = k < 0 ? lab_of(n - 1) : lab_of(k);
+        float bx, by, br;
+        if (k + 1 < n)
+            vtx_anchor(lab, lab_of(k + 1), slots, zc, fa, bx, by, br);
+        else {
+            bx = x0;
+            by = y0;
+        }
+        if (k < 0) {
+            x0 = vx = bx;
+            y0 = vy = by;
+            continue;
+        }
+        const float cr = vx * by - vy * bx;
+        const float aa = vx * vx + vy * vy, ab = vx * bx + vy * by, bb = bx * bx + by * by;
+        m0.add(cr);
+        m1x.add(cr * (vx + bx));
+        m1y.add(cr * (vy + by));
+        q2.add(cr * (aa + ab + bb));
+        const float ka = 3.0f * aa + 2.0f * ab + bb, kb = aa + 2.0f * ab + 3.0f * bb;
+        c3x.add(cr * (vx * ka + bx * kb));
+        c3y.add(cr * (vy * ka + by * kb));
+        sxx.add(cr * (2.0f * (vx * vx + bx * bx) + 2.0f * vx * bx));
+        syy.add(cr * (2.0f * (vy * vy + by * by) + 2.0f * vy * by));
+        sxy.add(cr * (2.0f * (vx * vy + bx * by) + vx * by + bx * vy));
+        if (lab >= 0) {
+            const Slot d = slots[lab];
+            const float ex = bx - vx, ey = by - vy;
+            const float ratio = fabsf(ex * d.dy - ey * d.dx) / (d.dx * d.dx + d.dy * d.dy);
+            const float mx = 0.5f * (vx + bx), my = 0.5f * (vy + by);
+            const float ra = caf + gxf * vx + gyf * vy, rb = caf + gxf * bx + gyf * by, rm = caf + gxf * mx + gyf * my;
+            const float w6 = ratio * (1.0f / 6.0f);
+            const double E0 = (double)(ratio * rm);
+            const double Evx = (double)(w6 * (ra * vx + 4.0f * rm * mx + rb * bx));
+            const double Evy = (double)(w6 * (ra * vy + 4.0f * rm * my + rb * by));
+            const double Evxx = (double)(w6 * (ra * vx * vx + 4.0f * rm * mx * mx + rb * bx * bx));
+            const double Evyy = (double)(w6 * (ra * vy * vy + 4.0f * rm * my * my + rb * by * by));
+            const double Evxy = (double)(w6 * (ra * vx * vy + 4.0f * rm * mx * my + rb * bx * by));
+            const double Eux = Evx + ax * E0, Euy = Evy + ay * E0;
+            const double Exx = Evxx + 2.0 * ax * Evx + ax * ax * E0;
+            const double Eyy = Evyy + 2.0 * ay * Evy + ay * ay * E0;
+            const double Exy = Evxy + ax * Evy + ay * Evx + ax * ay * E0;
+            double bj, ejx, ejy;
+            cot(lab, bj, ejx, ejy);
+            const double db = bi - bj, dex = exi - ejx, dey = eyi - ejy;
+            gw += 0.5 * db * E0 + 0.5 * (dex * (xi * E0 + Eux) + dey * (yi * E0 + Euy));
+            const double dxi = dex * xi + dey * yi;
+            gpx += (db + dxi) * Eux + Exx * dex + Exy * dey;
+            gpy += (db + dxi) * Euy + Exy * dex + Eyy * dey;
+        }
+        vx = bx;
+        vy = by;
+    }
+    const double I1 = 0.5 * (double)m0.val();
+    const double Ivx = (double)m1x.val() * (1.0 / 6.0), Ivy = (double)m1y.val() * (1.0 / 6.0);
+    const double Sxx = (double)sxx.val() * (1.0 / 24.0), Syy = (double)syy.val() * (1.0 / 24.0),
+                 Sxy = (double)sxy.val() * (1.0 / 24.0);
+    const double Iqv = (double)q2.val() * (1.0 / 12.0);
+    const double Icvx = (double)c3x.val() * (1.0 / 60.0), Icvy = (double)c3y.val() * (1.0 / 60.0);
+    const double aIv = ax * Ivx + ay * Ivy, a2 = ax * ax + ay * ay;
+    M.I1 = I1;
+    M.Iux = Ivx + ax * I1;
+    M.Iuy = Ivy + ay * I1;
+    M.Sxx = Sxx + 2.0 * ax * Ivx + ax * ax * I1;
+    M.Syy = Syy + 2.0 * ay * Ivy + ay * ay * I1;
+    M.Sxy = Sxy + ax * Ivy + ay * Ivx + ax * ay * I1;
+    M.Iq = Iqv + 2.0 * aIv + a2 * I1;
+    M.Icx = Icvx + 2.0 * (ax * Sxx + ay * Sxy) + a2 * Ivx + ax * Iqv + 2.0 * ax * aIv + ax * a2 * I1;
+    M.Icy = Icvy + 2.0 * (ax * Sxy + ay * Syy) + a2 * Ivy + ay * Iqv + 2.0 * ay * aIv + ay * a2 * I1;
+}
+
 template <int CAP, bool MOM>
 MA_HD void integrate_piece(const Poly<CAP>& P, const Nb64* nb, const Fixed& fx, double c0, double gx,
                            double gy, Acc& acc, double* hv, Bits<CAP>& touched)

@@ -916,7 +916,8 @@ struct CellInfo {
 
 // modes of k_pieces: the evaluation, the evaluation with moments, the adjoint, and
 // the two passes that materialise the pieces (count per cell, then emit)
-constexpr int kModeEval = 0, kModeMoments = 1, kModeVjp = 2, kModeCount = 3, kModeEmit = 4, kModeMixed = 5;
+constexpr int kModeEval = 0, kModeMoments = 1, kModeVjp = 2, kModeCount = 3, kModeEmit = 4, kModeMixed = 5,
+              kModeVjpMixed = 6;
 
 // phase A's cooperative clip: the polygon being clipped (one vertex per lane) passes
 // through here between clip steps; the round's clipped pieces wait here for the list
@@ -929,11 +930,12 @@ struct ClipStage {
 
 template <int MODE>
 struct PieceWarp {
-    static constexpr int kAcc = MODE == kModeVjp || MODE == kModeMixed ? 3 : (MODE == kModeMoments ? 7 : 2);
+    static constexpr int kAcc =
+        MODE == kModeVjp || MODE == kModeVjpMixed || MODE == kModeMixed ? 3 : (MODE == kModeMoments ? 7 : 2);
     ClipStage cs;
     Slot slot[kSlotPool];
     Nb64 nb[kSlotPool];
-    float zc[MODE == kModeMixed ? kSlotPool : 1];  // mixed: each radical axis about its cell's anchor
+    float zc[MODE == kModeMixed || MODE == kModeVjpMixed ? kSlotPool : 1];  // mixed: each axis about its cell's anchor
     PieceRec rec[kList];
     double out[kAcc][kList];
     double hvc[kPV][kList];
@@ -1103,10 +1105,11 @@ __device__ __forceinline__ void finish_cell(const CellArgs& A, const CellInfo& C
 // a int rho and 2 a int rho u), and its share of g_rho on the triangle's corners,
 //     int_piece (a (w_i - |u|^2) + b_i + e_i . x) lambda_k(x)
 // for the barycentric coordinate lambda_k (linear; the integrand is cubic in u)
-template <class E>
+template <bool F32, class E>
 __device__ __forceinline__ void vjp_piece(const CellArgs& A, const E& mesh, const PieceRec& R, int k, int gi,
-                                          const SiteD& S, const Slot* sl, const Nb64* nb, const Fixed& T, double c0,
-                                          double gx, double gy, double& ow, double& ox, double& oy)
+                                          const SiteD& S, const Slot* sl, const Nb64* nb, const float* zc, double ax,
+                                          double ay, const Fixed& T, double c0, double gx, double gy, double& ow,
+                                          double& ox, double& oy)
 {
     const double a = A.cot_value;
     const double bi = A.cot_mass ? A.cot_mass[gi] : 0.0;
@@ -1114,15 +1117,17 @@ __device__ __forceinline__ void vjp_piece(const CellArgs& A, const E& mesh, cons
     const double eyi = A.cot_mom ? A.cot_mom[2 * (size_t)gi + 1] : 0.0;
     PieceMoments M;
     double gw = 0.0, gpx = 0.0, gpy = 0.0;
-    integrate_vjp(
-        (int)R.n, [&](int e) { return (int)R.lab[e]; }, nb, T, c0, gx, gy, S.x, S.y, bi, exi, eyi,
-        [&](int slot, double& bj, double& ejx, double& ejy) {
-            const int gj = A.perm[sl[slot].site];
-            bj = A.cot_mass ? A.cot_mass[gj] : 0.0;
-            ejx = A.cot_mom ? A.cot_mom[2 * (size_t)gj] : 0.0;
-            ejy = A.cot_mom ? A.cot_mom[2 * (size_t)gj + 1] : 0.0;
-        },
-        M, gw, gpx, gpy);
+    auto lab_of = [&](int e) { return (int)R.lab[e]; };
+    auto cot = [&](int slot, double& bj, double& ejx, double& ejy) {
+        const int gj = A.perm[sl[slot].site];
+        bj = A.cot_mass ? A.cot_mass[gj] : 0.0;
+        ejx = A.cot_mom ? A.cot_mom[2 * (size_t)gj] : 0.0;
+        ejy = A.cot_mom ? A.cot_mom[2 * (size_t)gj + 1] : 0.0;
+    };
+    if (F32)
+        integrate_vjp32((int)R.n, lab_of, sl, zc, ax, ay, T, c0, gx, gy, S.x, S.y, bi, exi, eyi, cot, M, gw, gpx, gpy);
+    else
+        integrate_vjp((int)R.n, lab_of, nb, T, c0, gx, gy, S.x, S.y, bi, exi, eyi, cot, M, gw, gpx, gpy);
     const double rho_m = c0 * M.I1 + gx * M.Iux + gy * M.Iuy;
     const double rux = c0 * M.Iux + gx * M.Sxx + gy * M.Sxy, ruy = c0 * M.Iuy + gx * M.Sxy + gy * M.Syy;
     ow = gw + a * rho_m;
@@ -1149,7 +1154,9 @@ __device__ __forceinline__ void vjp_piece(const CellArgs& A, const E& mesh, cons
 template <int MODE, class E>
 __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E mesh)
 {
-    constexpr bool MOM = MODE == kModeMoments, VJP = MODE == kModeVjp;
+    constexpr bool MOM = MODE == kModeMoments, VJP = MODE == kModeVjp || MODE == kModeVjpMixed;
+    // the mixed modes take the cell's integrals about its anchor (integrate_piece32)
+    constexpr bool ANCHOR = MODE == kModeMixed || MODE == kModeVjpMixed;
     constexpr bool LISTING = MODE == kModeCount || MODE == kModeEmit;
     constexpr bool MIXED = MODE == kModeMixed;
     constexpr int kAcc = PieceWarp<MODE>::kAcc;
@@ -1186,7 +1193,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
         if (my_m >= 0) {
             const double4 cb = A.cell_box[k];
             my_cnt = mesh.setup(cb, my_box);
-            if (MIXED) {
+            if (ANCHOR) {
                 const SiteD S = A.sites[k];
                 my_ax = 0.5 * (cb.x + cb.z) - S.x;
                 my_ay = 0.5 * (cb.y + cb.w) - S.y;
@@ -1226,7 +1233,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
             const Nb64 nbq = make_nb64(Q, o);
             W.nb[idx] = nbq;
             // mixed: the radical axis about the cell's anchor, 2 v.d = z - 2 a.d
-            if (MIXED) W.zc[idx] = (float)(nbq.z - 2.0 * (C.ax * nbq.dx + C.ay * nbq.dy));
+            if (ANCHOR) W.zc[idx] = (float)(nbq.z - 2.0 * (C.ax * nbq.dx + C.ay * nbq.dy));
         }
         __syncwarp();
         int f = 0;     // next flat entry
@@ -1478,8 +1485,9 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                 mesh.triangle(R.tri, o, T, c0, gx, gy);
                 if (VJP) {
                     double ow, ox, oy;
-                    vjp_piece(A, mesh, R, C.k, A.perm[C.k], S, W.slot + C.soff, W.nb + C.soff, T, c0, gx, gy, ow, ox,
-                              oy);
+                    vjp_piece<MODE == kModeVjpMixed>(A, mesh, R, C.k, A.perm[C.k], S, W.slot + C.soff, W.nb + C.soff,
+                                                     W.zc + (ANCHOR ? C.soff : 0), C.ax, C.ay, T, c0, gx, gy, ow,
+                                                     ox, oy);
                     W.out[0][p] = ow;
                     W.out[1 % kAcc][p] = ox;
                     W.out[2 % kAcc][p] = oy;
@@ -1690,6 +1698,8 @@ void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, int mode, cudaS
     GridPieces e{m};
     if (mode == kModeVjp)
         k_pieces<kModeVjp><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeVjpMixed)
+        k_pieces<kModeVjpMixed><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeCount)
         k_pieces<kModeCount><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeEmit)
@@ -1708,6 +1718,8 @@ void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, int mode, cudaStr
     TriPieces e{m};
     if (mode == kModeVjp)
         k_pieces<kModeVjp><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+    else if (mode == kModeVjpMixed)
+        k_pieces<kModeVjpMixed><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeCount)
         k_pieces<kModeCount><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeEmit)

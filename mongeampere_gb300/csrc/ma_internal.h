@@ -129,7 +129,8 @@ size_t scan_scratch_ints(int n);
 // cell kernels (ma_cells.cu)
 void launch_cells_stage1(const CellArgs& a, cudaStream_t s);
 // mode: 0 evaluation, 1 evaluation with moments, 2 adjoint (vector-Jacobian product),
-// 3 count the pieces per cell, 4 emit them, 5 evaluation with FP32 piece integrals
+// 3 count the pieces per cell, 4 emit them, 5 evaluation with FP32 piece integrals, 6 the
+// adjoint with FP32 piece integrals
 void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, int mode, cudaStream_t s);
 void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, int mode, cudaStream_t s);
 void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s);

@@ -170,3 +170,73 @@ def test_torch_autograd_binding(ctx):
     np.testing.assert_allclose(gX, rX, rtol=1e-10, atol=1e-12 * np.abs(rX).max())
     np.testing.assert_allclose(gw, rw, rtol=1e-10, atol=1e-12 * np.abs(rw).max())
     np.testing.assert_allclose(gr, rr, rtol=1e-9, atol=1e-12 * np.abs(rr).max())
+
+
+def _gpu_objective(api, ctx, mesh, X, w, a, b, e):
+    v, g, _ = api.kantorovich(mesh, X, w, hessian=False, ctx=ctx)
+    _, first = api.first_moment(mesh, X, w, ctx=ctx)
+    return a * v + float(np.dot(b, np.asarray(g))) + float(np.sum(e * np.asarray(first)))
+
+
+@pytest.mark.parametrize("solved", [False, True])
+def test_fp32_adjoint_against_fp64_adjoint_and_central_differences(ctx, solved):
+    # The FP32 adjoint (precision="mixed": the pieces' integrals in FP32 about a point of
+    # each cell) against the FP64 adjoint, at w = 0 and at the solution of a Gaussian
+    # density (cells far from their sites); and both against central differences
+    # of the GPU's FP64 forward pass on 100 random coordinates of the sites, the weights
+    # and the density's vertex values, with h = 1e-6 in each coordinate's own scale: the
+    # mean cell size 1/sqrt(n) for the sites, the mean cell area 1/n for the weights, 1 for
+    # the vertex values.  (A weight step of 1e-6 is several percent of a cell's weight
+    # scale here, and near a short edge the objective bends within it: the central
+    # difference converges to the adjoint only for smaller steps.)
+    from mongeampere_gb300 import api
+    p = W.make_problem(128, 20000, "gauss", "uniform", "random", seed=21)
+    X = np.c_[p.x, p.y]
+    w = np.zeros(p.n)
+    if solved:
+        w = np.asarray(api.ot_solve(p.mesh, X, p.nu, eps_g=1e-6, stop="rel", ctx=ctx))
+    a, b, e = _cotangents(p.n, 8)
+    g64 = api.kantorovich_vjp(p.mesh, X, w, a, b, e, ctx=ctx)
+    g32 = api.kantorovich_vjp(p.mesh, X, w, a, b, e, precision="mixed", ctx=ctx)
+    for q64, q32 in zip(g64, g32):
+        q64, q32 = np.asarray(q64), np.asarray(q32)
+        assert np.linalg.norm(q32 - q64) <= 1e-4 * np.linalg.norm(q64)
+    rng = np.random.default_rng(9)
+    vals = p.mesh.values.copy()
+    dm = ctx.mesh(p.mesh)
+    kinds = rng.integers(0, 4, 100)
+    fd, ad64, ad32 = [], [], []
+    for kind in kinds:
+        if kind < 2:  # a site coordinate
+            i = int(rng.integers(p.n))
+            def f(t):
+                Xp = X.copy()
+                Xp[i, kind] += t
+                return _gpu_objective(api, ctx, dm, Xp, w, a, b, e)
+            ad64.append(g64[0][i, kind])
+            ad32.append(g32[0][i, kind])
+        elif kind == 2:  # a weight
+            i = int(rng.integers(p.n))
+            def f(t):
+                wp = w.copy()
+                wp[i] += t
+                return _gpu_objective(api, ctx, dm, X, wp, a, b, e)
+            ad64.append(g64[1][i])
+            ad32.append(g32[1][i])
+        else:  # a density vertex value
+            j = int(rng.integers(vals.size))
+            def f(t):
+                vp = vals.copy().reshape(-1)
+                vp[j] += t
+                dm.set_values(vp)
+                r = _gpu_objective(api, ctx, dm, X, w, a, b, e)
+                dm.set_values(vals.reshape(-1))
+                return r
+            ad64.append(g64[2][j])
+            ad32.append(g32[2][j])
+        hk = FD_H * (1.0 / p.n if kind == 2 else (p.n ** -0.5 if kind < 2 else 1.0))
+        fd.append((f(hk) - f(-hk)) / (2 * hk))
+    fd, ad64, ad32 = np.array(fd), np.array(ad64), np.array(ad32)
+    scale = np.abs(fd).max()
+    assert np.max(np.abs(ad64 - fd)) <= FD_RTOL * scale, f"FP64 adjoint vs FD: {np.max(np.abs(ad64 - fd)) / scale:.2e}"
+    assert np.max(np.abs(ad32 - fd)) <= 1e-4 * scale, f"FP32 adjoint vs FD: {np.max(np.abs(ad32 - fd)) / scale:.2e}"
