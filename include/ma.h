@@ -299,8 +299,9 @@ ma_status ma_laplacian_solve_static(int64_t n, const int32_t* rowptr, const int3
  *               radical axis it lies on (original index; the reference's EDGE_DT), or
  *               -1-e for edge e (v_e -> v_e+1) of the triangle (EDGE_T)
  * Pieces are ordered by cell (in the site index's Morton order), then by triangle.
- * Cells of more than 48 neighbours, or whose pieces need exact predicates, are not
- * listed (MA_ERR_CAPACITY). */
+ * Cells of more than 48 neighbours, or whose clips meet exact ties (lattice sites,
+ * bisectors through mesh vertices), are listed by a one-thread-per-cell pass with exact
+ * predicates; MA_ERR_CAPACITY only for a cell beyond its 256 slots. */
 ma_status ma_pieces(ma_ctx* ctx, const ma_mesh* mesh, int64_t n, const double* x, const double* y,
                     const double* w, ma_mem mem, int64_t* npieces, int64_t* nverts);
 ma_status ma_pieces_copy(ma_ctx* ctx, int32_t* site, int32_t* tri, int64_t* off, double* xy, int32_t* edge,

@@ -310,11 +310,30 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         // the count pass is done: offsets, then the emit pass over the same cells
         c->have_h = false;
         c->have_pieces = false;
-        if (nredo > 0)
-            return fail(c, MA_ERR_CAPACITY,
-                        "the pieces are listed for cells of at most 48 neighbours whose pieces need no exact "
-                        "predicate");
         if ((uint32_t)c->hinfo[1] & ST_BAD_INPUT) return fail(c, MA_ERR_INVALID_ARGUMENT, "non-finite site or weight");
+        // cells beyond stage 1's capacity or whose clips meet exact ties: counted (and
+        // below emitted) one thread per cell with exact predicates
+        CellArgs b = a;
+        const MeshGridDev gd = m->grid_dev();
+        const MeshTriDev td = m->tri_dev();
+        if (nredo > 0) {
+            b.abort_flag = nullptr;
+            b.work = c->redo.as<int>();
+            b.nwork = nredo;
+            MA_CUDA(c, c->big_work.ensure(large_work_bytes() * (size_t)nredo));
+            b.scratch = c->big_work.p;
+            b.nredo = c->nredo.as<int>() + 1;
+            {
+                ProfScope ps(c, &c->profile.cells_large_ms, &c->profile.cells_large_launches);
+                launch_cells_large_list(b, m->kind == 0 ? &gd : nullptr, m->kind == 0 ? nullptr : &td, false, s);
+            }
+            c->launches += 2;
+            c->profile.large_sites += nredo;
+            MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+            MA_CUDA(c, ctx_sync(c));
+            if (c->hinfo[0] > 0)
+                return fail(c, MA_ERR_CAPACITY, "a Laguerre cell has more vertices than the largest kernel capacity");
+        }
         launch_scan(c->pc_cnt.as<int>(), c->pc_base.as<int>(), n, c->scan_scratch.as<int>(), s);
         launch_scan(c->pv_cnt.as<int>(), c->pv_base.as<int>(), n, c->scan_scratch.as<int>(), s);
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 4, c->pc_base.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -338,6 +357,17 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         else
             launch_pieces_tri(a, m->tri_dev(), 4, s);
         c->launches += 5;
+        if (nredo > 0) {
+            b.pc_base = a.pc_base;
+            b.pv_base = a.pv_base;
+            b.out_site = a.out_site;
+            b.out_tri = a.out_tri;
+            b.out_off = a.out_off;
+            b.out_xy = a.out_xy;
+            b.out_edge = a.out_edge;
+            launch_cells_large_list(b, m->kind == 0 ? &gd : nullptr, m->kind == 0 ? nullptr : &td, true, s);
+            c->launches += 1;
+        }
         MA_CUDA(c, cudaMemcpyAsync(c->pc_off.as<int64_t>() + np, &nv, sizeof(int64_t), cudaMemcpyHostToDevice, s));
         MA_CUDA(c, ctx_sync(c));
         c->npieces = np;

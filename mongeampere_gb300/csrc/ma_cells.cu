@@ -149,7 +149,7 @@ struct GridVisitor {
                 for (int tt = 0; tt < 2; tt++) {
                     double c0, gx, gy;
                     grid_triangle(m, i, j, tt, o, T, c0, gx, gy);
-                    fn(T, c0, gx, gy);
+                    fn(T, c0, gx, gy, ((j * (m.nx - 1) + i) << 1) | tt);
                 }
     }
 };
@@ -189,7 +189,7 @@ struct TriVisitor {
                     if (bx != max(r.x, cx0) || by != max(r.y, cy0)) continue;
                     double c0, gx, gy;
                     tri_triangle(m, t, o, T, c0, gx, gy);
-                    fn(T, c0, gx, gy);
+                    fn(T, c0, gx, gy, t);
                 }
             }
         }
@@ -369,7 +369,7 @@ __device__ void process_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>&
             W.hv[s] = 0.0;
         }
         bool bad = false;
-        M.visit(o, bb.x, bb.y, bb.z, bb.w, [&](const Fixed& T, double c0, double gx, double gy) {
+        M.visit(o, bb.x, bb.y, bb.z, bb.w, [&](const Fixed& T, double c0, double gx, double gy, int) {
             if (bad) return;
             if (!piece<CAP, MOM, true>(T, c0, gx, gy, W.slots, W.nb, m, o, A.sites, P, Q, acc, W.hv, touched, st))
                 bad = true;
@@ -381,6 +381,94 @@ __device__ void process_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>&
         }
     }
     write_site<MOM>(A, gi, S, acc, m, W.slots, W.nb, W.hv, touched.w, W.cols, W.vals, big_slot);
+    if (st) atomicOr(A.status, st);
+}
+
+// The pieces of one cell, one thread per cell with exact predicates (the large-capacity
+// pass of ma_pieces: cells beyond stage 1's capacity, or whose clips meet exact ties):
+// count them (pc_cnt, pv_cnt) or emit them at the cell's offsets, in the order of the
+// warp kernel (triangles in the mesh's order under the cell's box, every triangle
+// clipped by the neighbours in site order, vertex e the start of edge e).
+template <int CAP, bool EMIT, class Mesh>
+__device__ void list_site(const CellArgs& A, const Mesh& M, int k, Work<CAP>& W)
+{
+    const SiteD S = A.sites[k];
+    const int gi = A.perm[k];
+    Owner o{S.x, S.y, S.w, k};
+    Poly<CAP>* P = &W.PA;
+    Poly<CAP>* Q = &W.PB;
+    CellOut c = cell_stage<CAP, true>(A, k, S, o, domain_box(A, o), W.slots, W.map, P, Q);
+    uint32_t st = c.st;
+    bool bad = c.overflow;
+    int np = 0, nv = 0;
+    int64_t gp = EMIT ? A.pc_base[k] : 0, gv = EMIT ? A.pv_base[k] : 0;
+    const int m = c.empty ? 0 : c.ns;
+    if (!bad && !c.empty && P->n > 0) {
+        const double4 bb = cell_box(*P, S, A);
+        for (int s = 1; s < m; s++) {
+            const Slot v = W.slots[s];
+            int r = s - 1;
+            while (r >= 0 && W.slots[r].site > v.site) {
+                W.slots[r + 1] = W.slots[r];
+                r--;
+            }
+            W.slots[r + 1] = v;
+        }
+        for (int s = 0; s < m; s++) W.nb[s] = make_nb64(A.sites[W.slots[s].site], o);
+        M.visit(o, bb.x, bb.y, bb.z, bb.w, [&](const Fixed& T, double, double, double, int id) {
+            if (bad) return;
+            Poly<CAP>* Wp = P;
+            Poly<CAP>* Vp = Q;
+            Wp->n = 3;
+            for (int e = 0; e < 3; e++) {
+                Wp->lab[e] = -1 - e;
+                Wp->ux[e] = T.ux[e];
+                Wp->uy[e] = T.uy[e];
+                Wp->ur[e] = T.ur[e];
+            }
+            bool overflow = false;
+            for (int s = 0; s < m && Wp->n > 0; s++) {
+                if (clip_poly<CAP, true>(*Wp, *Vp, s, W.slots, T, o, A.sites, st, overflow)) {
+                    if (overflow) {
+                        bad = true;
+                        return;
+                    }
+                    Poly<CAP>* t = Wp;
+                    Wp = Vp;
+                    Vp = t;
+                }
+            }
+            const int n = Wp->n;
+            if (n == 0) return;
+            if (EMIT) {
+                A.out_site[gp] = gi;
+                A.out_tri[gp] = id;
+                A.out_off[gp] = gv;
+                for (int e = 0; e < n; e++) {
+                    double X, Y;
+                    vtx64(Wp->lab[e == 0 ? n - 1 : e - 1], Wp->lab[e], W.nb, T, X, Y);
+                    A.out_xy[2 * (gv + e)] = S.x + X;
+                    A.out_xy[2 * (gv + e) + 1] = S.y + Y;
+                    const int l = Wp->lab[e];
+                    A.out_edge[gv + e] = l >= 0 ? A.perm[W.slots[l].site] : l;
+                }
+            }
+            np++;
+            nv += n;
+            gp++;
+            gv += n;
+        });
+    }
+    if (bad) {
+        atomicAdd(A.nredo, 1);  // beyond every capacity: the call fails
+        atomicOr(A.status, ST_POLY_OVERFLOW);
+        return;
+    }
+    if (!EMIT) {
+        A.pc_cnt[k] = np;
+        A.pv_cnt[k] = nv;
+    }
+    st &= ~(uint32_t)ST_NEED_EXACT;
     if (st) atomicOr(A.status, st);
 }
 
@@ -1673,6 +1761,41 @@ __global__ void __launch_bounds__(64) k_cells_large(CellArgs A, Mesh M)
     if (t >= A.nwork) return;
     Work<CAP>* W = reinterpret_cast<Work<CAP>*>(A.scratch) + t;
     process_site<CAP, MOM>(A, M, A.work[t], *W, t);
+}
+
+template <bool EMIT, class Mesh>
+__global__ void __launch_bounds__(64) k_cells_large_list(CellArgs A, Mesh M)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.nwork) return;
+    Work<kCapLarge>* W = reinterpret_cast<Work<kCapLarge>*>(A.scratch) + t;
+    list_site<kCapLarge, EMIT>(A, M, A.work[t], *W);
+}
+
+__global__ void k_mark_large(const int* work, int nwork, int* nb_cnt)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nwork) nb_cnt[work[t]] = -3;
+}
+
+void launch_cells_large_list(const CellArgs& a, const MeshGridDev* g, const MeshTriDev* tm, bool emit, cudaStream_t s)
+{
+    if (a.nwork <= 0) return;
+    const int nb = (a.nwork + 63) / 64;
+    if (!emit) k_mark_large<<<(a.nwork + 255) / 256, 256, 0, s>>>(a.work, a.nwork, a.nb_cnt);
+    if (g) {
+        GridVisitor v{*g};
+        if (emit)
+            k_cells_large_list<true><<<nb, 64, 0, s>>>(a, v);
+        else
+            k_cells_large_list<false><<<nb, 64, 0, s>>>(a, v);
+    } else {
+        TriVisitor v{*tm};
+        if (emit)
+            k_cells_large_list<true><<<nb, 64, 0, s>>>(a, v);
+        else
+            k_cells_large_list<false><<<nb, 64, 0, s>>>(a, v);
+    }
 }
 
 size_t large_work_bytes() { return sizeof(Work<kCapLarge>); }

@@ -136,6 +136,12 @@ void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, int mode, cudaStr
 void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s);
 void launch_cells_large_tri(const CellArgs& a, const MeshTriDev& m, bool mom, cudaStream_t s);
 int stage1_cap();
+// the pieces of the cells a.work[0..a.nwork) (sorted indices), one thread per cell with
+// exact predicates: count them (pc_cnt, pv_cnt; the cells' nb_cnt become -3 so that the
+// warp kernel's emit pass leaves them) or emit them; a cell beyond every capacity adds 1
+// to *a.nredo.  g (grid) or tm (triangles) is the mesh.
+void launch_cells_large_list(const CellArgs& a, const MeshGridDev* g, const MeshTriDev* tm, bool emit,
+                             cudaStream_t s);
 void launch_csr_compact(int n, const int* rowptr, const int* rowcnt, const int* st_col, const double* st_val,
                         int scap, const int* big_index, const int* big_col, const double* big_val, int big_cap,
                         int* col, double* val, cudaStream_t s);

@@ -406,7 +406,8 @@ def lloyd(mesh, x, y, w, mode: int = 1):
     """lloyd.hpp:126-144: masses and centroids (first moments / mass)."""
     r = kantorovich(mesh, x, y, w, mode=mode)
     m = r.moments[:, 0]
-    c = r.moments[:, 1:3] / m[:, None]
+    c = np.full((m.shape[0], 2), np.nan)  # an empty cell has no centroid
+    np.divide(r.moments[:, 1:3], m[:, None], out=c, where=m[:, None] > 0)
     return m, c
 
 

@@ -66,3 +66,38 @@ def test_pieces_tile_the_domain_at_scale(ctx):
     tri_area = np.bincount(P.tri, weights=area, minlength=2 * 127 * 127)
     np.testing.assert_allclose(tri_area, 0.5 / 127 ** 2, rtol=1e-10)
     assert np.unique(P.site).shape[0] == p.n
+
+
+def _lattice(k):
+    g = (np.arange(k) + 0.5) / k
+    X, Y = np.meshgrid(g, g)
+    return X.ravel().copy(), Y.ravel().copy()
+
+
+def test_pieces_of_an_exactly_degenerate_lattice(ctx, oracle):
+    # Lattice sites: every vertex of every cell is co-circular with four sites and the
+    # bisectors run through mesh vertices, so the clips meet exact ties, which send the
+    # cells to the one-thread exact pass (the reference lists these pieces too,
+    # voronoi_triangulation_intersection.hpp:315-343).  The pieces tile the square, each
+    # cell is its 1/256 square, and the pieces of positive area are the oracle's.
+    from mongeampere_gb300 import api
+    from mongeampere_gb300.mesh import unit_grid
+    x, y = _lattice(16)
+    mesh = unit_grid(9, np.ones((9, 9)))
+    w = np.zeros(x.size)
+    P = api.pieces(mesh, np.c_[x, y], w, ctx=ctx)
+    area = np.array([_area(P.polygon(k)[0]) for k in range(len(P.site))])
+    assert area.min() >= -1e-15
+    assert abs(area.sum() - 1.0) < 1e-12
+    np.testing.assert_allclose(np.bincount(P.site, weights=area, minlength=x.size), 1.0 / x.size, rtol=1e-12)
+    np.testing.assert_allclose(np.bincount(P.tri, weights=area, minlength=2 * 64), 0.5 / 64, rtol=1e-12)
+    r = oracle.kantorovich(mesh, x, y, w, keep_pieces=True, arith="dd")
+    R = r.pieces
+    oarea = np.array([_area(R.xy[R.offsets[k]:R.offsets[k + 1]]) for k in range(len(R.site))])
+    gpu = {(int(s), int(t)) for s, t, a in zip(P.site, P.tri, area) if a > 1e-14}
+    ora = {(int(s), int(t)) for s, t, a in zip(R.site, R.face, oarea) if a > 1e-14}
+    assert gpu == ora
+    # the drawing goes through the same listing: colour 1 and a constant density give
+    # each pixel's covered area
+    img = api.draw_laguerre_diagram(mesh, np.c_[x, y], w, np.ones(x.size), (0, 0, 1, 1), 64, 64, ctx=ctx)
+    np.testing.assert_allclose(img, 1.0, rtol=0, atol=1e-12)
