@@ -115,7 +115,7 @@ typedef struct ma_profile {
     double amg_setup_ms;      /* multigrid hierarchy: fine matrix, aggregation, Galerkin levels */
     int64_t amg_levels;       /* levels of the last hierarchy */
     int64_t mixed[4];         /* mixed-precision evaluations: pieces integrated, cells redone in
-                                 FP64 (their certified FP32 mass error above 2^-14), radical-axis
+                                 FP64 (their certified FP32 mass error above 2^-12), radical-axis
                                  edges, edges integrated in FP64 */
 } ma_profile;
 /* enable != 0: reset the profile and start recording; 0: stop. */

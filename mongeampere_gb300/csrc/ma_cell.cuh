@@ -640,12 +640,12 @@ struct CompF {
 // R), the fan sums are compensated FP32 sums.  The certified radii give two bounds:
 //   err_mass: the piece's mass moves by at most 1/2 sum over its edges of
 //   (R_a + R_b) |e|_1 times the largest density on it; the caller sums these per cell and
-//   redoes in FP64 a cell whose total exceeds kMassTol32 of its mass;
+//   redoes in FP64 a cell whose total exceeds kMassTol32 (2.4e-4) of its mass;
 //   a radical-axis edge is integrated in FP64 (vtx64, site-relative) when 2 (R_a + R_b)
 //   exceeds kEdgeTol32 of its length |e|_1: crs = |e x d| = |e| |d| with
 //   |e| >= |e|_1 / sqrt 2, so a kept edge is within kEdgeTol32 plus a few FP32 roundings,
 //   and every Hessian entry, a sum of edges of one sign, within ~2.5e-4 of the FP64 one.
-constexpr float kMassTol32 = 0x1p-14f;
+constexpr float kMassTol32 = 0x1p-12f;
 constexpr float kEdgeTol32 = 0x1p-12f;
 
 // a triangle's corners about the anchor (FP32 values and error radii)

@@ -277,7 +277,7 @@ def test_continuation_solves_clustered_sites(ctx, oracle):
 def test_mixed_precision_with_cells_far_from_their_sites(ctx):
     # at the solution of a 20-fold density contrast the cells lie many cell sizes from
     # their sites; the mixed integrals are taken about a point of the cell, so their
-    # error stays that of the FP32 certified bounds: masses within 2^-14, every Hessian
+    # error stays that of the FP32 certified bounds: masses within 2^-12, every Hessian
     # entry within 2.5e-4 of the FP64 evaluation
     from mongeampere_gb300 import api
     p = W.make_problem(256, 20000, "gauss", "uniform", "random", seed=11)
@@ -287,7 +287,7 @@ def test_mixed_precision_with_cells_far_from_their_sites(ctx):
     v32, g32, h32 = api.kantorovich(p.mesh, X, w, precision="mixed", ctx=ctx)
     g64, g32 = np.asarray(g64), np.asarray(g32)
     rel = np.abs(g32 - g64) / g64
-    assert rel.max() <= 2.0 ** -14, f"mixed mass off by {rel.max():.3e}"
+    assert rel.max() <= 2.0 ** -12, f"mixed mass off by {rel.max():.3e}"
     assert abs(v32 - v64) <= 1e-6 * abs(v64)
     np.testing.assert_array_equal(h32.col, h64.col)
     hrel = np.abs(np.asarray(h32.val) - np.asarray(h64.val)) / np.abs(np.asarray(h64.val))
