@@ -478,6 +478,8 @@ def run_c5(args, ctx, dev, rank):
         X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
         items.append((dm, X, torch.tensor(p.nu, device=dev)))
     prec = "mixed"
+    clocks = ClockSampler(0)
+    clocks.start()
     # sequential
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -497,6 +499,7 @@ def run_c5(args, ctx, dev, rank):
         torch.cuda.synchronize()
         runs.append((time.perf_counter() - t0, used, stats))
     t_b, used, stats = runs[-1]
+    clk = clocks.stop()
     ok = sum(int(s.status == 0 and s.max_rel_err <= 1e-6) for s in stats)
     sites = int(sum(p.n for p in probs))
     out = {"metric": METRIC, "workload": "c5", "n_gpus": 1,
@@ -505,7 +508,7 @@ def run_c5(args, ctx, dev, rank):
            "total_sites": sites, "sequential_problems_per_s": len(probs) / t_seq,
            "batched_problems_per_s": len(probs) / t_b, "batched_speedup": t_seq / t_b,
            "workers": used, "first_batch_s_with_autotune": runs[0][0], "batched_s": t_b, "sequential_s": t_seq,
-           "converged_sequential": seq_ok, "converged_batched": ok}
+           "converged_sequential": seq_ok, "converged_batched": ok, "clocks": clk}
     if rank == 0:
         print(json.dumps(out))
 

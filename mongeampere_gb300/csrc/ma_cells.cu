@@ -1252,16 +1252,20 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
     __shared__ PieceWarp<MODE> shw[kPieceWarps];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     PieceWarp<MODE>& W = shw[wib];
+    // the cells: sorted indices kbase .. kbase + 7, or entries of a cell list (the
+    // mixed form's cells redone in FP64)
+    const int ntot = A.cell_list ? A.ncell_list : A.n;
+    auto cell_at = [&](int q) { return A.cell_list ? A.cell_list[q] : q; };
     const int kbase = (blockIdx.x * kPieceWarps + wib) * kWarpCells;
-    if (kbase >= A.n) return;
+    if (kbase >= ntot) return;
     if (A.abort_flag && *(volatile const int*)A.abort_flag) return;
-    const int ncell = min(kWarpCells, A.n - kbase);
+    const int ncell = min(kWarpCells, ntot - kbase);
     // lane c sets up cell c
     int my_m = -2, my_cnt = 0;
     int4 my_box = make_int4(0, 0, 0, 0);
     double my_ax = 0.0, my_ay = 0.0;
     if (lane < ncell) {
-        const int k = kbase + lane;
+        const int k = cell_at(kbase + lane);
         my_m = A.nb_cnt[k];
         if (my_m == -1) {
             const int gi = A.perm[k];
@@ -1301,7 +1305,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
             const int used = max(mc, 0);
             if (soff + used > kSlotPool) break;
             const double cax = __shfl_sync(kFull, my_ax, g1), cay = __shfl_sync(kFull, my_ay, g1);
-            if (lane == 0) W.ci[g1 - g0] = CellInfo{kbase + g1, mc, soff, pre, bx, 0, 0, cax, cay};
+            if (lane == 0) W.ci[g1 - g0] = CellInfo{cell_at(kbase + g1), mc, soff, pre, bx, 0, 0, cax, cay};
             soff += used;
             pre += nc;
             g1++;
@@ -1701,12 +1705,15 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                 if (!complete) break;
                 if (C.m >= 0) {
                     // mixed: a cell whose certified FP32 mass error exceeds kMassTol32 of its
-                    // mass is redone in FP64 by the large-capacity pass
-                    if (MIXED && !(run[2 % kAcc] <= (double)kMassTol32 * fabs(run[0]))) {
-                        redo |= 1u << (g0 + cfin);
-                        if (lane == 0) mx_fa++;
-                    }
-                    if ((redo >> (g0 + cfin)) & 1u) {
+                    // mass is redone by the FP64 pieces kernel (its cell list)
+                    const bool fp64_redo = MIXED && !((redo >> (g0 + cfin)) & 1u) &&
+                                           !(run[2 % kAcc] <= (double)kMassTol32 * fabs(run[0]));
+                    if (fp64_redo) {
+                        if (lane == 0) {
+                            A.redo64[atomicAdd(A.nredo64, 1)] = C.k;
+                            mx_fa++;
+                        }
+                    } else if ((redo >> (g0 + cfin)) & 1u) {
                         if (lane == 0) {
                             A.redo[atomicAdd(A.nredo, 1)] = C.k;
                             atomicOr(A.status, ST_POLY_OVERFLOW);
@@ -1817,42 +1824,44 @@ static unsigned pieces_blocks(int n)
 
 void launch_pieces_grid(const CellArgs& a, const MeshGridDev& m, int mode, cudaStream_t s)
 {
-    if (a.n <= 0) return;
+    if (a.n <= 0 || (a.cell_list && a.ncell_list <= 0)) return;
+    const int nc = a.cell_list ? a.ncell_list : a.n;
     GridPieces e{m};
     if (mode == kModeVjp)
-        k_pieces<kModeVjp><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeVjp><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeVjpMixed)
-        k_pieces<kModeVjpMixed><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeVjpMixed><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeCount)
-        k_pieces<kModeCount><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeCount><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeEmit)
-        k_pieces<kModeEmit><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeEmit><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeMixed)
-        k_pieces<kModeMixed><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeMixed><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeMoments)
-        k_pieces<kModeMoments><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeMoments><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else
-        k_pieces<kModeEval><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeEval><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
 }
 
 void launch_pieces_tri(const CellArgs& a, const MeshTriDev& m, int mode, cudaStream_t s)
 {
-    if (a.n <= 0) return;
+    if (a.n <= 0 || (a.cell_list && a.ncell_list <= 0)) return;
+    const int nc = a.cell_list ? a.ncell_list : a.n;
     TriPieces e{m};
     if (mode == kModeVjp)
-        k_pieces<kModeVjp><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeVjp><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeVjpMixed)
-        k_pieces<kModeVjpMixed><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeVjpMixed><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeCount)
-        k_pieces<kModeCount><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeCount><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeEmit)
-        k_pieces<kModeEmit><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeEmit><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeMixed)
-        k_pieces<kModeMixed><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeMixed><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else if (mode == kModeMoments)
-        k_pieces<kModeMoments><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeMoments><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
     else
-        k_pieces<kModeEval><<<pieces_blocks(a.n), 32 * kPieceWarps, 0, s>>>(a, e);
+        k_pieces<kModeEval><<<pieces_blocks(nc), 32 * kPieceWarps, 0, s>>>(a, e);
 }
 
 void launch_cells_large_grid(const CellArgs& a, const MeshGridDev& m, bool mom, cudaStream_t s)

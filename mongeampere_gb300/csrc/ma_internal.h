@@ -95,6 +95,10 @@ struct CellArgs {
     int64_t* out_off;    //                  first vertex
     double* out_xy;      // emit, per vertex: absolute position (x, y)
     int* out_edge;       //                  the edge starting there: neighbour site, or -1-e for triangle edge e
+    const int* cell_list;    // k_pieces: the sorted indices of the cells to do (null: all n)
+    int ncell_list;
+    int* redo64;             // mixed form: cells whose certified FP32 mass error is too large,
+    int* nredo64;            // redone by the FP64 pieces kernel
     void* scratch;           // large-capacity pass: one workspace per work item
     int* big_index;          // per site: row slot in the side buffer, -1 otherwise
     int* big_col;

@@ -98,6 +98,7 @@ struct Ctx {
     // evaluation outputs
     DevBuf mass, vpart, mom, rowcnt, st_col, st_val, rowptr, col, val, status, redo, nredo, stat_partial, stat_out;
     DevBuf big_index, big_col, big_val, big_work;  // large-capacity pass
+    DevBuf redo64;                                 // mixed form: cells redone in FP64
     DevBuf nb_cnt, nb_lab, cell_box;               // stage 1 -> stage 2
     bool prev_valid = false;                       // nb_cnt/nb_lab match the current site index
     DevBuf abortf;                                 // empty-cell flag of a line-search trial
