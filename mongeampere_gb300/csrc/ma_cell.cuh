@@ -637,7 +637,8 @@ struct CompF {
 // the anchor, per piece, and each radical axis's offset about the anchor, once per cell
 // and neighbour (zc): the axis {u : 2 u.d = z} becomes {v : 2 v.d = z - 2 a.d}.  The vertices come from the
 // certified FP32 constructions (vtx_fixed_bis, vtx_bis_bis: a value and an error radius
-// R), the fan sums are compensated FP32 sums.  The certified radii give two bounds:
+// R); the mass's fan sums are compensated, the moments' plain FP32.  The certified radii
+// give two bounds:
 //   err_mass: the piece's mass moves by at most 1/2 sum over its edges of
 //   (R_a + R_b) |e|_1 times the largest density on it; the caller sums these per cell and
 //   redoes in FP64 a cell whose total exceeds kMassTol32 (2.4e-4) of its mass;
@@ -706,8 +707,11 @@ MA_HD void integrate_piece32(int n, const Lab& lab_of, const Slot* slots, const 
     const float caf = (float)(c0 + gx * ax + gy * ay), gxf = (float)gx, gyf = (float)gy;
     float x0 = 0.0f, y0 = 0.0f, r0 = 0.0f;
     float vx = 0.0f, vy = 0.0f, vr = 0.0f;
-    CompF m0{0, 0}, m1x{0, 0}, m1y{0, 0}, q2{0, 0}, c3x{0, 0}, c3y{0, 0}, sxx{0, 0}, syy{0, 0}, sxy{0, 0};
-    float errA = 0.0f, vmax = 0.0f;
+    // the mass's sums compensated; the value part's moments as plain FP32 sums (at most 12
+    // terms, each with its own product rounding, which the error bound below counts)
+    CompF m0{0, 0}, m1x{0, 0}, m1y{0, 0};
+    float q2 = 0.0f, c3x = 0.0f, c3y = 0.0f, sxx = 0.0f, syy = 0.0f, sxy = 0.0f;
+    float errA = 0.0f, vmax = 0.0f, acr = 0.0f;
     // vertex k + 1 in iteration k; iteration -1 makes vertex 0 (one copy of the constructions)
     for (int k = -1; k < n; k++) {
         const int lab = k < 0 ? lab_of(n - 1) : lab_of(k);
@@ -730,17 +734,18 @@ MA_HD void integrate_piece32(int n, const Lab& lab_of, const Slot* slots, const 
         errA += (vr + br) * e1;
         vmax = fmaxf(vmax, fabsf(bx) + fabsf(by) + br);
         const float cr = vx * by - vy * bx;
+        acr += fabsf(vx * by) + fabsf(vy * bx);
         const float aa = vx * vx + vy * vy, ab = vx * bx + vy * by, bb = bx * bx + by * by;
         m0.add(cr);
         m1x.add(cr * (vx + bx));
         m1y.add(cr * (vy + by));
-        q2.add(cr * (aa + ab + bb));
+        q2 += cr * (aa + ab + bb);
         const float ka = 3.0f * aa + 2.0f * ab + bb, kb = aa + 2.0f * ab + 3.0f * bb;
-        c3x.add(cr * (vx * ka + bx * kb));
-        c3y.add(cr * (vy * ka + by * kb));
-        sxx.add(cr * (2.0f * (vx * vx + bx * bx) + 2.0f * vx * bx));
-        syy.add(cr * (2.0f * (vy * vy + by * by) + 2.0f * vy * by));
-        sxy.add(cr * (2.0f * (vx * vy + bx * by) + vx * by + bx * vy));
+        c3x += cr * (vx * ka + bx * kb);
+        c3y += cr * (vy * ka + by * kb);
+        sxx += cr * (2.0f * (vx * vx + bx * bx) + 2.0f * vx * bx);
+        syy += cr * (2.0f * (vy * vy + by * by) + 2.0f * vy * by);
+        sxy += cr * (2.0f * (vx * vy + bx * by) + vx * by + bx * vy);
         if (lab >= 0) {
             nedge++;
             if (2.0f * (vr + br) <= kEdgeTol32 * e1) {
@@ -757,15 +762,16 @@ MA_HD void integrate_piece32(int n, const Lab& lab_of, const Slot* slots, const 
         vr = br;
     }
     const float A2 = m0.val();  // twice the area
-    // the vertices' radii, and the FP32 roundings of the sum (a few ulps of its terms)
-    err_mass = 0.5 * ((double)errA + 4.0 * (double)kU32 * (double)fabsf(A2)) *
+    // the vertices' radii, and the FP32 roundings of the products and the sum (a few ulps
+    // of the terms' magnitudes, which can exceed the piece's area: slivers)
+    err_mass = 0.5 * ((double)errA + 4.0 * (double)kU32 * (double)acr) *
                ((double)fabsf(caf) + ((double)fabsf(gxf) + (double)fabsf(gyf)) * (double)vmax);
     // int rho, int rho v, int rho |v|^2 about the anchor (fan from it, see integrate_labels)
     const float I1 = A2 * 0.5f, Ivx = m1x.val() * (1.0f / 6.0f), Ivy = m1y.val() * (1.0f / 6.0f);
-    const float Sxx = sxx.val() * (1.0f / 24.0f), Syy = syy.val() * (1.0f / 24.0f), Sxy = sxy.val() * (1.0f / 24.0f);
+    const float Sxx = sxx * (1.0f / 24.0f), Syy = syy * (1.0f / 24.0f), Sxy = sxy * (1.0f / 24.0f);
     const float rm = caf * I1 + gxf * Ivx + gyf * Ivy;
     const float rvx = caf * Ivx + gxf * Sxx + gyf * Sxy, rvy = caf * Ivy + gxf * Sxy + gyf * Syy;
-    const float rq = caf * (q2.val() * (1.0f / 12.0f)) + gxf * (c3x.val() * (1.0f / 60.0f)) + gyf * (c3y.val() * (1.0f / 60.0f));
+    const float rq = caf * (q2 * (1.0f / 12.0f)) + gxf * (c3x * (1.0f / 60.0f)) + gyf * (c3y * (1.0f / 60.0f));
     // int rho |u|^2 with u = v + a: int rho |v|^2 + 2 a . int rho v + |a|^2 int rho
     mass = (double)rm;
     second = (double)rq + 2.0 * (ax * (double)rvx + ay * (double)rvy) + (ax * ax + ay * ay) * (double)rm;

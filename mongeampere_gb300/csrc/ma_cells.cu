@@ -21,6 +21,7 @@
 // or more than 12 vertices, are redone end to end by k_cells_large, one thread per
 // cell with a 256-slot workspace in global scratch.
 #include <climits>
+#include <type_traits>
 
 #include "ma_internal.h"
 
@@ -1026,7 +1027,10 @@ struct PieceWarp {
     float zc[MODE == kModeMixed || MODE == kModeVjpMixed ? kSlotPool : 1];  // mixed: each axis about its cell's anchor
     PieceRec rec[kList];
     double out[kAcc][kList];
-    double hvc[kPV][kList];
+    // the Hessian part of each listed piece's edges; FP32 in the mixed evaluation (its
+    // edges are FP32 integrals, or FP64 ones that need only 2.5e-4), which leaves room
+    // for one more block per SM
+    typename std::conditional<MODE == kModeMixed, float, double>::type hvc[kPV][kList];
     CellInfo ci[kWarpCells + 1];
     short epre[kList + 1];  // phase C: first contribution of each of the cell's listed pieces
     signed char lead[64];   // phase C: the lane holding each slot's sum of a batch, or -1
