@@ -43,6 +43,17 @@ struct SiteD {
     double x, y, w, pad;
 };
 
+// element e of a small fixed-size array by a chain of selects: a runtime index into a
+// local array would place the whole array in local memory
+template <class T, int N>
+MA_HD T pick(const T (&a)[N], int e)
+{
+    T v = a[0];
+#pragma unroll
+    for (int k = 1; k < N; k++) v = e == k ? a[k] : v;
+    return v;
+}
+
 // A site whose radical axis (with the owner) bounds, or may bound, the polygon.
 // d = x_site - x_owner, z = |d|^2 - (w_site - w_owner); the radical axis is
 // {u : 2 u.d = z} in owner-relative coordinates u, and u is strictly closer to
@@ -380,7 +391,8 @@ template <class FX>
 MA_HD void vtx_fixed_bis(const FX& fx, int e, const Slot& a, float& ux, float& uy, float& ur)
 {
     int e1 = (e + 1 == fx.n) ? 0 : e + 1;
-    vtx_seg_bis(fx.ux[e], fx.uy[e], fx.ur[e], fx.ux[e1], fx.uy[e1], fx.ur[e1], a, ux, uy, ur);
+    vtx_seg_bis(pick(fx.ux, e), pick(fx.uy, e), pick(fx.ur, e), pick(fx.ux, e1), pick(fx.uy, e1), pick(fx.ur, e1), a,
+                ux, uy, ur);
 }
 
 // crossing of the radical axes of slots a and b (weighted circumcentre)
@@ -499,8 +511,8 @@ MA_HD void vtx64(int prev, int cur, const Nb64* nb, const FX& fx, double& X, dou
 {
     if (prev < 0 && cur < 0) {
         int e = -1 - cur;
-        X = fx.rx[e];
-        Y = fx.ry[e];
+        X = pick(fx.rx, e);
+        Y = pick(fx.ry, e);
         return;
     }
     if (prev >= 0 && cur >= 0) {
@@ -514,8 +526,8 @@ MA_HD void vtx64(int prev, int cur, const Nb64* nb, const FX& fx, double& X, dou
     int e = (prev < 0) ? -1 - prev : -1 - cur;
     const Nb64 a = nb[(prev < 0) ? cur : prev];
     int e1 = (e + 1 == fx.n) ? 0 : e + 1;
-    double px = fx.rx[e], py = fx.ry[e];
-    double ex = fx.rx[e1] - px, ey = fx.ry[e1] - py;
+    double px = pick(fx.rx, e), py = pick(fx.ry, e);
+    double ex = pick(fx.rx, e1) - px, ey = pick(fx.ry, e1) - py;
     double Ap = 2.0 * (px * a.dx + py * a.dy) - a.z;
     double den = 2.0 * (ex * a.dx + ey * a.dy);
     double t = -Ap / den;
@@ -667,9 +679,9 @@ MA_HD void vtx_anchor(int prev, int cur, const Slot* slots, const float* zc, con
     };
     if (prev < 0 && cur < 0) {
         const int e = -1 - cur;
-        X = fa.ux[e];
-        Y = fa.uy[e];
-        R = fa.ur[e];
+        X = pick(fa.ux, e);
+        Y = pick(fa.uy, e);
+        R = pick(fa.ur, e);
     } else if (prev >= 0 && cur >= 0) {
         vtx_bis_bis(slot_at(prev), slot_at(cur), X, Y, R);
     } else {
@@ -698,7 +710,8 @@ MA_HD void integrate_piece32(int n, const Lab& lab_of, const Slot* slots, const 
     // the triangle's corners about the anchor
     FixedA fa;
     fa.n = fx.n;
-    for (int e = 0; e < fx.n; e++) {
+#pragma unroll
+    for (int e = 0; e < 3; e++) {  // triangles
         fa.ux[e] = (float)(fx.rx[e] - ax);
         fa.uy[e] = (float)(fx.ry[e] - ay);
         fa.ur[e] = kU32 * fmaxf(fabsf(fa.ux[e]), fabsf(fa.uy[e])) + 1e-37f;
@@ -881,7 +894,8 @@ MA_HD void integrate_vjp32(int n, const Lab& lab_of, const Slot* slots, const fl
 {
     FixedA fa;
     fa.n = fx.n;
-    for (int e = 0; e < fx.n; e++) {
+#pragma unroll
+    for (int e = 0; e < 3; e++) {  // triangles
         fa.ux[e] = (float)(fx.rx[e] - ax);
         fa.uy[e] = (float)(fx.ry[e] - ay);
         fa.ur[e] = kU32 * fmaxf(fabsf(fa.ux[e]), fabsf(fa.uy[e])) + 1e-37f;

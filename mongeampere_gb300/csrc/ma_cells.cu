@@ -1472,7 +1472,8 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                                 float nx, ny, nr;
                                 if (plab < 0) {
                                     const int e = -1 - plab, e1 = e == 2 ? 0 : e + 1;
-                                    vtx_seg_bis(cx[e], cy[e], cr[e], cx[e1], cy[e1], cr[e1], c, nx, ny, nr);
+                                    vtx_seg_bis(pick(cx, e), pick(cy, e), pick(cr, e), pick(cx, e1), pick(cy, e1),
+                                                pick(cr, e1), c, nx, ny, nr);
                                 } else {
                                     vtx_bis_bis(sl[plab], c, nx, ny, nr);
                                 }
@@ -1550,7 +1551,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
             __syncwarp();
             // B: one piece per lane
             for (int p = lane; p < L && MODE != kModeCount; p += 32) {
-                const PieceRec R = W.rec[p];
+                const PieceRec& R = W.rec[p];  // read in place: a local copy would sit in local memory
                 if (MODE == kModeEmit) {
                     const CellInfo& C = W.ci[R.cell];
                     const SiteD S = A.sites[C.k];
