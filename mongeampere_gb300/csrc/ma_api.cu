@@ -298,24 +298,9 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     }
     const int mode = f.pieces ? 3 : (f.vjp ? (f.mixed ? 6 : 2) : (f.moments > 0 ? 1 : (f.mixed ? 5 : 0)));
     launch_cells(c, m, a, 0, mode);
-    if (mode == 5) {
-        // mixed: the cells whose certified FP32 mass error exceeds its bound, in FP64
+    c->hinfo[2] = 0;
+    if (mode == 5)
         MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 2, c->nredo.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
-        MA_CUDA(c, ctx_sync(c));
-        if (c->hinfo[2] > 0) {
-            CellArgs r = a;
-            r.cell_list = c->redo64.as<int>();
-            r.ncell_list = c->hinfo[2];
-            {
-                ProfScope ps(c, &c->profile.pieces_ms, &c->profile.pieces_launches);
-                if (m->kind == 0)
-                    launch_pieces_grid(r, m->grid_dev(), 0, s);
-                else
-                    launch_pieces_tri(r, m->tri_dev(), 0, s);
-            }
-            c->launches += 1;
-        }
-    }
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo, c->nredo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     MA_CUDA(c, cudaMemcpyAsync(c->hinfo + 1, c->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     c->hinfo[3] = 0;
@@ -329,6 +314,21 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
         return MA_OK;
     }
     int nredo = c->hinfo[0];
+    if (mode == 5 && c->hinfo[2] > 0) {
+        // mixed: the cells whose certified FP32 mass error exceeds its bound, in FP64
+        // (ordered on the stream before everything that reads the outputs)
+        CellArgs r = a;
+        r.cell_list = c->redo64.as<int>();
+        r.ncell_list = c->hinfo[2];
+        {
+            ProfScope ps(c, &c->profile.pieces_ms, &c->profile.pieces_launches);
+            if (m->kind == 0)
+                launch_pieces_grid(r, m->grid_dev(), 0, s);
+            else
+                launch_pieces_tri(r, m->tri_dev(), 0, s);
+        }
+        c->launches += 1;
+    }
     if (f.pieces) {
         // the count pass is done: offsets, then the emit pass over the same cells
         c->have_h = false;
