@@ -172,7 +172,7 @@ typedef enum ma_init {
                                initial guess as an argument); for sites near a uniform spread */
     MA_INIT_CONTINUATION = 2 /* continuation in the target masses from those of w_inout: stages
                                nu_t = m(w_in) + t (nu - m(w_in)), no cell's target changing by more
-                               than 2x between stages, each the reference's damped Newton to 1e-2
+                               than 2x between stages, each the reference's damped Newton to 1e-1
                                relative (at most 5 * maxiter steps), the last one to the caller's
                                rule; no counterpart in the reference.  For sites far from equilibrium
                                (clustered sites), where the damped Newton from w_inout stalls */
