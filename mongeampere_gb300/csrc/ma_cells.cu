@@ -714,18 +714,9 @@ __global__ void __launch_bounds__(32 * kS1Warps, 6) k_cells_stage1(CellArgs A)
         ccount = nseed;
     }
     __syncwarp();
-    auto is_seed = [&](int q) -> bool {
-        if (windowed) return q >= wlo && q <= whi;
-        int lo = 0, hi = nseed - 1;  // the previous list is sorted by site index
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (W.seed[mid] < q)
-                lo = mid + 1;
-            else
-                hi = mid;
-        }
-        return W.seed[lo] == q;
-    };
+    // a window seed is skipped by its range; a previous-list seed is one of the cell's
+    // slots (the previous neighbours bound the cell again) and try_sites skips it there
+    auto is_seed = [&](int q) -> bool { return windowed && q >= wlo && q <= whi; };
 
     // 2. the site tree, a batch of up to 32 nodes after each list of candidates
     int sp = -1;  // -1: the walk has not started
