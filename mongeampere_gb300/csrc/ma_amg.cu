@@ -36,6 +36,8 @@
 // to no aggregate and are held at zero on every level.
 #include <cooperative_groups.h>
 
+#include <cfloat>
+
 #include <algorithm>
 
 #include "ma_runtime.h"
@@ -49,8 +51,10 @@ constexpr int kAggGroup = 4;        // rows per aggregate where the matching sta
 constexpr int kCoarsest = 64;       // dense solve at or below this many nodes
 constexpr int kRowCap = 512;        // gathered entries of one coarse row
 constexpr int kRowWarps = 4;        // coarse rows per block in the setup
-constexpr double kOmega = 2.0 / 3.0;
+constexpr double kOmega = 0.8;  // Jacobi damping (|1 - omega lambda| <= 0.6 on D^-1 H's [0, 2])
 constexpr double kCoarseScale = 1.5;
+constexpr float kOmegaF = (float)kOmega;  // the preconditioner's FP32 arithmetic
+constexpr float kCoarseScaleF = (float)kCoarseScale;
 
 // ---------------------------------------------------------------------------
 // setup: coarse rows
@@ -505,6 +509,15 @@ __global__ void k_fine_fill(const int* rp, const int* ci, const double* va, cons
     dinv[k] = (i == n - 1 || !(d > 0.0)) ? 0.0 : 1.0 / d;
 }
 
+// An FP64 value for the preconditioner's FP32 arithmetic: nonzero stays nonzero (a
+// row's diagonal inverse marks it active) and the range saturates at FLT_MAX.
+__host__ __device__ __forceinline__ float to_f32(double v)
+{
+    float f = (float)v;
+    if (f == 0.0f && v != 0.0) f = v > 0.0 ? FLT_MIN : -FLT_MIN;
+    return fminf(fmaxf(f, -FLT_MAX), FLT_MAX);
+}
+
 // sliced ELL of the Morton-ordered fine level: 32 x (longest row of the slice)
 // entries per slice of 32 rows
 __global__ void k_sell_width(const int* rp, int n, int* cnt)
@@ -516,7 +529,7 @@ __global__ void k_sell_width(const int* rp, int n, int* cnt)
 }
 
 __global__ void k_sell_fill(const int* rp, const int* ci, const double* va, int n, const int* sp, int* eci,
-                            double* eva)
+                            double* eva, float* eva32)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -525,6 +538,7 @@ __global__ void k_sell_fill(const int* rp, const int* ci, const double* va, int 
     for (int e = 0; e < w; e++) {
         eci[b0 + 32 * e] = e < len ? ci[k0 + e] : k;
         eva[b0 + 32 * e] = e < len ? va[k0 + e] : 0.0;
+        eva32[b0 + 32 * e] = e < len ? to_f32(va[k0 + e]) : 0.0f;
     }
 }
 
@@ -537,20 +551,28 @@ __global__ void k_sell_fill(const int* rp, const int* ci, const double* va, int 
 // T = 1 .. 32 adjacent lanes (sized so that the grid covers the level), the lanes
 // striding over the row's entries and summing by shuffles, so that the small levels
 // are not a chain of dependent loads in a few threads.  An aggregate's members are
-// listed (mem[mp[J] .. mp[J+1])); agg maps a row to its aggregate.  Grid barriers
-// per CG iteration: 2 (nlev - 2) + 4.
+// listed (mem[mp[J] .. mp[J+1])); agg maps a row to its aggregate.  The
+// preconditioner computes in FP32, on FP32 copies of the levels' matrices (GB300
+// issues FP64 at 1/64 of its FP32 rate, and the per-SM FP64 issue bounded these
+// phases; the V-cycle's rounding lies far below its approximation error), while the
+// CG recurrences, the product A p and the dot products stay FP64, so that the
+// residual the iteration reaches is an FP64 residual.  Grid barriers
+// per CG iteration: 2 (nlev - 2) + 4 without the block-local coarse cycle below,
+// 2 (c - 1) + 5 with it.
 constexpr int kAmgMaxLevels = 16;
-constexpr int kAmgThreads = 256;
+constexpr int kAmgMaxThreads = 1024;  // the PCG block size is chosen at launch, up to this
 
 struct AmgLevelDev {
     int n;
     const int* rp;
     const int* ci;
-    const double* va;
+    const double* va;    // the setup's FP64 matrix
     const double* dinv;
-    double* b;   // restricted residual
-    double* xp;  // post-smoothed correction
-    double* y;   // pre-smoothed plus prolonged correction (levels 1 .. nlev-3)
+    float* va32;         // its FP32 copy for the preconditioner (written by the PCG kernel)
+    float* dinv32;
+    float* b;   // restricted residual
+    float* xp;  // post-smoothed correction
+    float* y;   // pre-smoothed plus prolonged correction (levels 1 .. nlev-3)
     int tr;      // team size restricting this level into the next
     int tp;      // team size prolonging into this level
     const int* agg;  // row -> node of the next level (-1: inactive)
@@ -562,6 +584,7 @@ struct AmgLevelDev {
     const int* sp;
     const int* eci;
     const double* eva;
+    const float* eva32;
 };
 
 struct AmgPcgArgs {
@@ -578,12 +601,17 @@ struct AmgPcgArgs {
     double* z;
     double* p;
     double* q;
-    double* ys;    // the fine level's pre-smoothed plus prolonged correction (levels >= 3)
+    float* ys;     // the fine level's pre-smoothed plus prolonged correction (levels >= 3)
+    float* r32a;   // FP32 copies of the residual (double-buffered like r0/r1) and of q,
+    float* r32b;   // which the preconditioner reads
+    float* q32;
+    float* s32;    // the fine residual of the pre-smoothed correction
     double* part;  // 3 * gridDim.x partial sums
     double* out;   // [iterations, |r|, |b|]
     double rtol;
     int maxiter;
     const int* overflow;  // set by the setup: fall back to Jacobi
+    int tail_bytes;       // dynamic shared memory of a block, for the block-local coarse cycle
 };
 
 __device__ __forceinline__ double amg_block_sum(double v, double* sh)
@@ -594,7 +622,7 @@ __device__ __forceinline__ double amg_block_sum(double v, double* sh)
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0.0;
-        for (int k = 0; k < kAmgThreads / 32; k++) s += sh[k];
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k];
         sh[32] = s;
     }
     __syncthreads();
@@ -606,12 +634,12 @@ __device__ __forceinline__ double amg_block_sum(double v, double* sh)
 __device__ __forceinline__ double amg_grid_total(const double* part, int nb, double* sh)
 {
     double v = 0.0;
-    for (int k = threadIdx.x; k < nb; k += kAmgThreads) v += part[k];
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) v += part[k];
     return amg_block_sum(v, sh);
 }
 
 // sum over lanes xor-adjacent below `width` (bitwise identical on all of them)
-__device__ __forceinline__ double team_sum(double v, int width)
+__device__ __forceinline__ float team_sum(float v, int width)
 {
     for (int o = width >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -629,12 +657,13 @@ __device__ __forceinline__ int team_scan(int v, int t, int T)
 
 // Loop over rows [0, nrows) with teams of T lanes: calls fn(row, lane_in_team)
 // with row < nrows, or row = -1 for lanes without a row in this pass (they still
-// take part in the team's shuffles).  Warp-uniform trip count.
-template <class Fn>
+// take part in the team's shuffles).  Warp-uniform trip count.  LOCAL: the teams of
+// this block alone (the block-local coarse cycle), else those of the whole grid.
+template <bool LOCAL, class Fn>
 __device__ __forceinline__ void team_rows(int nrows, int T, Fn&& fn)
 {
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nteams = gridDim.x * blockDim.x / T;
+    const int tid = LOCAL ? (int)threadIdx.x : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int nteams = (LOCAL ? (int)blockDim.x : (int)(gridDim.x * blockDim.x)) / T;
     const int lane = threadIdx.x & 31;
     const int wteam0 = (tid >> 5) * (32 / T);  // first team of this warp
     for (int base = wteam0; base < nrows; base += nteams) {
@@ -646,18 +675,19 @@ __device__ __forceinline__ void team_rows(int nrows, int T, Fn&& fn)
 // b_{l+1} from level l >= 1: the residual of the pre-smoothed correction summed
 // over each aggregate, b_{l+1}[J] = sum_{I in J} b_l[I] - omega sum over the
 // member rows' entries a_IK D_K^-1 b_l[K]
-__device__ __forceinline__ void restrict_level(const AmgPcgArgs& a, int l)
+template <bool LOCAL>
+__device__ __forceinline__ void restrict_level(const AmgLevelDev* L, int l, int tail)
 {
-    const AmgLevelDev& A = a.L[l];
-    const AmgLevelDev& C = a.L[l + 1];
+    const AmgLevelDev& A = L[l];
+    const AmgLevelDev& C = L[l + 1];
     const int T = A.tr;
-    team_rows(C.n, T, [&](int J, int t) {
+    team_rows<LOCAL>(C.n, T, [&](int J, int t) {
         // the members' rows at once (member q on team lane q), then their entries in
         // member order, T at a time
         // every loop bound is a maximum over the warp (teams of one warp share it)
         const int q0 = J >= 0 ? A.mp[J] : 0, M = J >= 0 ? A.mp[J + 1] - q0 : 0;
         const int Mmax = __reduce_max_sync(0xffffffffu, M);
-        double s = 0.0;
+        float s = 0.0f;
         for (int m0 = 0; m0 < Mmax; m0 += T) {
             const int mm = max(0, min(T, M - m0));
             int rb = 0, len = 0;
@@ -681,47 +711,47 @@ __device__ __forceinline__ void restrict_level(const AmgPcgArgs& a, int l)
                 if (e < tot && J >= 0) {
                     const int k = kb + (e - ko);
                     const int K = A.ci[k];
-                    s -= A.va[k] * (kOmega * A.dinv[K] * A.b[K]);
+                    s -= A.va32[k] * (kOmegaF * A.dinv32[K] * A.b[K]);
                 }
             }
         }
         s = team_sum(s, T);
         if (J >= 0 && t == 0) {
-            C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
-            if (C.y) C.y[J] = C.dinv[J] != 0.0 ? kOmega * C.dinv[J] * s : 0.0;
+            C.b[J] = C.dinv32[J] != 0.0f ? s : 0.0f;
+            if (C.y && l + 1 != tail - 1) C.y[J] = C.dinv32[J] != 0.0f ? kOmegaF * C.dinv32[J] * s : 0.0f;
         }
     });
 }
 
 // b_1 from the fine level: the fine residuals of the pre-smoothed correction (in s)
 // summed over each aggregate
-__device__ __forceinline__ void restrict_fine(const AmgPcgArgs& a, const double* s_fine)
+__device__ __forceinline__ void restrict_fine(const AmgPcgArgs& a, const float* s_fine, int tail)
 {
     const AmgLevelDev& F = a.L[0];
     const AmgLevelDev& C = a.L[1];
     const int T = F.tr;
-    team_rows(C.n, T, [&](int J, int t) {
-        double s = 0.0;
+    team_rows<false>(C.n, T, [&](int J, int t) {
+        float s = 0.0f;
         if (J >= 0)
             for (int q = F.mp[J] + t; q < F.mp[J + 1]; q += T) s += s_fine[F.mem[q]];
         s = team_sum(s, T);
         if (J >= 0 && t == 0) {
-            C.b[J] = C.dinv[J] != 0.0 ? s : 0.0;
-            if (C.y) C.y[J] = C.dinv[J] != 0.0 ? kOmega * C.dinv[J] * s : 0.0;
+            C.b[J] = C.dinv32[J] != 0.0f ? s : 0.0f;
+            if (C.y && tail != 2) C.y[J] = C.dinv32[J] != 0.0f ? kOmegaF * C.dinv32[J] * s : 0.0f;
         }
     });
 }
 
-// the coarsest level's solution cinv b, computed by every block into shared memory
-// (xc) before the phase that prolongs it; cinv itself stays in shared memory (sinv)
-// for the whole kernel.  Thread r < n forms row r, its b[k] from shared memory.
-__device__ __forceinline__ void coarsest_solve(const AmgPcgArgs& a, double* xc, const double* sinv, double* sb)
+// the coarsest level's solution cinv b, computed into shared memory (xc) before the
+// phase that prolongs it, by every block or by the block of the block-local cycle;
+// cinv itself stays in shared memory (sinv) for the whole kernel.  Thread r < n
+// forms row r, its b[k] from shared memory.
+__device__ __forceinline__ void coarsest_solve(const AmgLevelDev& C, float* xc, const float* sinv, float* sb)
 {
-    const AmgLevelDev& C = a.L[a.nlev - 1];
-    for (int k = threadIdx.x; k < C.n; k += kAmgThreads) sb[k] = C.b[k];
+    for (int k = threadIdx.x; k < C.n; k += blockDim.x) sb[k] = C.b[k];
     __syncthreads();
-    for (int r = threadIdx.x; r < C.n; r += kAmgThreads) {
-        double v = 0.0;
+    for (int r = threadIdx.x; r < C.n; r += blockDim.x) {
+        float v = 0.0f;
         for (int k = 0; k < C.n; k++) v += sinv[k * C.n + r] * sb[k];
         xc[r] = v;
     }
@@ -729,59 +759,205 @@ __device__ __forceinline__ void coarsest_solve(const AmgPcgArgs& a, double* xc, 
 }
 
 // the coarse correction of aggregate J of level l, i.e. node J of level l+1
-__device__ __forceinline__ double coarse_corr(const AmgPcgArgs& a, int l, int J, const double* xc)
+__device__ __forceinline__ float coarse_corr(const AmgLevelDev* L, int nlev, int l, int J, const float* xc)
 {
-    if (J < 0) return 0.0;  // a row in no aggregate
-    return (l + 2 < a.nlev) ? a.L[l + 1].xp[J] : xc[J];
+    if (J < 0) return 0.0f;  // a row in no aggregate
+    return (l + 2 < nlev) ? L[l + 1].xp[J] : xc[J];
 }
 
 // xp_l for level l >= 1: pre-smoothed plus scaled coarse correction, then one
 // damped Jacobi sweep
-__device__ __forceinline__ void prolong_level(const AmgPcgArgs& a, int l, double* xc, const double* sinv, double* sb)
+template <bool LOCAL>
+__device__ __forceinline__ void prolong_level(const AmgLevelDev* L, int nlev, int l, int tail, float* ys,
+                                              float* xc, const float* sinv, float* sb)
 {
-    const AmgLevelDev& A = a.L[l];
+    const AmgLevelDev& A = L[l];
     const int T = A.tp;
-    if (l + 2 == a.nlev) coarsest_solve(a, xc, sinv, sb);
-    team_rows(A.n, T, [&](int I, int t) {
-        double s = 0.0, yI = 0.0, dI = 0.0;
+    // level tail - 1 keeps no y: its prolongation recomputes the terms from b and the
+    // corrections of level tail (the same values), which the block-local cycle
+    // leaves in global memory, so that the cycle scatters nothing into level tail - 1
+    const bool has_y = A.y != nullptr && l != tail - 1;
+    if (l + 2 == nlev) coarsest_solve(L[nlev - 1], xc, sinv, sb);
+    team_rows<LOCAL>(A.n, T, [&](int I, int t) {
+        float s = 0.0f, yI = 0.0f, dI = 0.0f;
         if (I >= 0) {
-            dI = A.dinv[I];
-            if (dI != 0.0) {
-                if (A.y) {
+            dI = A.dinv32[I];
+            if (dI != 0.0f) {
+                if (has_y) {
                     // y complete since the prolongation of level l + 1: one gather
-                    for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) s -= A.va[k] * A.y[A.ci[k]];
+                    for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) s -= A.va32[k] * A.y[A.ci[k]];
                     yI = A.y[I];
                 } else {
                     for (int k = A.rp[I] + t; k < A.rp[I + 1]; k += T) {
                         const int K = A.ci[k];
-                        const double dK = A.dinv[K];
-                        const double yK =
-                            dK != 0.0 ? kOmega * dK * A.b[K] + kCoarseScale * coarse_corr(a, l, A.agg[K], xc) : 0.0;
-                        s -= A.va[k] * yK;
+                        const float dK = A.dinv32[K];
+                        const float yK = dK != 0.0f ? kOmegaF * dK * A.b[K] +
+                                                          kCoarseScaleF * coarse_corr(L, nlev, l, A.agg[K], xc)
+                                                    : 0.0f;
+                        s -= A.va32[k] * yK;
                     }
-                    yI = kOmega * dI * A.b[I] + kCoarseScale * coarse_corr(a, l, A.agg[I], xc);
+                    yI = kOmegaF * dI * A.b[I] + kCoarseScaleF * coarse_corr(L, nlev, l, A.agg[I], xc);
                 }
             }
         }
         s = team_sum(s, T);
-        const double xI = dI != 0.0 ? yI + kOmega * dI * (A.b[I] + s) : 0.0;
+        const float xI = dI != 0.0f ? yI + kOmegaF * dI * (A.b[I] + s) : 0.0f;
         if (I >= 0 && t == 0) A.xp[I] = xI;
-        if (I >= 0) {
+        if (I >= 0 && l != tail) {
             // the rows of aggregate I one level down take their share of the correction now
-            const AmgLevelDev& D = a.L[l - 1];
-            double* yd = l == 1 ? a.ys : D.y;
-            for (int q = D.mp[I] + t; q < D.mp[I + 1]; q += T) yd[D.mem[q]] += kCoarseScale * xI;
+            const AmgLevelDev& D = L[l - 1];
+            float* yd = l == 1 ? ys : D.y;
+            for (int q = D.mp[I] + t; q < D.mp[I + 1]; q += T) yd[D.mem[q]] += kCoarseScaleF * xI;
         }
     });
 }
 
-__global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
+// The block-local coarse cycle.  Levels c .. nlev-1 of the hierarchy, when they fit the
+// dynamic shared memory of a block, are copied there once per launch, and each
+// iteration block 0 alone restricts through them, solves the coarsest level and
+// prolongs back to level c with block barriers, while the other blocks wait at one
+// grid barrier: the small levels cost shared-memory latencies instead of a grid
+// barrier and a chain of L2 loads each.  The arithmetic is that of the grid-wide
+// phases, term for term.  Per level, in this order, each array padded to 16 bytes:
+// va32, dinv32, b, [xp for l > c], [y where the level keeps one], rp, ci, agg, mem, mp;
+// the coarsest level holds b and dinv.  Level c's xp stays in global memory, where
+// the prolongation of level c - 1 reads it per entry (level c - 1 keeps no y, so the
+// cycle writes nothing else), and level c - 1's aggregates stay there too.
+constexpr int kTailMaxRows = 2048;  // a larger level is faster on the whole grid
+
+__host__ __device__ __forceinline__ size_t tail_pad(size_t b) { return (b + 15) & ~(size_t)15; }
+
+__host__ __device__ __forceinline__ size_t tail_level_bytes(int l, int c, int nlev, int n, int nnz, int nnext)
+{
+    const size_t vn = tail_pad(4 * (size_t)n);
+    if (l == nlev - 1) return 2 * vn;
+    size_t s = tail_pad(4 * (size_t)nnz) + 2 * vn;
+    if (l > c) s += vn;
+    if (l + 3 <= nlev) s += vn;
+    s += tail_pad(4 * (size_t)(n + 1)) + tail_pad(4 * (size_t)nnz) + 2 * tail_pad(4 * (size_t)n) +
+         tail_pad(4 * (size_t)(nnext + 1));
+    return s;
+}
+
+// the first level c >= 1 of the block-local cycle, 0 for none; every block finds the
+// same from the same sizes
+__device__ __forceinline__ int tail_level(const AmgPcgArgs& a)
+{
+    int best = 0;
+    if (a.tail_bytes <= 0) return 0;
+    for (int c = a.nlev - 2; c >= 1; c--) {
+        if (a.L[c].n > kTailMaxRows) break;
+        size_t tot = 0;
+        for (int l = c; l < a.nlev; l++) {
+            const int n = a.L[l].n;
+            const bool last = l == a.nlev - 1;
+            tot += tail_level_bytes(l, c, a.nlev, n, last ? 0 : a.L[l].rp[n], last ? 0 : a.L[l + 1].n);
+        }
+        if (tot > (size_t)a.tail_bytes) break;
+        best = c;
+    }
+    return best;
+}
+
+// lanes per row for a level cycled through by one block
+__device__ __forceinline__ int local_team(int rows)
+{
+    int t = 1;
+    while (t < 32 && rows * t * 2 <= (int)blockDim.x) t <<= 1;
+    return t;
+}
+
+// block 0: the level table of the cycle (levels below c as they are, levels c and
+// up in shared memory) and the copies of their matrices and aggregates
+__device__ __forceinline__ void tail_setup(const AmgPcgArgs& a, int c, AmgLevelDev* tl, unsigned char* sm)
+{
+    if (threadIdx.x == 0) {
+        for (int l = 0; l < a.nlev; l++) tl[l] = a.L[l];
+        size_t off = 0;
+        auto take = [&](size_t bytes) {
+            unsigned char* q = sm + off;
+            off += tail_pad(bytes);
+            return q;
+        };
+        for (int l = c; l < a.nlev; l++) {
+            AmgLevelDev& T = tl[l];
+            const int n = T.n;
+            if (l == a.nlev - 1) {
+                T.b = (float*)take(4 * (size_t)n);
+                T.dinv32 = (float*)take(4 * (size_t)n);
+                continue;
+            }
+            const int nnz = a.L[l].rp[n], nn = a.L[l + 1].n;
+            T.va32 = (float*)take(4 * (size_t)nnz);
+            T.dinv32 = (float*)take(4 * (size_t)n);
+            T.b = (float*)take(4 * (size_t)n);
+            if (l > c) T.xp = (float*)take(4 * (size_t)n);
+            if (l + 3 <= a.nlev) T.y = (float*)take(4 * (size_t)n);
+            T.rp = (const int*)take(4 * (size_t)(n + 1));
+            T.ci = (const int*)take(4 * (size_t)nnz);
+            T.agg = (const int*)take(4 * (size_t)n);
+            T.mem = (const int*)take(4 * (size_t)n);
+            T.mp = (const int*)take(4 * (size_t)(nn + 1));
+            T.tr = local_team(nn);
+            T.tp = local_team(n);
+        }
+    }
+    __syncthreads();
+    for (int l = c; l < a.nlev; l++) {
+        const AmgLevelDev& G = a.L[l];
+        const AmgLevelDev& T = tl[l];
+        const int n = G.n;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) T.dinv32[k] = G.dinv32[k];
+        if (l == a.nlev - 1) continue;
+        const int nnz = G.rp[n], nn = a.L[l + 1].n;
+        for (int k = threadIdx.x; k < nnz; k += blockDim.x) {
+            T.va32[k] = G.va32[k];
+            const_cast<int*>(T.ci)[k] = G.ci[k];
+        }
+        for (int k = threadIdx.x; k <= n; k += blockDim.x) const_cast<int*>(T.rp)[k] = G.rp[k];
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const_cast<int*>(T.agg)[k] = G.agg[k];
+            const_cast<int*>(T.mem)[k] = G.mem[k];
+        }
+        for (int k = threadIdx.x; k <= nn; k += blockDim.x) const_cast<int*>(T.mp)[k] = G.mp[k];
+    }
+    __syncthreads();
+}
+
+// block 0, each iteration: level c's restricted residual (and y) in, level c's
+// correction out
+__device__ __forceinline__ void tail_cycle(const AmgPcgArgs& a, int c, const AmgLevelDev* tl, float* xc,
+                                           const float* sinv, float* sb)
+{
+    {
+        const AmgLevelDev& T = tl[c];
+        const AmgLevelDev& G = a.L[c];
+        for (int k = threadIdx.x; k < T.n; k += blockDim.x) {
+            T.b[k] = G.b[k];
+            if (T.y) T.y[k] = G.y[k];
+        }
+    }
+    __syncthreads();
+    for (int l = c; l + 1 < a.nlev; l++) {
+        restrict_level<true>(tl, l, c);
+        __syncthreads();
+    }
+    for (int l = a.nlev - 2; l >= c; l--) {
+        prolong_level<true>(tl, a.nlev, l, c, a.ys, xc, sinv, sb);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kAmgMaxThreads, 1) k_pcg_amg(const __grid_constant__ AmgPcgArgs a)
 {
     cg::grid_group grid = cg::this_grid();
+    extern __shared__ __align__(16) unsigned char tail_sm[];
     __shared__ double sh[40];
-    __shared__ double xc[kCoarsest];
-    __shared__ double sb[kCoarsest];
-    __shared__ double sinv[kCoarsest * kCoarsest];  // the coarsest inverse, transposed
+    __shared__ float xc[kCoarsest];
+    __shared__ float sb[kCoarsest];
+    __shared__ float sinv[kCoarsest * kCoarsest];  // the coarsest inverse, transposed
+    __shared__ AmgLevelDev tl[kAmgMaxLevels];        // the block-local cycle's levels
+    __shared__ int s_tail;
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
@@ -796,10 +972,24 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
     double* part_pq = a.part + 2 * nb;
     double* rc = a.r0;  // current residual
     double* rn = a.r1;  // next residual
+    float* rc32 = a.r32a;
+    float* rn32 = a.r32b;
 
-    if (!jacobi) {  // the coarsest inverse into shared memory, transposed
+    if (threadIdx.x == 0) s_tail = jacobi ? 0 : tail_level(a);
+    __syncthreads();
+    const int tail = s_tail;  // first level of the block-local cycle, 0: none
+    if (!jacobi && (tail == 0 || blockIdx.x == 0)) {  // the coarsest inverse, transposed
         const int cn = a.L[a.nlev - 1].n;
-        for (int t = threadIdx.x; t < cn * cn; t += kAmgThreads) sinv[(t % cn) * cn + t / cn] = a.cinv[t];
+        for (int t = threadIdx.x; t < cn * cn; t += blockDim.x) sinv[(t % cn) * cn + t / cn] = (float)a.cinv[t];
+    }
+    if (!jacobi) {
+        // the FP32 copies of the coarse levels' matrices
+        for (int l = 1; l < a.nlev; l++) {
+            const AmgLevelDev& A = a.L[l];
+            const int nnz = A.rp[A.n];
+            for (int k = tid; k < nnz; k += stride) A.va32[k] = to_f32(A.va[k]);
+            for (int k = tid; k < A.n; k += stride) A.dinv32[k] = to_f32(A.dinv[k]);
+        }
     }
     // x = 0, p = q = 0, r = b (active rows); the first pass below is a CG update
     // with alpha = 0
@@ -807,34 +997,47 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
         a.xs[k] = 0.0;
         a.p[k] = 0.0;
         a.q[k] = 0.0;
-        rc[k] = F.dinv[k] != 0.0 ? a.b[a.perm[k]] : 0.0;
+        const double r = F.dinv[k] != 0.0 ? a.b[a.perm[k]] : 0.0;
+        rc[k] = r;
+        if (!jacobi) {
+            F.dinv32[k] = to_f32(F.dinv[k]);
+            rc32[k] = (float)r;
+            a.q32[k] = 0.0f;
+        }
     }
     grid.sync();
+    if (tail > 0 && blockIdx.x == 0) tail_setup(a, tail, tl, tail_sm);
     double alpha = 0.0, rz = 0.0, rr = 0.0, bnorm = 0.0, tol = 0.0;
     int it = 0;
     for (;;) {
-        // ---- x += alpha p, r -= alpha q, and the fine residual of the pre-smoothed
-        // correction (into z, free until the preconditioner writes it) -------------
+        // ---- x += alpha p, r -= alpha q (FP64), and in FP32 the fine residual of the
+        // pre-smoothed correction, the neighbours' new residuals formed from the FP32
+        // copies of r and q --------------------------------------------------------
         {
             double l_rr = 0.0;
+            const float alpha32 = (float)alpha;
             for (int k = tid; k < n; k += stride) {
                 const double rk = rc[k] - alpha * a.q[k];
                 a.xs[k] += alpha * a.p[k];
                 rn[k] = rk;
                 l_rr += rk * rk;
-                const double dk = F.dinv[k];
-                double s = 0.0;
-                if (!jacobi) a.ys[k] = dk != 0.0 ? kOmega * dk * rk : 0.0;
-                if (!jacobi && dk != 0.0) {
-                    s = rk;
-                    const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
+                if (!jacobi) {
+                    const float rk32 = (float)rk;
+                    const float dk = F.dinv32[k];
+                    rn32[k] = rk32;
+                    a.ys[k] = dk != 0.0f ? kOmegaF * dk * rk32 : 0.0f;
+                    float s = 0.0f;
+                    if (dk != 0.0f) {
+                        s = rk32;
+                        const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
 #pragma unroll 4
-                    for (int e = 0; e < w; e++) {
-                        const int j = F.eci[b0 + 32 * e];
-                        s -= F.eva[b0 + 32 * e] * (kOmega * F.dinv[j] * (rc[j] - alpha * a.q[j]));
+                        for (int e = 0; e < w; e++) {
+                            const int j = F.eci[b0 + 32 * e];
+                            s -= F.eva32[b0 + 32 * e] * (kOmegaF * F.dinv32[j] * (rc32[j] - alpha32 * a.q32[j]));
+                        }
                     }
+                    a.s32[k] = s;
                 }
-                if (!jacobi) a.z[k] = s;
             }
             const double t = amg_block_sum(l_rr, sh);
             if (threadIdx.x == 0) part_rr[blockIdx.x] = t;
@@ -844,6 +1047,9 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
             double* t = rc;
             rc = rn;
             rn = t;
+            float* t32 = rc32;
+            rc32 = rn32;
+            rn32 = t32;
         }
         rr = amg_grid_total(part_rr, nb, sh);
         if (it == 0) {
@@ -860,54 +1066,63 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
                 l_rz += zk * rc[k];
             }
         } else {
-            restrict_fine(a, a.z);
+            restrict_fine(a, a.s32, tail);
             grid.sync();
-            for (int l = 1; l + 1 < a.nlev; l++) {
-                restrict_level(a, l);
+            const int lr = tail > 0 ? tail : a.nlev - 1;  // grid-wide restrictions below lr
+            for (int l = 1; l < lr; l++) {
+                restrict_level<false>(a.L, l, tail);
                 grid.sync();
             }
-            for (int l = a.nlev - 2; l >= 1; l--) {
-                prolong_level(a, l, xc, sinv, sb);
+            if (tail > 0) {
+                if (blockIdx.x == 0) tail_cycle(a, tail, tl, xc, sinv, sb);
                 grid.sync();
             }
-            if (a.nlev == 2) coarsest_solve(a, xc, sinv, sb);
-            if (a.nlev > 2) {
+            for (int l = (tail > 0 ? tail - 1 : a.nlev - 2); l >= 1; l--) {
+                prolong_level<false>(a.L, a.nlev, l, tail, a.ys, xc, sinv, sb);
+                grid.sync();
+            }
+            if (a.nlev == 2) coarsest_solve(a.L[1], xc, sinv, sb);
+            if (a.nlev > 2 && tail != 1) {
                 // y, complete since the level-1 prolongation: one gather per entry
                 for (int k = tid; k < n; k += stride) {
-                    const double dk = F.dinv[k];
-                    double zk = 0.0;
-                    if (dk != 0.0) {
-                        double s = rc[k];
+                    const float dk = F.dinv32[k];
+                    float zk = 0.0f;
+                    if (dk != 0.0f) {
+                        float s = rc32[k];
                         const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
 #pragma unroll 4
-                        for (int e = 0; e < w; e++) s -= F.eva[b0 + 32 * e] * a.ys[F.eci[b0 + 32 * e]];
-                        zk = a.ys[k] + kOmega * dk * s;
+                        for (int e = 0; e < w; e++) s -= F.eva32[b0 + 32 * e] * a.ys[F.eci[b0 + 32 * e]];
+                        zk = a.ys[k] + kOmegaF * dk * s;
                     }
-                    a.z[k] = zk;
-                    l_rz += zk * rc[k];
+                    const double zd = (double)zk;
+                    a.z[k] = zd;
+                    l_rz += zd * rc[k];
                 }
             } else {
-                // two levels: the coarsest correction straight from xc
+                // two levels, or level 1 in the block-local cycle: the corrections of
+                // level 1 (xc, or xp of level 1) gathered per entry
                 for (int k = tid; k < n; k += stride) {
-                    const double dk = F.dinv[k];
-                    double zk = 0.0;
-                    if (dk != 0.0) {
-                        const double yk = kOmega * dk * rc[k] + kCoarseScale * coarse_corr(a, 0, F.agg[k], xc);
-                        double s = rc[k];
+                    const float dk = F.dinv32[k];
+                    float zk = 0.0f;
+                    if (dk != 0.0f) {
+                        const float yk =
+                            kOmegaF * dk * rc32[k] + kCoarseScaleF * coarse_corr(a.L, a.nlev, 0, F.agg[k], xc);
+                        float s = rc32[k];
                         const int b0 = F.sp[k >> 5] + (k & 31), w = (F.sp[(k >> 5) + 1] - F.sp[k >> 5]) >> 5;
 #pragma unroll 4
                         for (int e = 0; e < w; e++) {
                             const int j = F.eci[b0 + 32 * e];
-                            const double dj = F.dinv[j];
-                            const double yj =
-                                dj != 0.0 ? kOmega * dj * rc[j] + kCoarseScale * coarse_corr(a, 0, F.agg[j], xc)
-                                          : 0.0;
-                            s -= F.eva[b0 + 32 * e] * yj;
+                            const float dj = F.dinv32[j];
+                            const float yj = dj != 0.0f ? kOmegaF * dj * rc32[j] +
+                                                              kCoarseScaleF * coarse_corr(a.L, a.nlev, 0, F.agg[j], xc)
+                                                        : 0.0f;
+                            s -= F.eva32[b0 + 32 * e] * yj;
                         }
-                        zk = yk + kOmega * dk * s;
+                        zk = yk + kOmegaF * dk * s;
                     }
-                    a.z[k] = zk;
-                    l_rz += zk * rc[k];
+                    const double zd = (double)zk;
+                    a.z[k] = zd;
+                    l_rz += zd * rc[k];
                 }
             }
         }
@@ -933,6 +1148,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_pcg_amg(AmgPcgArgs a)
             const double qk = w + beta * a.q[k];
             a.p[k] = pk;
             a.q[k] = qk;
+            if (!jacobi) a.q32[k] = (float)qk;
             l_pq += pk * qk;
         }
         {
@@ -1013,15 +1229,27 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     }
     MA_CUDA(c, G.eci.ensure(sizeof(int) * ell_cap));
     MA_CUDA(c, G.eva.ensure(sizeof(double) * ell_cap));
+    MA_CUDA(c, G.eva32.ensure(sizeof(float) * ell_cap));
     k_sell_fill<<<g1, 256, 0, s>>>(G.rp0.as<int>(), G.ci0.as<int>(), G.va0.as<double>(), n, G.sp.as<int>(),
-                                   G.eci.as<int>(), G.eva.as<double>());
+                                   G.eci.as<int>(), G.eva.as<double>(), G.eva32.as<float>());
     c->launches += 9;
+    for (DevBuf* d : {&G.dinv32, &G.r32a, &G.r32b, &G.q32, &G.s32}) MA_CUDA(c, d->ensure(sizeof(float) * n));
 
     AmgPcgArgs a{};
-    a.L[0] = AmgLevelDev{n,       G.rp0.as<int>(), G.ci0.as<int>(), G.va0.as<double>(), c->cg_dinv.as<double>(),
-                         nullptr, nullptr,         nullptr,         1,                 1,
-                         nullptr, nullptr,         nullptr,         G.sp.as<int>(),    G.eci.as<int>(),
-                         G.eva.as<double>()};
+    {
+        AmgLevelDev& F = a.L[0];
+        F.n = n;
+        F.rp = G.rp0.as<int>();
+        F.ci = G.ci0.as<int>();
+        F.va = G.va0.as<double>();
+        F.dinv = c->cg_dinv.as<double>();
+        F.dinv32 = G.dinv32.as<float>();
+        F.tr = F.tp = 1;
+        F.sp = G.sp.as<int>();
+        F.eci = G.eci.as<int>();
+        F.eva = G.eva.as<double>();
+        F.eva32 = G.eva32.as<float>();
+    }
     // the level setup's cooperative grid: co-resident blocks, at most one row per thread
     int setup_max = 0, sms = 0;
     {
@@ -1047,8 +1275,10 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         MA_CUDA(c, Cb.ci.ensure(sizeof(int) * nnz));
         MA_CUDA(c, Cb.va.ensure(sizeof(double) * nnz));
         MA_CUDA(c, Cb.dinv.ensure(sizeof(double) * A.n));
-        MA_CUDA(c, Cb.b.ensure(sizeof(double) * A.n));
-        MA_CUDA(c, Cb.xp.ensure(sizeof(double) * A.n));
+        MA_CUDA(c, Cb.b.ensure(sizeof(float) * A.n));
+        MA_CUDA(c, Cb.xp.ensure(sizeof(float) * A.n));
+        MA_CUDA(c, Cb.va32.ensure(sizeof(float) * nnz));
+        MA_CUDA(c, Cb.dinv32.ensure(sizeof(float) * A.n));
         SetupArgs sa;
         sa.A = LevelCsr{A.n, A.rp, A.ci, A.va, A.dinv};
         sa.mate = G.mate.as<int>();
@@ -1096,9 +1326,20 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         A.agg = B.agg.as<int>();
         A.mp = B.mp.as<int>();
         A.mem = B.mem.as<int>();
-        a.L[l + 1] = AmgLevelDev{nc,      Cb.rp.as<int>(), Cb.ci.as<int>(), Cb.va.as<double>(), Cb.dinv.as<double>(),
-                                 Cb.b.as<double>(), Cb.xp.as<double>(), nullptr, 1, 1, nullptr, nullptr, nullptr,
-                                 nullptr, nullptr, nullptr};
+        {
+            AmgLevelDev& C = a.L[l + 1];
+            C = AmgLevelDev{};
+            C.n = nc;
+            C.rp = Cb.rp.as<int>();
+            C.ci = Cb.ci.as<int>();
+            C.va = Cb.va.as<double>();
+            C.dinv = Cb.dinv.as<double>();
+            C.va32 = Cb.va32.as<float>();
+            C.dinv32 = Cb.dinv32.as<float>();
+            C.b = Cb.b.as<float>();
+            C.xp = Cb.xp.as<float>();
+            C.tr = C.tp = 1;
+        }
         nlev++;
     }
     if (a.L[nlev - 1].n > kCoarsest) {
@@ -1107,8 +1348,8 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     }
     a.nlev = nlev;
     for (int l = 1; l + 3 <= nlev; l++) {  // levels whose corrections are materialised
-        MA_CUDA(c, G.lev[l].y.ensure(sizeof(double) * (size_t)a.L[l].n));
-        a.L[l].y = G.lev[l].y.as<double>();
+        MA_CUDA(c, G.lev[l].y.ensure(sizeof(float) * (size_t)a.L[l].n));
+        a.L[l].y = G.lev[l].y.as<float>();
     }
     if (!keep) {
         G.agg_epoch = c->index_epoch;
@@ -1122,24 +1363,41 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     setup_scope.end();
     c->profile.amg_levels = nlev;
 
-    // the co-resident grid, at most kBlocksPerSm blocks per SM: every grid barrier
-    // waits for all blocks, and the coarse levels' teams want the lanes
-    constexpr int kBlocksPerSm = 4;
-    int max_blocks = 0;
+    // the co-resident grid: kWideBlocksPerSm blocks of kWideThreads per SM, the rest of
+    // the SM's shared memory split between them for the block-local coarse cycle
+    // (512 x 2 measured faster than 1024 x 1 and 256 x 4 on 100,000 sites); a batch
+    // worker, which shares the GPU with the other workers' kernels, launches blocks of
+    // kShareThreads, up to kShareBlocksPerSm of them on an SM, and a cycle sized to match
+    constexpr int kWideThreads = 512, kWideBlocksPerSm = 2;
+    constexpr int kShareThreads = 256, kShareBlocksPerSm = 4;
+    const bool shared_gpu = c->grid_share > 1;
+    const int bthreads = shared_gpu ? kShareThreads : kWideThreads;
+    const int bps = shared_gpu ? kShareBlocksPerSm : kWideBlocksPerSm;
+    int max_blocks = 0, dyn = 0;
     {
-        int per_sm = 0, sms = 0;
-        MA_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_amg, kAmgThreads, 0));
+        int per_sm = 0, sms = 0, sm_bytes = 0, optin = 0;
+        cudaFuncAttributes fa;
+        MA_CUDA(c, cudaFuncGetAttributes(&fa, k_pcg_amg));
         MA_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
-        max_blocks = (per_sm < kBlocksPerSm ? per_sm : kBlocksPerSm) * sms;
+        MA_CUDA(c, cudaDeviceGetAttribute(&sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device));
+        MA_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+        // each resident block also takes 1 KB that the system reserves
+        dyn = sm_bytes / bps - 1024 - (int)fa.sharedSizeBytes;
+        dyn = std::min(dyn, optin - (int)fa.sharedSizeBytes);
+        dyn = std::max(0, dyn) & ~15;
+        MA_CUDA(c, cudaFuncSetAttribute(k_pcg_amg, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+        MA_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_amg, bthreads, dyn));
+        if (per_sm < 1) return fail(c, MA_ERR_CUDA, "the multigrid PCG kernel does not fit an SM");
+        max_blocks = std::min(per_sm, bps) * sms;
         // a batch worker leaves the rest of the GPU to the other workers' problems
-        if (c->grid_share > 1) max_blocks = std::max(1, max_blocks / c->grid_share);
+        if (shared_gpu) max_blocks = std::max(1, max_blocks / c->grid_share);
     }
-    int want = (n + kAmgThreads / 4 - 1) / (kAmgThreads / 4);
+    int want = (n + bthreads / 4 - 1) / (bthreads / 4);
     int nb = want < max_blocks ? want : max_blocks;
     if (nb < 1) nb = 1;
     MA_CUDA(c, c->cg_part.ensure(sizeof(double) * 3 * nb));
     // lanes per coarse row: enough teams to cover the level with the launched grid
-    const int threads = nb * kAmgThreads;
+    const int threads = nb * bthreads;
     auto team = [&](int rows) {
         int t = 1;
         while (t < 32 && (int64_t)rows * t * 2 <= threads) t <<= 1;
@@ -1160,17 +1418,22 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
     a.z = c->cg_z.as<double>();
     a.p = c->cg_p.as<double>();
     a.q = c->cg_q.as<double>();
-    MA_CUDA(c, G.ys.ensure(sizeof(double) * n));
-    a.ys = G.ys.as<double>();
+    MA_CUDA(c, G.ys.ensure(sizeof(float) * n));
+    a.ys = G.ys.as<float>();
+    a.r32a = G.r32a.as<float>();
+    a.r32b = G.r32b.as<float>();
+    a.q32 = G.q32.as<float>();
+    a.s32 = G.s32.as<float>();
     a.part = c->cg_part.as<double>();
     a.out = c->cg_scal.as<double>();
     a.rtol = rtol;
     a.maxiter = maxiter;
     a.overflow = G.flag.as<int>();
+    a.tail_bytes = dyn;
     void* args[] = {&a};
     {
         ProfScope ps(c, &c->profile.pcg_ms, &c->profile.pcg_launches);
-        MA_CUDA(c, cudaLaunchCooperativeKernel((void*)k_pcg_amg, dim3(nb), dim3(kAmgThreads), args, 0, s));
+        MA_CUDA(c, cudaLaunchCooperativeKernel((void*)k_pcg_amg, dim3(nb), dim3(bthreads), args, (size_t)dyn, s));
     }
     c->launches += 1;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat + 8, c->cg_scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));

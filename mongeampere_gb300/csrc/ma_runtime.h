@@ -65,11 +65,13 @@ struct Mesh {
 // aggregation multigrid hierarchy (levels 1.. of the Newton system)
 struct AmgBuf {
     DevBuf rp, ci, va, dinv, b, xp, y;  // the level's matrix (levels >= 1) and work vectors
+    DevBuf va32, dinv32;                // the FP32 copy of the matrix for the preconditioner
     DevBuf agg, mp, mem;             // its aggregates: row -> node of the next level, member lists
 };
 struct Amg {
     AmgBuf lev[16];
     DevBuf r1, xs, inv, cnt, rp0, ci0, va0, sp, eci, eva, flag, cinv, ys;
+    DevBuf eva32, dinv32, r32a, r32b, q32, s32;  // the fine level's FP32 preconditioner data
     // aggregation scratch: the matching state, the first pass's aggregates and
     // their Galerkin matrix
     DevBuf mate, best, claim, mflag, mid, join, agg1, agg2, mp1, mem1, mfill, rp1, ci1, va1, dinv1, part, counts;
