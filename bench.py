@@ -12,6 +12,10 @@ line search of ma_ot_solve).  ``value`` = OT solves/s with the inputs resident i
 device memory; ``e2e`` = the same through the C ABI with host buffers (host->device
 copy of sites, masses and initial weights, device->host copy of the weights inside
 the timed region).  L2 is flushed (a 512 MB write) before every timed step.
+Beside the C2 line, rank 0 reports the clustered 1M-site workload (workloads.c3):
+complete evaluations at w = 0 in FP64 and in the mixed form (``c3_evaluations``) and
+one complete solve of each form from w = 0, each with its own clock record
+(``c3_solves``, about 3 minutes; ``--no-c3-solves`` leaves it out).
 
 ``--impl reference`` times the reference algorithm's CPU restatement (oracle/) on
 the host cores instead.  It first solves the workload once with it (FP64 evaluations,
@@ -242,42 +246,21 @@ def c3_evaluations(ctx, dev, steps, warmup):
     return out
 
 
-def run_c3(args, ctx, dev, rank):
-    """Mixed precision against FP64 on the clustered 1M-site workload (workloads.c3:
-    2048^2 grid U[0.5,1.5], 1,000,000 sites, 70% in 20 Gaussian blobs, equal masses):
-    (a) complete Laguerre evaluations at w = 0, evaluations/s of each form; (b) one
-    complete OT solve of each form from w = 0 to max relative mass error 1e-6, by the
-    continuation in the target masses (MA_INIT_CONTINUATION: the reference's damped
-    Newton from w = 0 cuts every step to a few 2^-11 on these sites), each timed with its
-    own clock record; (c) the mixed solution's errors against the FP64 evaluation (which
+def c3_solves(ctx, dev, p=None):
+    """One complete OT solve of the clustered 1M-site workload (workloads.c3) in each
+    form, FP64 and mixed, from w = 0 to max relative mass error 1e-6 by the continuation
+    in the target masses (MA_INIT_CONTINUATION), each timed with CUDA events and its own
+    clock record; then the mixed solution's errors against the FP64 evaluation (which
     the tests pin to the oracle at this size): weights, masses and every Hessian entry."""
     import numpy as np
     import torch
 
     from mongeampere_gb300 import api
     from mongeampere_gb300 import workloads as W
-    out = {"metric": METRIC, "workload": "c3", "n_gpus": 1,
-           "config": "1,000,000 sites (70% in 20 Gaussian blobs), 2048^2 grid U[0.5,1.5], equal masses, "
-                     "inputs in device memory"}
-    p = W.c3(0)
+    p = p if p is not None else W.c3(0)
     dm = ctx.mesh(p.mesh)
     X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
     nu = torch.tensor(p.nu, device=dev)
-    w0 = torch.zeros(p.n, dtype=torch.float64, device=dev)
-    ev = {}
-    for prec in ("fp64", "mixed"):
-        for _ in range(max(args.warmup, 1)):
-            api.kantorovich(dm, X, w0, precision=prec, ctx=ctx)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record()
-        for _ in range(args.steps):
-            api.kantorovich(dm, X, w0, precision=prec, ctx=ctx)
-        e1.record()
-        torch.cuda.synchronize()
-        ev[prec] = args.steps / (e0.elapsed_time(e1) * 1e-3)
-    out["evaluations_at_w0"] = {"fp64_evals_per_s": ev["fp64"], "mixed_evals_per_s": ev["mixed"],
-                                "mixed_speedup": ev["mixed"] / ev["fp64"]}
     solves, wsol = {}, {}
     for prec in ("fp64", "mixed"):
         w = torch.zeros(p.n, dtype=torch.float64, device=dev)
@@ -307,14 +290,53 @@ def run_c3(args, ctx, dev, rank):
     wm, wd = wsol["mixed"].cpu().numpy(), wsol["fp64"].cpu().numpy()
     same = bool(np.array_equal(h32.col, h64.col))
     hrel = float(np.max(np.abs(h32.val - h64.val) / np.abs(h64.val))) if same else None
-    out["solve"] = {"fp64": solves["fp64"], "mixed": solves["mixed"],
-                    "mixed_speedup": solves["fp64"]["seconds"] / solves["mixed"]["seconds"],
-                    "mixed_solution_fp64_mass_rel_err_max": float(np.max(np.abs(g64n - p.nu) / p.nu)),
-                    "mixed_vs_fp64_weights_max_abs_diff": float(np.max(np.abs(wm - wd))),
-                    "weights_scale": float(np.max(np.abs(wd))),
-                    "mixed_eval_mass_rel_err_max": float(np.max(np.abs(g32n - g64n) / g64n)),
-                    "mixed_eval_value_rel_err": float(abs(v32 - v64) / abs(v64)),
-                    "mixed_eval_hessian_entry_rel_err_max": hrel, "same_sparsity": same}
+    return {"config": "1,000,000 sites (70% in 20 Gaussian blobs), 2048^2 grid U[0.5,1.5], equal masses, "
+                      "from w = 0 to max rel mass err 1e-6, inputs in device memory",
+            "fp64": solves["fp64"], "mixed": solves["mixed"],
+            "mixed_speedup": solves["fp64"]["seconds"] / solves["mixed"]["seconds"],
+            "mixed_solution_fp64_mass_rel_err_max": float(np.max(np.abs(g64n - p.nu) / p.nu)),
+            "mixed_vs_fp64_weights_max_abs_diff": float(np.max(np.abs(wm - wd))),
+            "weights_scale": float(np.max(np.abs(wd))),
+            "mixed_eval_mass_rel_err_max": float(np.max(np.abs(g32n - g64n) / g64n)),
+            "mixed_eval_value_rel_err": float(abs(v32 - v64) / abs(v64)),
+            "mixed_eval_hessian_entry_rel_err_max": hrel, "same_sparsity": same}
+
+
+def run_c3(args, ctx, dev, rank):
+    """Mixed precision against FP64 on the clustered 1M-site workload (workloads.c3:
+    2048^2 grid U[0.5,1.5], 1,000,000 sites, 70% in 20 Gaussian blobs, equal masses):
+    (a) complete Laguerre evaluations at w = 0, evaluations/s of each form; (b) one
+    complete OT solve of each form from w = 0 to max relative mass error 1e-6, by the
+    continuation in the target masses (MA_INIT_CONTINUATION: the reference's damped
+    Newton from w = 0 cuts every step to a few 2^-11 on these sites), each timed with its
+    own clock record; (c) the mixed solution's errors against the FP64 evaluation (which
+    the tests pin to the oracle at this size): weights, masses and every Hessian entry."""
+    import torch
+
+    from mongeampere_gb300 import api
+    from mongeampere_gb300 import workloads as W
+    out = {"metric": METRIC, "workload": "c3", "n_gpus": 1,
+           "config": "1,000,000 sites (70% in 20 Gaussian blobs), 2048^2 grid U[0.5,1.5], equal masses, "
+                     "inputs in device memory"}
+    p = W.c3(0)
+    dm = ctx.mesh(p.mesh)
+    X = torch.stack([torch.tensor(p.x, device=dev), torch.tensor(p.y, device=dev)], 1)
+    w0 = torch.zeros(p.n, dtype=torch.float64, device=dev)
+    ev = {}
+    for prec in ("fp64", "mixed"):
+        for _ in range(max(args.warmup, 1)):
+            api.kantorovich(dm, X, w0, precision=prec, ctx=ctx)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            api.kantorovich(dm, X, w0, precision=prec, ctx=ctx)
+        e1.record()
+        torch.cuda.synchronize()
+        ev[prec] = args.steps / (e0.elapsed_time(e1) * 1e-3)
+    out["evaluations_at_w0"] = {"fp64_evals_per_s": ev["fp64"], "mixed_evals_per_s": ev["mixed"],
+                                "mixed_speedup": ev["mixed"] / ev["fp64"]}
+    out["solve"] = c3_solves(ctx, dev, p)
     if rank == 0:
         print(json.dumps(out))
 
@@ -522,6 +544,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c3", action="store_true", help="leave out the 1M-site FP64 / mixed evaluations")
+    ap.add_argument("--no-c3-solves", action="store_true",
+                    help="leave out the 1M-site FP64 and mixed complete solves (about 3 minutes)")
     ap.add_argument("--profile-evals", type=int, default=0,
                     help="profiling driver: solve once, then run this many Laguerre evaluations at the "
                          "solution weights and print per-kernel device times (no benchmark line)")
@@ -709,6 +733,12 @@ def main():
     c3 = None
     if rank == 0 and not args.no_c3:
         c3 = c3_evaluations(ctx, dev, max(args.steps, 3), 2)
+    c3s = None
+    if rank == 0 and not args.no_c3_solves:
+        try:
+            c3s = c3_solves(ctx, dev)
+        except Exception as exc:  # the C2 line stands without it
+            c3s = {"error": f"{type(exc).__name__}: {exc}"}
 
     # ---- e2e through the C ABI with host buffers ----
     xh = torch.tensor(p.x).pin_memory().numpy()
@@ -749,6 +779,7 @@ def main():
         "roofline": roofline,
         "solve_roofline": solve_roofline,
         "c3_evaluations": c3,
+        "c3_solves": c3s,
         "clocks": clk,
         "gpu_launches": launches,
     }

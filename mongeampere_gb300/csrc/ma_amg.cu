@@ -1385,7 +1385,10 @@ ma_status amg_pcg_solve(Ctx* c, int n, const double* b, double* x, double rtol, 
         dyn = sm_bytes / bps - 1024 - (int)fa.sharedSizeBytes;
         dyn = std::min(dyn, optin - (int)fa.sharedSizeBytes);
         dyn = std::max(0, dyn) & ~15;
-        MA_CUDA(c, cudaFuncSetAttribute(k_pcg_amg, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+        // the attribute at the largest size any launch asks for, so that contexts with
+        // different launch shapes never race on it
+        MA_CUDA(c, cudaFuncSetAttribute(k_pcg_amg, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        std::max(0, optin - (int)fa.sharedSizeBytes)));
         MA_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_amg, bthreads, dyn));
         if (per_sm < 1) return fail(c, MA_ERR_CUDA, "the multigrid PCG kernel does not fit an SM");
         max_blocks = std::min(per_sm, bps) * sms;
