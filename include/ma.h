@@ -198,7 +198,8 @@ typedef struct ma_stats {
     size_t linesearch_halvings;
     double grad_norm;            /* |m - nu|_2 at exit */
     double max_rel_err;          /* max_i |m_i - nu_i| / nu_i at exit */
-    double value;                /* Kantorovich value minus <nu, w> at exit */
+    double value;                /* Kantorovich value minus <nu, w> at exit (NaN after
+                                    MA_LINESEARCH_FAIL) */
     double t_eval_ms;            /* device time spent in Laguerre evaluations */
     double t_linsolve_ms;        /* device time spent in linear solves */
     size_t neval_fp64;           /* evaluations with FP64 integrals (all of them unless precision

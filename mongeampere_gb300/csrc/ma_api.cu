@@ -231,6 +231,7 @@ ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlag
     a.Y1 = m->Y1;
     a.mass = c->mass.as<double>();
     a.vpart = c->vpart.as<double>();
+    a.value = f.value ? 1 : 0;
     a.mom = f.moments > 0 ? c->mom.as<double>() : nullptr;
     a.rowcnt = c->rowcnt.as<int>();
     a.st_col = c->st_col.as<int>();

@@ -558,9 +558,11 @@ struct Acc {
 // length * rho(mid) / (2 |x_i - x_j|), with length = |e x d| / |d|).
 // The polygon is given by its edge labels lab(0..n-1); edge(k, slot, v) receives the
 // Hessian part v of edge k when that edge lies on the radical axis of `slot`.
+// value = false leaves out int rho |u|^2 (acc.second stays 0): a Newton solve's
+// evaluations need the value only at its end.
 template <bool MOM, class Lab, class Edge>
 MA_HD void integrate_labels(int n, const Lab& lab_of, const Nb64* nb, const Fixed& fx, double c0, double gx,
-                            double gy, Acc& acc, const Edge& edge)
+                            double gy, Acc& acc, const Edge& edge, bool value = true)
 {
     double x0, y0;
     vtx64(lab_of(n - 1), lab_of(0), nb, fx, x0, y0);
@@ -577,14 +579,16 @@ MA_HD void integrate_labels(int n, const Lab& lab_of, const Nb64* nb, const Fixe
             by = y0;
         }
         double cr = ax * by - ay * bx;
-        double aa = ax * ax + ay * ay, ab = ax * bx + ay * by, bb = bx * bx + by * by;
         m0 += cr;
         m1x += cr * (ax + bx);
         m1y += cr * (ay + by);
-        q2 += cr * (aa + ab + bb);
-        double ka = 3.0 * aa + 2.0 * ab + bb, kb = aa + 2.0 * ab + 3.0 * bb;
-        c3x += cr * (ax * ka + bx * kb);
-        c3y += cr * (ay * ka + by * kb);
+        if (value) {
+            double aa = ax * ax + ay * ay, ab = ax * bx + ay * by, bb = bx * bx + by * by;
+            q2 += cr * (aa + ab + bb);
+            double ka = 3.0 * aa + 2.0 * ab + bb, kb = aa + 2.0 * ab + 3.0 * bb;
+            c3x += cr * (ax * ka + bx * kb);
+            c3y += cr * (ay * ka + by * kb);
+        }
         if (MOM) {
             sxx += cr * (2.0 * (ax * ax + bx * bx) + 2.0 * ax * bx);
             syy += cr * (2.0 * (ay * ay + by * by) + 2.0 * ay * by);

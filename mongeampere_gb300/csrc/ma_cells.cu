@@ -1597,7 +1597,7 @@ __global__ void __launch_bounds__(32 * kPieceWarps, 7) k_pieces(CellArgs A, E me
                 Acc acc{0, 0, 0, 0, 0, 0, 0};
                 integrate_labels<MOM>(
                     (int)R.n, [&](int e) { return (int)R.lab[e]; }, W.nb + C.soff, T, c0, gx, gy, acc,
-                    [&](int e, int, double v) { W.hvc[e][p] = v; });
+                    [&](int e, int, double v) { W.hvc[e][p] = v; }, MOM || A.value != 0);
                 W.out[0][p] = acc.mass;
                 W.out[1][p] = acc.second;
                 if (MOM) {

@@ -59,6 +59,8 @@ struct CellArgs {
     // outputs, original order
     double* mass;
     double* vpart;           // w_i m_i - int_{cell i} rho |x - x_i|^2
+    int value = 1;           // 0: the grid-piece integrals leave out int rho |x - x_i|^2
+                             // (vpart then holds w_i m_i only)
     double* mom;             // 6 per site or null: rho, rho x, rho y, rho x^2, rho y^2, rho x y
     int* rowcnt;
     int* st_col;

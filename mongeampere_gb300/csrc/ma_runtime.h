@@ -195,6 +195,9 @@ struct EvalFlags {
     // is below eps0 > 0), so the evaluation stops at the first one and sets
     // Ctx::aborted instead of computing the rest
     bool abort_on_empty = false;
+    // the Kantorovich value's integrals (int rho |x - x_i|^2, a third of an FP64 piece's
+    // edge terms): a Newton solve needs the value of its last evaluation only
+    bool value = true;
 };
 ma_status run_eval(Ctx* c, const Mesh* m, int n, const double* w, const EvalFlags& f);
 // Newton linear solve H[:n-1,:n-1] x = b with the multigrid-preconditioned CG (ma_amg.cu);

@@ -343,14 +343,27 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
     // FP64.  Above it the noise cannot decide a line search; a mixed line search that
     // fails all the same is redone in FP64.
     constexpr double kMixedFloor = 1e-2;
-    auto timed_eval = [&](const double* wv, bool trial) -> ma_status {
+    // Only the value of the last evaluation is reported, so the FP64 evaluations leave
+    // out the value's integrals (a third of a piece's FP64 edge terms) until the
+    // accepted point is within kValueNear of the stopping tolerance; the first
+    // evaluation has them (an empty cell there ends the solve with its value), the
+    // mixed integrals always do, and a solve whose last evaluation lacks them ends
+    // with one FP64 evaluation of the final weights.  fx_valid: fx is the value.
+    constexpr double kValueNear = 1e3;
+    bool fx_valid = false;
+    auto near_end = [&](double gn, double mr) {
+        return o.stop_rule == MA_STOP_MAX_REL ? (mr <= kValueNear * o.eps_g) : (gn <= kValueNear * o.eps_g);
+    };
+    auto timed_eval = [&](const double* wv, bool trial, bool value) -> ma_status {
         cudaEventRecord(e0, s);
         EvalFlags f;
         f.hessian = true;
         f.nu = dnu;
         f.abort_on_empty = trial;
         f.mixed = mixed_phase;
-        if (!mixed_phase) S.neval_fp64++;
+        f.value = value;
+        fx_valid = value || f.mixed;
+        if (!f.mixed) S.neval_fp64++;
         ma_status r = run_eval(c, m, n, wv, f);
         if (r != MA_OK) return r;
         cudaEventRecord(e1, s);
@@ -379,7 +392,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
     k_min_nu<<<1, 256, 0, s>>>(dnu, n, c->cg_scal.as<double>() + 7);
     c->launches += 1;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat + 15, c->cg_scal.as<double>() + 7, sizeof(double), cudaMemcpyDeviceToHost, s));
-    if ((st = timed_eval(w, false)) != MA_OK) {
+    if ((st = timed_eval(w, false, true)) != MA_OK) {
         result = st;
         goto core_done;
     }
@@ -400,7 +413,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
                 if (!mixed_phase || (!fp64_finish && converged(gn, mr))) break;
                 // the mixed residual has converged: check (and finish) in FP64
                 mixed_phase = false;
-                if ((st = timed_eval(w, false)) != MA_OK) {
+                if ((st = timed_eval(w, false, true)) != MA_OK) {
                     result = st;
                     break;
                 }
@@ -446,12 +459,13 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
             if (!(rr <= rtol * (1.0 + 1e-12))) S.cg_noconv++;  // rr = |r| / |g| of the direction
             MA_CUDA(c, cudaMemcpyAsync(c->w0.p, w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
             double alpha = 1.0, n0 = gn;
+            const bool want_value = near_end(gn, mr);
             bool ok = false;
             while (true) {
                 // w = w0 - alpha * solution
                 k_axpy_to<<<(n + 255) / 256, 256, 0, s>>>(c->w0.as<double>(), c->dirn.as<double>(), -alpha, n, w);
                 c->launches += 1;
-                if ((st = timed_eval(w, true)) != MA_OK) {
+                if ((st = timed_eval(w, true, want_value)) != MA_OK) {
                     result = st;
                     break;
                 }
@@ -474,7 +488,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
                 // the mixed residual is at its noise level: redo this step in FP64
                 mixed_phase = false;
                 MA_CUDA(c, cudaMemcpyAsync(w, c->w0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-                if ((st = timed_eval(w, false)) != MA_OK) {
+                if ((st = timed_eval(w, false, true)) != MA_OK) {
                     result = st;
                     break;
                 }
@@ -489,13 +503,23 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
                 break;
             }
             if (o.verbose)
-                fprintf(stderr, "it %lld: f=%.17g |df|=%.17g max_rel=%.3g tau=%g eval=%zu cg=%d\n", (long long)niter, fx,
-                        gn, mr, alpha, S.neval, it);
+                fprintf(stderr, "it %lld: |df|=%.17g max_rel=%.3g tau=%g eval=%zu cg=%d\n", (long long)niter, gn, mr,
+                        alpha, S.neval, it);
         }
         S.niter = (size_t)niter;
         S.grad_norm = gn;
         S.max_rel_err = mr;
-        S.value = fx;
+        if (!fx_valid && (result == MA_OK || result == MA_MAXITER)) {
+            // the value at the final weights: the same weights evaluated again, in FP64
+            // and with the value's integrals
+            mixed_phase = false;
+            if ((st = timed_eval(w, false, true)) != MA_OK) {
+                result = st;
+                goto core_done;
+            }
+            fx = c->hstat[0];
+        }
+        S.value = fx_valid ? fx : NAN;  // no value after a failed line search
     }
 core_done:
     cudaEventDestroy(e0);
