@@ -318,8 +318,12 @@ constexpr int kAggRefresh = 8;  // Newton steps per multigrid aggregation (the s
 
 // fp64_finish = false: a mixed-precision solve may stop on its mixed residual (the
 // intermediate stages of the continuation, whose tolerance is far above the FP32 noise)
+// report_value = false: a stage whose value nobody reads (a continuation stage before
+// the last, a coarse multiscale level); its evaluations leave out the value's integrals
+// and S.value is NaN.
 static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, const double* dy, const double* dnu,
-                             double* w, const ma_solve_opts& o, ma_stats& S, bool fp64_finish = true)
+                             double* w, const ma_solve_opts& o, ma_stats& S, bool fp64_finish = true,
+                             bool report_value = true)
 {
     cudaStream_t s = c->stream;
     const bool default_forcing = !(o.cg_rtol > 0);
@@ -392,7 +396,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
     k_min_nu<<<1, 256, 0, s>>>(dnu, n, c->cg_scal.as<double>() + 7);
     c->launches += 1;
     MA_CUDA(c, cudaMemcpyAsync(c->hstat + 15, c->cg_scal.as<double>() + 7, sizeof(double), cudaMemcpyDeviceToHost, s));
-    if ((st = timed_eval(w, false, true)) != MA_OK) {
+    if ((st = timed_eval(w, false, report_value)) != MA_OK) {
         result = st;
         goto core_done;
     }
@@ -404,7 +408,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
             result = fail(c, MA_EMPTY_CELL, "computed minimum mass is non-positive: a Laguerre cell is empty");
             S.grad_norm = gn;
             S.max_rel_err = mr;
-            S.value = fx;
+            S.value = fx_valid ? fx : NAN;
             goto core_done;
         }
         int64_t niter = 0;
@@ -413,7 +417,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
                 if (!mixed_phase || (!fp64_finish && converged(gn, mr))) break;
                 // the mixed residual has converged: check (and finish) in FP64
                 mixed_phase = false;
-                if ((st = timed_eval(w, false, true)) != MA_OK) {
+                if ((st = timed_eval(w, false, report_value)) != MA_OK) {
                     result = st;
                     break;
                 }
@@ -459,7 +463,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
             if (!(rr <= rtol * (1.0 + 1e-12))) S.cg_noconv++;  // rr = |r| / |g| of the direction
             MA_CUDA(c, cudaMemcpyAsync(c->w0.p, w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
             double alpha = 1.0, n0 = gn;
-            const bool want_value = near_end(gn, mr);
+            const bool want_value = report_value && near_end(gn, mr);
             bool ok = false;
             while (true) {
                 // w = w0 - alpha * solution
@@ -488,7 +492,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
                 // the mixed residual is at its noise level: redo this step in FP64
                 mixed_phase = false;
                 MA_CUDA(c, cudaMemcpyAsync(w, c->w0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-                if ((st = timed_eval(w, false, true)) != MA_OK) {
+                if ((st = timed_eval(w, false, report_value)) != MA_OK) {
                     result = st;
                     break;
                 }
@@ -509,7 +513,7 @@ static ma_status newton_core(Ctx* c, const Mesh* m, int n, const double* dx, con
         S.niter = (size_t)niter;
         S.grad_norm = gn;
         S.max_rel_err = mr;
-        if (!fx_valid && (result == MA_OK || result == MA_MAXITER)) {
+        if (report_value && !fx_valid && (result == MA_OK || result == MA_MAXITER)) {
             // the value at the final weights: the same weights evaluated again, in FP64
             // and with the value's integrals
             mixed_phase = false;
@@ -664,7 +668,7 @@ static ma_status multiscale_solve(Ctx* c, const Mesh* m, int n, const double* dx
             ol.verbose = 0;
         }
         ma_stats Sl{};
-        ma_status st = newton_core(c, m, nl, lx, ly, lnu, lw, ol, Sl);
+        ma_status st = newton_core(c, m, nl, lx, ly, lnu, lw, ol, Sl, true, l == 0);
         if (o.verbose)
             fprintf(stderr, "multiscale level %d: %d sites, guess scale %g, status %d, %zu Newton steps, max_rel %.3g\n",
                     l, nl, t, (int)st, Sl.niter, Sl.max_rel_err);
@@ -770,7 +774,7 @@ static ma_status continuation_solve(Ctx* c, const Mesh* m, int n, const double* 
             os.maxiter = o.maxiter * kContStageIters;
         }
         ma_stats Sl{};
-        st = newton_core(c, m, n, dx, dy, target, w, os, Sl, last);
+        st = newton_core(c, m, n, dx, dy, target, w, os, Sl, last, last);
         if (o.verbose)
             fprintf(stderr, "continuation stage %d: t = %.6g, status %d, %zu Newton steps, %zu evaluations, max_rel %.3g\n",
                     stage, tn, (int)st, Sl.niter, Sl.neval, Sl.max_rel_err);
