@@ -439,13 +439,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_level_setup(SetupArgs a)
 __global__ void __launch_bounds__(256) k_dense_inverse(const int* rp, const int* ci, const double* va,
                                                        const double* dinv, int n, double* inv)
 {
-    // elements over the padded kCoarsest x kCoarsest square (row t / kCoarsest and column
-    // t % kCoarsest are shifts), the pivot's reciprocal taken once per step
-    static_assert((kCoarsest & (kCoarsest - 1)) == 0, "kCoarsest is a power of two");
     __shared__ double a[kCoarsest][kCoarsest + 1];
-    __shared__ double fcol[kCoarsest];
-    __shared__ double piv;
-    for (int t = threadIdx.x; t < kCoarsest * kCoarsest; t += blockDim.x) a[t / kCoarsest][t % kCoarsest] = 0.0;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) a[t / n][t % n] = 0.0;
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         if (dinv[i] == 0.0) {
@@ -456,18 +451,18 @@ __global__ void __launch_bounds__(256) k_dense_inverse(const int* rp, const int*
             if (dinv[ci[k]] != 0.0) a[i][ci[k]] = va[k];
     }
     __syncthreads();
+    __shared__ double fcol[kCoarsest];
     for (int k = 0; k < n; k++) {
-        if (threadIdx.x == 0) piv = 1.0 / a[k][k];
+        const double p = 1.0 / a[k][k];
         // the multipliers of column k, read before any row changes
         for (int i = threadIdx.x; i < n; i += blockDim.x) fcol[i] = a[i][k];
         __syncthreads();
-        const double p = piv;
         // row k scaled (with the pivot position replaced by 1 first)
         for (int j = threadIdx.x; j < n; j += blockDim.x) a[k][j] = (j == k ? 1.0 : a[k][j]) * p;
         __syncthreads();
-        for (int t = threadIdx.x; t < kCoarsest * kCoarsest; t += blockDim.x) {
-            const int i = t / kCoarsest, j = t % kCoarsest;
-            if (i >= n || j >= n || i == k) continue;
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int i = t / n, j = t % n;
+            if (i == k) continue;
             const double f = fcol[i];
             if (j == k)
                 a[i][j] = -f * a[k][k];
@@ -476,10 +471,9 @@ __global__ void __launch_bounds__(256) k_dense_inverse(const int* rp, const int*
         }
         __syncthreads();
     }
-    for (int t = threadIdx.x; t < kCoarsest * kCoarsest; t += blockDim.x) {
-        const int i = t / kCoarsest, j = t % kCoarsest;
-        if (i >= n || j >= n) continue;
-        inv[i * n + j] = (dinv[i] == 0.0 || dinv[j] == 0.0) ? 0.0 : a[i][j];
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int i = t / n, j = t % n;
+        inv[t] = (dinv[i] == 0.0 || dinv[j] == 0.0) ? 0.0 : a[i][j];
     }
 }
 
